@@ -1,0 +1,239 @@
+/*
+ * sequoia_gpu.h -- C ABI of the GB300 BVH build and ray-trace library
+ * (libsequoia_gpu.so).
+ *
+ * This header is the drop-in boundary for Sequoia's build/trace path.  Every
+ * entry point names the reference interface it replaces (paths are relative
+ * to the Sequoia source tree).  Plain pointers and sizes only: no C++, no
+ * torch, no CUDA types in the signatures (a CUDA stream is passed as void*).
+ *
+ * Memory: every pointer argument may be host memory (pageable or pinned) or
+ * device memory of the context's GPU; the library detects which and copies
+ * as needed.  Calls whose outputs are all device pointers are asynchronous on
+ * the context stream; calls with a host output synchronise before returning.
+ *
+ * Errors: every call returns sq_status; sq_last_error() gives the message of
+ * the last failing call on that context.  Kernels never spin without a bound:
+ * a bounded wait that expires, or a traversal stack that would overflow,
+ * raises a device error word that the next synchronising call reports as
+ * SQ_ERR_DEVICE.
+ *
+ * Threading: one context is single-threaded; different contexts are
+ * independent and may be used from different host threads.
+ */
+#ifndef SEQUOIA_GPU_H
+#define SEQUOIA_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SQ_ABI_VERSION 1u
+
+typedef enum sq_status {
+    SQ_OK = 0,
+    SQ_ERR_INVALID = 1,     /* bad argument (null pointer, size, mode)        */
+    SQ_ERR_CUDA = 2,        /* a CUDA runtime call failed                     */
+    SQ_ERR_OOM = 3,         /* device or pinned allocation failed             */
+    SQ_ERR_DEVICE = 4,      /* a kernel raised the device error word          */
+    SQ_ERR_UNSUPPORTED = 5, /* valid request this build does not implement    */
+    SQ_ERR_NO_DEVICE = 6    /* no CUDA device / extension unusable            */
+} sq_status;
+
+/* Device error word bits (sq_device_error) */
+#define SQ_DEVERR_STACK_OVERFLOW   0x1u  /* traversal stack limit reached          */
+#define SQ_DEVERR_LOOKBACK_TIMEOUT 0x2u  /* radix-sort look-back wait ran out       */
+#define SQ_DEVERR_TOPOLOGY         0x4u  /* LBVH climb found an inconsistent state  */
+#define SQ_DEVERR_SAH_QUEUE        0x8u  /* SAH task queue overflow / wait ran out  */
+#define SQ_DEVERR_NODE_COUNT       0x10u /* a node would hold more than 65535 prims */
+
+typedef struct sq_ctx sq_ctx;
+typedef struct sq_bvh sq_bvh;
+
+/* Same 36-byte layout as Sequoia's Triangle (src/aabb.h:17-24). */
+typedef struct sq_triangle {
+    float v0[3];
+    float v1[3];
+    float v2[3];
+} sq_triangle;
+
+/* Same 32-byte layout as Sequoia's Node1 (src/aabb.h:34-42).  A leaf has
+ * flags == SQ_NODE_LEAF, count == 1 and child == triangle index; an internal
+ * node has children [child, child + count).                                  */
+typedef struct sq_node1 {
+    float min[3];
+    uint16_t count;
+    uint16_t flags;
+    float max[3];
+    uint32_t child;
+} sq_node1;
+#define SQ_NODE_LEAF 1u
+
+/* Same 32-byte layout as Sequoia's Ray<1> (src/ray.h:8-14). */
+typedef struct sq_ray {
+    float origin[3];
+    float tmin;
+    float dir[3];
+    float tmax;
+} sq_ray;
+
+/* One record per ray. id == SQ_NO_HIT when nothing was hit.  In SQ_TRACE_REF
+ * mode id is 0 (hit) or SQ_NO_HIT (miss) and t is 0, because the reference
+ * tracer keeps only a hit flag (src/tracer.h:112-115).                        */
+typedef struct sq_hit {
+    uint32_t id;
+    float t;
+    uint32_t tests; /* ray-box tests performed: the heatmap counter           */
+} sq_hit;
+#define SQ_NO_HIT 0xFFFFFFFFu
+
+typedef struct sq_options {
+    int device;      /* CUDA device ordinal                                  */
+    void* stream;    /* cudaStream_t to run on; NULL = context-owned stream  */
+    uint32_t flags;  /* reserved, 0                                          */
+} sq_options;
+
+typedef enum sq_builder_kind {
+    SQ_BUILDER_MORTON = 0, /* Builder::build_hierarchy_morton (src/builder.cpp:2474) */
+    SQ_BUILDER_SAH = 1,    /* Builder::build_hierarchy        (src/builder.cpp:1576) */
+    SQ_BUILDER_GRID = 2    /* Builder::build_hierarchy_grid   (src/builder.cpp:2133) */
+} sq_builder_kind;
+
+/* Morton quantisation domain.  PRIMITIVE follows the reference: codes are
+ * normalised by the union of the triangle AABBs (src/builder.cpp:2206-2215).
+ * CENTROID normalises by the bounds of the centroids.                        */
+#define SQ_MORTON_BOUNDS_PRIMITIVE 0u
+#define SQ_MORTON_BOUNDS_CENTROID 1u
+
+/* build flags */
+#define SQ_BUILD_GRID_SCENE_BOUNDS 0x1u /* grid: give cell nodes the scene box,
+                                           as the plain reference grid builder
+                                           does (src/builder.cpp:2173-2174)      */
+
+typedef struct sq_build_params {
+    uint32_t kind;            /* sq_builder_kind                                  */
+    uint32_t sah_bins;        /* SAH/grid bins: 8, 16 or 32 (0 = 8)               */
+    uint32_t leaf_size;       /* SAH/grid: leaf when count <= leaf_size (0 = 8)   */
+    uint32_t sort_digit_bits; /* Morton sort digit width 6, 8 or 10 (0 = 8)       */
+    uint32_t morton_bounds;   /* SQ_MORTON_BOUNDS_*                               */
+    uint32_t flags;           /* SQ_BUILD_*                                       */
+} sq_build_params;
+
+typedef struct sq_bvh_info {
+    uint32_t node_capacity;   /* entries in the node array                        */
+    uint32_t root;            /* root node index                                  */
+    uint32_t tri_count;
+    uint32_t kind;            /* sq_builder_kind, or 0xFFFFFFFF for imported trees */
+    float scene_min[3];
+    float scene_max[3];
+} sq_bvh_info;
+
+typedef enum sq_trace_mode {
+    SQ_TRACE_REF = 0,     /* the reference tracer: every box test counted, no
+                             near-child order, no early exit, Moller-Trumbore
+                             hit flag (src/tracer.cpp:47-65, src/tracer.h:12-116) */
+    SQ_TRACE_CLOSEST = 1, /* near-child order, t shrink, watertight test         */
+    SQ_TRACE_ANYHIT = 2   /* as CLOSEST, stops at the first accepted hit         */
+} sq_trace_mode;
+
+typedef enum sq_ray_kind {
+    SQ_RAYS_REFERENCE_CAMERA = 0, /* trace()'s camera (src/tracer.cpp:202-216)   */
+    SQ_RAYS_PINHOLE = 1,          /* eye / look-at / vertical FOV pinhole        */
+    SQ_RAYS_EXPLICIT = 2          /* caller-supplied sq_ray array                */
+} sq_ray_kind;
+
+typedef struct sq_ray_source {
+    uint32_t kind;     /* sq_ray_kind                                         */
+    uint32_t width;    /* camera kinds: image size; ray i = y * width + x     */
+    uint32_t height;
+    float origin[3];   /* REFERENCE_CAMERA: camera position; PINHOLE: eye     */
+    float target[3];   /* PINHOLE: look-at point                              */
+    float up[3];       /* PINHOLE: up vector                                  */
+    float vfov_deg;    /* PINHOLE: vertical field of view in degrees          */
+    const sq_ray* rays;/* EXPLICIT: host or device array                      */
+    uint32_t ray_count;/* EXPLICIT: number of rays                            */
+} sq_ray_source;
+
+/* ---- context ------------------------------------------------------------ */
+
+/* No reference counterpart: the reference is a global OpenMP program.       */
+sq_status sq_create(sq_ctx** out, const sq_options* options);
+sq_status sq_destroy(sq_ctx* ctx);
+const char* sq_last_error(const sq_ctx* ctx);
+uint32_t sq_abi_version(void);
+/* Wait for all work on the context stream, then report and clear the device
+ * error word (SQ_ERR_DEVICE if it was set; the bits go to *device_error).    */
+sq_status sq_sync(sq_ctx* ctx, uint32_t* device_error);
+
+/* ---- build -------------------------------------------------------------- */
+
+/* Replaces Builder::build_hierarchy, build_hierarchy_morton and
+ * build_hierarchy_grid (src/builder.h:85-94, src/builder.cpp:1576, 2474,
+ * 2133).  tris: n triangles, host or device.  A device tris pointer is
+ * referenced, not copied, exactly as Hierarchy::tri_base references the
+ * caller's vector (src/builder.cpp:1613): it must outlive the BVH.  The BVH
+ * lives on the device until sq_bvh_free.                                      */
+sq_status sq_build(sq_ctx* ctx, const sq_triangle* tris, uint32_t n,
+                   const sq_build_params* params, sq_bvh** out);
+sq_status sq_bvh_free(sq_bvh* bvh);
+sq_status sq_bvh_get_info(const sq_bvh* bvh, sq_bvh_info* info);
+
+/* Copy the node array out in Sequoia's Node1 layout so that the reference's
+ * traverse() (src/tracer.cpp:47) can walk a GPU-built tree.  nodes may be host
+ * or device; cap is its capacity in entries.                                 */
+sq_status sq_bvh_export_node1(sq_bvh* bvh, sq_node1* nodes, uint32_t cap,
+                              uint32_t* node_count, uint32_t* root);
+
+/* Upload a Node1 tree built elsewhere (the reference's Hierarchy: node_base,
+ * node_count, root_index, tri_base; src/aabb.h:197-205) so the GPU traverses
+ * exactly that tree.  Triangles are copied to the device.                    */
+sq_status sq_bvh_import_node1(sq_ctx* ctx, const sq_node1* nodes,
+                              uint32_t node_count, uint32_t root,
+                              const sq_triangle* tris, uint32_t n,
+                              sq_bvh** out);
+
+/* Build stages, exposed for parity checks and for callers that want only a
+ * stage.  Replaces setup_morton + bit_interleave_32 (src/builder.cpp:2204-
+ * 2237, src/algorithms.cpp:8-14): codes[i] is the 30-bit Morton code of
+ * triangle i; scene_box receives {min xyz, max xyz} of the quantisation box. */
+sq_status sq_morton_codes(sq_ctx* ctx, const sq_triangle* tris, uint32_t n,
+                          uint32_t bounds_mode, uint32_t* codes,
+                          float* scene_box);
+
+/* Replaces radix_sort<uint32_t, RadixInput32> (src/algorithms.h:89-113):
+ * stable ascending sort of (key, value) pairs by key over the low key_bits
+ * bits (1..32), onesweep with decoupled look-back.  keys_out / values_out
+ * may alias keys_in / values_in.                                            */
+sq_status sq_radix_sort_pairs(sq_ctx* ctx, const uint32_t* keys_in,
+                              const uint32_t* values_in, uint32_t n,
+                              uint32_t key_bits, uint32_t digit_bits,
+                              uint32_t* keys_out, uint32_t* values_out);
+
+/* The sorted Morton codes and triangle permutation of the last Morton build
+ * of this BVH (n entries each).                                              */
+sq_status sq_bvh_export_sorted(sq_bvh* bvh, uint32_t* codes, uint32_t* perm);
+
+/* ---- trace -------------------------------------------------------------- */
+
+/* Replaces trace() and traverse() (src/tracer.h:118-135,
+ * src/tracer.cpp:47-65, 195-230).  hits: one sq_hit per ray (may be NULL);
+ * heatmap_rgb: width*height*3 bytes, byte = (uint8)(min(1, tests/200)*255)
+ * in all three channels as in src/tracer.cpp:222-225 (may be NULL; for
+ * explicit rays it holds ray_count*3 bytes).  Outputs host or device.        */
+sq_status sq_trace(sq_ctx* ctx, const sq_bvh* bvh, const sq_ray_source* rays,
+                   uint32_t mode, sq_hit* hits, uint8_t* heatmap_rgb);
+
+/* Device time of the stages of the last sq_build / sq_trace on this context,
+ * in milliseconds, measured with CUDA events on the context stream
+ * (synchronises).  stage_ms[0] = build total, [1] = bounds+codes, [2] = sort,
+ * [3] = topology+refit, [4] = trace.                                         */
+sq_status sq_last_timings(sq_ctx* ctx, float stage_ms[8]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SEQUOIA_GPU_H */
