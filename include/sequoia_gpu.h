@@ -229,7 +229,8 @@ sq_status sq_trace(sq_ctx* ctx, const sq_bvh* bvh, const sq_ray_source* rays,
 /* Device time of the stages of the last sq_build / sq_trace on this context,
  * in milliseconds, measured with CUDA events on the context stream
  * (synchronises).  stage_ms[0] = build total, [1] = bounds+codes, [2] = sort,
- * [3] = topology+refit, [4] = trace.                                         */
+ * [3] = topology+refit, [4] = trace; [5] and [6] are the last trace's total
+ * ray-box and ray-triangle test counts (as floats).                          */
 sq_status sq_last_timings(sq_ctx* ctx, float stage_ms[8]);
 
 #ifdef __cplusplus

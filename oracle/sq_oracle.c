@@ -7,19 +7,22 @@
  *
  * Range-tree layout.  Every tree built here (and by the GPU library) is a
  * top-down tree over a final triangle order perm[0..n): each node covers a
- * contiguous range [b, e) of perm.  A binary node whose split boundary is q
- * (left = [b, q), right = [q, e)) stores its two child records in slots
- * base + 2q (left) and base + 2q + 1 (right).  A leaf cluster over [b, b+c)
- * stores its c single-triangle leaf records in slots base + 2b + 2 + k.  A
- * child range of one triangle is stored as a leaf record directly in the
- * parent's slot.  The root record is slot 0.  Slots are unique because the
- * c >= 2 leaves of a cluster fit in the 2c - 2 slots owned by the c - 1
- * boundaries inside it, which no binary node uses.  The position of every
- * record follows from the logical tree alone, so two builds of the same
- * logical tree produce byte-identical reachable records, whatever order they
- * were produced in.  Morton and SAH trees use base 0 and 2n + 2 slots; the
- * grid tree puts its 63-node heap in slots 0..62, its 64 cell nodes in
- * 63..126 and the cell subtrees at base 128.
+ * contiguous range [b, e) of perm.  With L = base + 2n + 2 (the leaf region):
+ *   - slot L + p holds the leaf record of the triangle at position p, for
+ *     every p (written whether or not a cluster references it);
+ *   - a binary node whose split boundary is q (left = [b, q), right = [q, e))
+ *     stores its two child records in slots base + 2q and base + 2q + 1;
+ *   - a leaf cluster over [b, b + c) is an inner record {child = L + b,
+ *     count = c}: its leaves are the leaf-region records, contiguous;
+ *   - a child range of one triangle is a copy of its leaf record stored in
+ *     the parent's slot;
+ *   - the root record is slot 0 (it is always an inner record, as in the
+ *     reference: src/builder.cpp:1604-1609, 2498-2501).
+ * The position of every record follows from the logical tree alone, so two
+ * builds of the same logical tree write identical records whatever order
+ * they run in.  Morton and SAH trees use base 0 and 3n + 2 slots; the grid
+ * tree puts its 63-node heap in slots 0..62, its 64 cell nodes in 63..126
+ * and the cell subtrees at base 128.
  */
 #include "sq_oracle.h"
 
@@ -256,7 +259,7 @@ uint32_t sqo_find_split_morton(const uint32_t* codes, uint32_t count)
 
 uint32_t sqo_node_capacity(uint32_t n, int kind)
 {
-    return (kind == 2 ? 128u : 0u) + 2u * n + 2u;
+    return (kind == 2 ? 128u : 0u) + 3u * n + 2u;
 }
 
 static inline void write_leaf(sqo_node1* nd, const box* b, uint32_t tri)
@@ -277,17 +280,17 @@ static inline void write_inner(sqo_node1* nd, const box* b, uint32_t child, uint
     nd->child = child;
 }
 
-/* Leaf cluster over perm[b, b+c): leaves at base + 2b + 2 + k; returns the
- * union of the triangle boxes.                                              */
-static void emit_cluster(const box* tb, const uint32_t* perm, uint32_t base,
-                         uint32_t b, uint32_t c, sqo_node1* nodes, box* out)
+/* Leaf-region records of every triangle: slot base + 2n + 2 + p */
+static void emit_leaves(const box* tb, const uint32_t* perm, uint32_t base, uint32_t n,
+                        sqo_node1* nodes)
+{
+    for (uint32_t p = 0; p < n; ++p) write_leaf(&nodes[base + 2u * n + 2u + p], &tb[perm[p]], perm[p]);
+}
+
+static inline void range_box(const box* tb, const uint32_t* perm, uint32_t b, uint32_t c, box* out)
 {
     box_reset(out);
-    for (uint32_t k = 0; k < c; ++k) {
-        uint32_t t = perm[b + k];
-        write_leaf(&nodes[base + 2u * b + 2u + k], &tb[t], t);
-        box_grow_box(out, &tb[t]);
-    }
+    for (uint32_t k = 0; k < c; ++k) box_grow_box(out, &tb[perm[b + k]]);
 }
 
 typedef struct morton_job {
@@ -295,6 +298,7 @@ typedef struct morton_job {
     const uint32_t* perm;
     const box* tb;
     sqo_node1* nodes;
+    uint32_t leaf0;
 } morton_job;
 
 /* recurse_morton (src/builder.cpp:2351-2409): writes the record of range
@@ -309,8 +313,8 @@ static void morton_range(const morton_job* j, uint32_t b, uint32_t e, uint32_t s
         return;
     }
     if (c < 8) {
-        emit_cluster(j->tb, j->perm, 0, b, c, j->nodes, out);
-        write_inner(&j->nodes[slot], out, 2u * b + 2u, c);
+        range_box(j->tb, j->perm, b, c, out);
+        write_inner(&j->nodes[slot], out, j->leaf0 + b, c);
         return;
     }
     uint32_t s = sqo_find_split_morton(j->codes + b, c);
@@ -343,15 +347,13 @@ uint32_t sqo_build_morton(const float* tris, uint32_t n, int bounds_mode,
         tri_box(tris + 9 * (size_t)i, &tb[i]);
     }
     sqo_sort_pairs(codes, perm, n, 32, 8);
-    morton_job j = {codes, perm, tb, nodes};
+    morton_job j = {codes, perm, tb, nodes, 2u * n + 2u};
+    emit_leaves(tb, perm, 0, n, nodes);
     box root;
-    if (n == 0) {
-        box_reset(&root);
-        write_inner(&nodes[0], &root, 2u, 0u);
-    } else if (n < 8) {
+    if (n < 8) {
         /* the root is always an inner record (src/builder.cpp:2498-2501) */
-        emit_cluster(tb, perm, 0, 0, n, nodes, &root);
-        write_inner(&nodes[0], &root, 2u, n);
+        range_box(tb, perm, 0, n, &root);
+        write_inner(&nodes[0], &root, j.leaf0, n);
     } else {
 #pragma omp parallel num_threads(sqo_get_threads())
 #pragma omp single
@@ -389,6 +391,7 @@ typedef struct sah_job {
     uint32_t* tmp;      /* partition scratch               */
     sqo_node1* nodes;
     uint32_t base;
+    uint32_t leaf0;     /* first leaf-region slot          */
     uint32_t bins;
     uint32_t leaf;
     int fail;
@@ -437,9 +440,7 @@ static void sah_range(sah_job* j, uint32_t b, uint32_t e, const box* p, const bo
             write_leaf(&j->nodes[slot], &j->tb[t], t);
             return;
         }
-        box u;
-        emit_cluster(j->tb, j->ids, j->base, b, cnt, j->nodes, &u);
-        write_inner(&j->nodes[slot], p, j->base + 2u * b + 2u, cnt);
+        write_inner(&j->nodes[slot], p, j->leaf0 + b, cnt);
         return;
     }
     int nb = (int)j->bins;
@@ -534,10 +535,11 @@ uint32_t sqo_build_sah(const float* tris, uint32_t n, uint32_t bins,
     box p, c;
     sah_setup(tris, n, tb, cen, &p, &c);
     for (uint32_t i = 0; i < n; ++i) ids[i] = i;
-    sah_job j = {tb, cen, ids, tmp, nodes, 0, bins, leaf_size, 0};
+    sah_job j = {tb, cen, ids, tmp, nodes, 0, 2u * n + 2u, bins, leaf_size, 0};
 #pragma omp parallel num_threads(sqo_get_threads())
 #pragma omp single
     sah_range(&j, 0, n, &p, &c, 0, 1);
+    emit_leaves(tb, ids, 0, n, nodes);
     if (perm_out) memcpy(perm_out, ids, sizeof(uint32_t) * (size_t)n);
     free(tb); free(cen); free(ids); free(tmp);
     return j.fail ? 0xFFFFFFFFu : 0u;
@@ -600,7 +602,7 @@ uint32_t sqo_build_grid(const float* tris, uint32_t n, uint32_t bins,
     for (int m = 0; m < 64; ++m) fill[m] = begin[m];
     for (uint32_t i = 0; i < n; ++i) ids[fill[slot_of_cell[cell_of[i]]]++] = i;
 
-    sah_job j = {tb, cen, ids, tmp, nodes, 128u, bins, leaf_size, 0};
+    sah_job j = {tb, cen, ids, tmp, nodes, 128u, 128u + 2u * n + 2u, bins, leaf_size, 0};
 #pragma omp parallel for schedule(dynamic, 1) num_threads(sqo_get_threads())
     for (int m = 0; m < 64; ++m) {
         const bin* cb = &cells[cell_at[m]];
@@ -610,6 +612,7 @@ uint32_t sqo_build_grid(const float* tris, uint32_t n, uint32_t bins,
             memcpy(nodes[63 + m].max, p.mx, 12);
         }
     }
+    emit_leaves(tb, ids, 128u, n, nodes);
     /* heap above the cells (src/builder.cpp:2181-2188) */
     for (int i = 62; i >= 0; --i) {
         box u;
@@ -910,14 +913,14 @@ static int trace_closest_one(const sqo_node1* nodes, uint32_t root, const float*
             }
             continue;
         }
-        se hits[64];
+        se hits[8];
         int nh = 0;
         for (uint32_t i = 0; i < nd->count; ++i) {
             uint32_t c = nd->child + i;
             cnt++;
             if (box_robust(&nodes[c], &rp, best_t, &tn)) {
-                if (nh < 64) { hits[nh].node = c; hits[nh].tn = tn; nh++; }
-                else err = 1;
+                if (nh < 8) { hits[nh].node = c; hits[nh].tn = tn; nh++; }
+                else { err = 1; break; }
             }
         }
         /* insertion sort by (tn, slot): stable on slot order */
@@ -927,6 +930,7 @@ static int trace_closest_one(const sqo_node1* nodes, uint32_t root, const float*
             while (b >= 0 && hits[b].tn > x.tn) { hits[b + 1] = hits[b]; b--; }
             hits[b + 1] = x;
         }
+        if (err) break;
         if (sp + nh > SQO_STACK) { err = 1; break; }
         for (int a = nh - 1; a >= 0; --a) stack[sp++] = hits[a];
     }

@@ -1,0 +1,357 @@
+"""sequoia_gb300 -- GB300-native BVH build and ray trace behind Sequoia's interface.
+
+Python host binding of libsequoia_gpu.so (the C ABI in include/sequoia_gpu.h).
+The classes mirror the reference's host interface (src/builder.h:81-104,
+src/tracer.h:118-135): `Builder.build_hierarchy*` return a `Hierarchy` and
+`trace()` returns the heatmap bytes, but every call runs the CUDA kernels
+through the C ABI.  There is no CPU fallback: if the library is missing or
+no GPU is present, calls raise.
+
+Arrays: host arguments are numpy arrays; device arguments are any object with
+`__cuda_array_interface__` (e.g. a torch CUDA tensor) or a raw integer
+address.  Triangles are float32 (n, 9); rays float32 (n, 8)
+{ox, oy, oz, tmin, dx, dy, dz, tmax}.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+__all__ = ["Context", "Bvh", "Hierarchy", "Builder", "trace", "traverse", "SequoiaError",
+           "NODE1", "HIT", "NO_HIT", "library_path", "load_library"]
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(HERE, "libsequoia_gpu.so")
+NO_HIT = 0xFFFFFFFF
+NODE1 = np.dtype([("min", "<f4", 3), ("count", "<u2"), ("flags", "<u2"), ("max", "<f4", 3), ("child", "<u4")])
+HIT = np.dtype([("id", "<u4"), ("t", "<f4"), ("tests", "<u4")])
+
+MODES = {"ref": 0, "closest": 1, "anyhit": 2}
+BUILDERS = {"morton": 0, "sah": 1, "recursive": 1, "grid": 2}
+STATUS = {0: "OK", 1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "device error",
+          5: "unsupported", 6: "no CUDA device"}
+
+
+class SequoiaError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s (%d): %s" % (STATUS.get(status, "?"), status, msg))
+        self.status = status
+
+
+class _Options(C.Structure):
+    _fields_ = [("device", C.c_int), ("stream", C.c_void_p), ("flags", C.c_uint32)]
+
+
+class _BuildParams(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("sah_bins", C.c_uint32), ("leaf_size", C.c_uint32),
+                ("sort_digit_bits", C.c_uint32), ("morton_bounds", C.c_uint32), ("flags", C.c_uint32)]
+
+
+class _BvhInfo(C.Structure):
+    _fields_ = [("node_capacity", C.c_uint32), ("root", C.c_uint32), ("tri_count", C.c_uint32),
+                ("kind", C.c_uint32), ("scene_min", C.c_float * 3), ("scene_max", C.c_float * 3)]
+
+
+class _RaySource(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("origin", C.c_float * 3), ("target", C.c_float * 3), ("up", C.c_float * 3),
+                ("vfov_deg", C.c_float), ("rays", C.c_void_p), ("ray_count", C.c_uint32)]
+
+
+_lib = None
+
+
+def library_path():
+    return _LIB_PATH
+
+
+def load_library():
+    """Load libsequoia_gpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_LIB_PATH):
+        raise RuntimeError("libsequoia_gpu.so is not built (run `python -c \"import __graft_entry__ as g; g.build()\"`)")
+    L = C.CDLL(_LIB_PATH)
+    vp, u32, i32 = C.c_void_p, C.c_uint32, C.c_int
+    sig = {
+        "sq_abi_version": (u32, []),
+        "sq_create": (i32, [C.POINTER(vp), C.POINTER(_Options)]),
+        "sq_destroy": (i32, [vp]),
+        "sq_last_error": (C.c_char_p, [vp]),
+        "sq_sync": (i32, [vp, C.POINTER(u32)]),
+        "sq_build": (i32, [vp, vp, u32, C.POINTER(_BuildParams), C.POINTER(vp)]),
+        "sq_bvh_free": (i32, [vp]),
+        "sq_bvh_get_info": (i32, [vp, C.POINTER(_BvhInfo)]),
+        "sq_bvh_export_node1": (i32, [vp, vp, u32, C.POINTER(u32), C.POINTER(u32)]),
+        "sq_bvh_import_node1": (i32, [vp, vp, u32, u32, vp, u32, C.POINTER(vp)]),
+        "sq_morton_codes": (i32, [vp, vp, u32, u32, vp, vp]),
+        "sq_radix_sort_pairs": (i32, [vp, vp, vp, u32, u32, u32, vp, vp]),
+        "sq_bvh_export_sorted": (i32, [vp, vp, vp]),
+        "sq_trace": (i32, [vp, vp, C.POINTER(_RaySource), u32, vp, vp]),
+        "sq_last_timings": (i32, [vp, C.POINTER(C.c_float * 8)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _addr(x):
+    """Address of a host numpy array, a device array or an int (None -> None)."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if isinstance(x, np.ndarray):
+        if not x.flags["C_CONTIGUOUS"]:
+            raise ValueError("array must be C-contiguous")
+        return x.ctypes.data
+    cai = getattr(x, "__cuda_array_interface__", None)
+    if cai is not None:
+        return int(cai["data"][0])
+    if hasattr(x, "data_ptr"):
+        return int(x.data_ptr())
+    raise TypeError("unsupported buffer type %r" % type(x))
+
+
+def _len(x, width):
+    if isinstance(x, np.ndarray):
+        return x.size // width
+    shape = getattr(x, "shape", None)
+    if shape is not None:
+        total = 1
+        for s in shape:
+            total *= int(s)
+        return total // width
+    raise TypeError("cannot infer the length of %r" % type(x))
+
+
+class Bvh:
+    """A device-resident BVH (sq_bvh)."""
+
+    def __init__(self, ctx, handle, tris_ref=None):
+        self.ctx = ctx
+        self.handle = handle
+        self._tris_ref = tris_ref  # keeps a device triangle buffer alive
+
+    def info(self):
+        info = _BvhInfo()
+        self.ctx._check(load_library().sq_bvh_get_info(self.handle, C.byref(info)))
+        return info
+
+    @property
+    def node_capacity(self):
+        return self.info().node_capacity
+
+    @property
+    def root(self):
+        return self.info().root
+
+    def export_node1(self):
+        L = load_library()
+        cap = self.info().node_capacity
+        nodes = np.zeros(cap, NODE1)
+        cnt, root = C.c_uint32(), C.c_uint32()
+        self.ctx._check(L.sq_bvh_export_node1(self.handle, nodes.ctypes.data, cap, C.byref(cnt), C.byref(root)))
+        return nodes, int(root.value)
+
+    def export_sorted(self):
+        n = self.info().tri_count
+        codes = np.empty(n, np.uint32)
+        perm = np.empty(n, np.uint32)
+        self.ctx._check(load_library().sq_bvh_export_sorted(self.handle, codes.ctypes.data, perm.ctypes.data))
+        return codes, perm
+
+    def free(self):
+        if self.handle:
+            load_library().sq_bvh_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Context:
+    """A CUDA context wrapper (sq_ctx): one device, one stream."""
+
+    def __init__(self, device: int = 0, stream=None):
+        L = load_library()
+        opt = _Options(device, stream if stream is not None else None, 0)
+        h = C.c_void_p()
+        st = L.sq_create(C.byref(h), C.byref(opt))
+        if st != 0:
+            raise SequoiaError(st, "sq_create failed")
+        self.handle = h
+
+    def _check(self, st):
+        if st != 0:
+            msg = load_library().sq_last_error(self.handle)
+            raise SequoiaError(st, msg.decode() if msg else "")
+
+    def close(self):
+        if getattr(self, "handle", None):
+            load_library().sq_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sync(self):
+        bits = C.c_uint32()
+        self._check(load_library().sq_sync(self.handle, C.byref(bits)))
+        return bits.value
+
+    def build(self, tris, builder="morton", bins=8, leaf=8, digit_bits=8, morton_bounds=0, flags=0):
+        n = _len(tris, 9)
+        p = _BuildParams(BUILDERS[builder] if isinstance(builder, str) else int(builder), bins, leaf,
+                         digit_bits, morton_bounds, flags)
+        h = C.c_void_p()
+        self._check(load_library().sq_build(self.handle, _addr(tris), n, C.byref(p), C.byref(h)))
+        keep = None if isinstance(tris, np.ndarray) else tris
+        return Bvh(self, h, keep)
+
+    def import_node1(self, nodes, root, tris):
+        nodes = np.ascontiguousarray(nodes, NODE1)
+        tris = np.ascontiguousarray(tris, np.float32)
+        h = C.c_void_p()
+        self._check(load_library().sq_bvh_import_node1(self.handle, nodes.ctypes.data, len(nodes), int(root),
+                                                        tris.ctypes.data, len(tris), C.byref(h)))
+        return Bvh(self, h)
+
+    def morton_codes(self, tris, bounds_mode=0):
+        n = _len(tris, 9)
+        codes = np.empty(n, np.uint32)
+        box = np.empty(6, np.float32)
+        self._check(load_library().sq_morton_codes(self.handle, _addr(tris), n, bounds_mode,
+                                                   codes.ctypes.data, box.ctypes.data))
+        return codes, box
+
+    def radix_sort_pairs(self, keys, values, key_bits=32, digit_bits=8, keys_out=None, values_out=None):
+        n = _len(keys, 1)
+        host = keys_out is None
+        if host:
+            keys_out = np.empty(n, np.uint32)
+            values_out = np.empty(n, np.uint32)
+        self._check(load_library().sq_radix_sort_pairs(self.handle, _addr(keys), _addr(values), n, key_bits,
+                                                       digit_bits, _addr(keys_out), _addr(values_out)))
+        return keys_out, values_out
+
+    def _ray_source(self, rays=None, camera=None, width=0, height=0, origin=(0, 0, 0), target=(0, 0, -1),
+                    up=(0, 1, 0), vfov=60.0):
+        src = _RaySource()
+        if rays is not None:
+            src.kind = 2
+            src.rays = _addr(rays)
+            src.ray_count = _len(rays, 8)
+            return src, src.ray_count
+        src.kind = 0 if camera == "reference" else 1
+        src.width, src.height = width, height
+        src.origin[:] = [float(v) for v in origin]
+        src.target[:] = [float(v) for v in target]
+        src.up[:] = [float(v) for v in up]
+        src.vfov_deg = float(vfov)
+        return src, width * height
+
+    def trace(self, bvh, mode="closest", rays=None, camera=None, width=0, height=0, origin=(0, 0, 0),
+              target=(0, 0, -1), up=(0, 1, 0), vfov=60.0, hits=True, heatmap=False):
+        """Trace rays; returns (hits structured array or None, heatmap bytes or None).
+        `hits` / `heatmap` may also be device buffers to write into."""
+        src, count = self._ray_source(rays, camera, width, height, origin, target, up, vfov)
+        h_arr = np.empty(count, HIT) if hits is True else (hits if hits is not False else None)
+        m_arr = np.empty(count * 3, np.uint8) if heatmap is True else (heatmap if heatmap is not False else None)
+        self._check(load_library().sq_trace(self.handle, bvh.handle, C.byref(src), MODES[mode],
+                                            _addr(h_arr), _addr(m_arr)))
+        return h_arr, m_arr
+
+    def timings(self):
+        arr = (C.c_float * 8)()
+        self._check(load_library().sq_last_timings(self.handle, C.byref(arr)))
+        return {"build": arr[0], "codes": arr[1], "sort": arr[2], "topology": arr[3], "trace": arr[4],
+                "box_tests": arr[5], "tri_tests": arr[6]}
+
+
+# ---------------------------------------------------------------------------
+# Mirror of the reference's host interface (src/builder.h:81-104,
+# src/tracer.h:118-135, src/aabb.h:197-205).
+
+_default_ctx = None
+
+
+def default_context():
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+class Hierarchy:
+    """Host view of a BVH in the reference's layout: node_base (Node1 array),
+    node_count, tri_base (the triangles), tri_count, root_index."""
+
+    def __init__(self, node_base, root_index, tri_base, bvh=None):
+        self.node_base = node_base
+        self.node_count = len(node_base)
+        self.tri_base = tri_base
+        self.tri_count = len(tri_base)
+        self.root_index = root_index
+        self.bvh = bvh
+
+
+class Builder:
+    """Builder::build_hierarchy* (src/builder.h:81-104), on the GPU."""
+
+    @staticmethod
+    def _build(primitives, builder, **kw):
+        ctx = default_context()
+        tris = np.ascontiguousarray(primitives, np.float32).reshape(-1, 9)
+        bvh = ctx.build(tris, builder, **kw)
+        nodes, root = bvh.export_node1()
+        return Hierarchy(nodes, root, tris, bvh)
+
+    @staticmethod
+    def build_hierarchy(primitives, bins=8, leaf=8):
+        return Builder._build(primitives, "sah", bins=bins, leaf=leaf)
+
+    @staticmethod
+    def build_hierarchy_morton(primitives):
+        return Builder._build(primitives, "morton")
+
+    @staticmethod
+    def build_hierarchy_grid(primitives, bins=8, leaf=8, scene_bounds_cells=True):
+        return Builder._build(primitives, "grid", bins=bins, leaf=leaf, flags=1 if scene_bounds_cells else 0)
+
+
+def _bvh_of(h):
+    ctx = default_context()
+    if h.bvh is not None:
+        return ctx, h.bvh
+    h.bvh = ctx.import_node1(h.node_base, h.root_index, h.tri_base)
+    return ctx, h.bvh
+
+
+def trace(hierarchy, w, h, origin):
+    """trace() (src/tracer.cpp:195-230): reference camera at `origin`, w x h
+    primary rays; returns the w*h*3 heatmap bytes."""
+    ctx, bvh = _bvh_of(hierarchy)
+    _, heat = ctx.trace(bvh, mode="ref", camera="reference", width=w, height=h, origin=origin,
+                        hits=False, heatmap=True)
+    return heat
+
+
+def traverse(hierarchy, rays):
+    """traverse() (src/tracer.cpp:47-65) for explicit rays: returns (hit flag,
+    number of ray-box tests) per ray."""
+    ctx, bvh = _bvh_of(hierarchy)
+    hits, _ = ctx.trace(bvh, mode="ref", rays=np.ascontiguousarray(rays, np.float32))
+    return (hits["id"] != NO_HIT).astype(np.uint32), hits["tests"].copy()

@@ -1,0 +1,600 @@
+// sq_api.cu -- the C ABI of libsequoia_gpu (include/sequoia_gpu.h).
+//
+// Host side of the library: contexts (one CUDA stream each), a caching device
+// allocator so repeated builds and traces do not call cudaMalloc, host/device
+// pointer detection, and the build / trace dispatch.
+#include "sq_common.cuh"
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <new>
+#include <string>
+#include <vector>
+
+using sq::Node;
+
+struct sq_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+    uint32_t* ctrl = nullptr;  // [0] device error word, [1] work counter, [4..7] trace stats (2 x u64)
+    std::multimap<size_t, void*> free_blocks;
+    std::map<void*, size_t> live_blocks;
+    cudaEvent_t ev[8] = {};
+    bool build_timed = false, trace_timed = false;
+};
+
+struct sq_bvh {
+    sq_ctx* ctx = nullptr;
+    Node* nodes = nullptr;
+    uint32_t cap = 0;
+    uint32_t root = 0;
+    uint32_t n = 0;
+    const float* tris = nullptr;  // device
+    float* tris_own = nullptr;
+    uint32_t kind = 0;
+    float scene[6] = {0, 0, 0, 0, 0, 0};
+    uint32_t* codes = nullptr;  // sorted codes (Morton builds)
+    uint32_t* perm = nullptr;   // sorted permutation
+};
+
+namespace {
+
+sq_status fail(sq_ctx* c, sq_status st, const char* fmt, ...)
+{
+    if (c) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        c->err = buf;
+    }
+    return st;
+}
+
+#define SQ_CUDA(c, call)                                                                              \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess)                                                                        \
+            return fail((c), e_ == cudaErrorMemoryAllocation ? SQ_ERR_OOM : SQ_ERR_CUDA, "%s: %s (%s:%d)", \
+                        #call, cudaGetErrorString(e_), __FILE__, __LINE__);                           \
+    } while (0)
+
+size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Caching allocator: freed blocks are kept by size and reused.
+void* dalloc(sq_ctx* c, size_t bytes)
+{
+    if (bytes == 0) bytes = 256;
+    const size_t sz = bytes < (1u << 20) ? round_up(bytes, 256) : round_up(bytes, 2u << 20);
+    auto it = c->free_blocks.lower_bound(sz);
+    if (it != c->free_blocks.end() && it->first <= sz * 2) {
+        void* p = it->second;
+        c->live_blocks[p] = it->first;
+        c->free_blocks.erase(it);
+        return p;
+    }
+    void* p = nullptr;
+    if (cudaMalloc(&p, sz) != cudaSuccess) {
+        cudaGetLastError();
+        // release the cache and retry once
+        cudaStreamSynchronize(c->stream);
+        for (auto& kv : c->free_blocks) cudaFree(kv.second);
+        c->free_blocks.clear();
+        if (cudaMalloc(&p, sz) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+    }
+    c->live_blocks[p] = sz;
+    return p;
+}
+
+void dfree(sq_ctx* c, void* p)
+{
+    if (!p) return;
+    auto it = c->live_blocks.find(p);
+    if (it == c->live_blocks.end()) return;
+    c->free_blocks.emplace(it->second, p);
+    c->live_blocks.erase(it);
+}
+
+bool is_device_ptr(const void* p)
+{
+    if (!p) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+struct Guard {
+    int prev = -1;
+    explicit Guard(int dev)
+    {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~Guard()
+    {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+sq_status check_device_error(sq_ctx* c, uint32_t* bits_out)
+{
+    uint32_t bits = 0;
+    SQ_CUDA(c, cudaMemcpyAsync(&bits, c->ctrl, sizeof bits, cudaMemcpyDeviceToHost, c->stream));
+    SQ_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (bits_out) *bits_out = bits;
+    if (bits) {
+        SQ_CUDA(c, cudaMemsetAsync(c->ctrl, 0, sizeof(uint32_t), c->stream));
+        SQ_CUDA(c, cudaStreamSynchronize(c->stream));
+        return fail(c, SQ_ERR_DEVICE, "device error word 0x%x (1 stack overflow, 2 look-back timeout, 4 topology, 8 SAH queue, 16 node count)", bits);
+    }
+    return SQ_OK;
+}
+
+uint32_t sort_passes_for(uint32_t key_bits, uint32_t digit_bits) { return (key_bits + digit_bits - 1) / digit_bits; }
+
+sq_status new_bvh(sq_ctx* c, uint32_t n, uint32_t cap, sq_bvh** out)
+{
+    sq_bvh* b = new (std::nothrow) sq_bvh;
+    if (!b) return fail(c, SQ_ERR_OOM, "host allocation failed");
+    b->ctx = c;
+    b->n = n;
+    b->cap = cap;
+    b->nodes = static_cast<Node*>(dalloc(c, sizeof(Node) * (size_t)cap));
+    if (!b->nodes) {
+        delete b;
+        return fail(c, SQ_ERR_OOM, "device allocation of %u nodes failed", cap);
+    }
+    *out = b;
+    return SQ_OK;
+}
+
+// tris argument -> device pointer (copy if host)
+sq_status device_tris(sq_ctx* c, const sq_triangle* tris, uint32_t n, const float** dev, float** owned)
+{
+    *owned = nullptr;
+    if (n == 0) { *dev = nullptr; return SQ_OK; }
+    if (is_device_ptr(tris)) {
+        *dev = reinterpret_cast<const float*>(tris);
+        return SQ_OK;
+    }
+    float* d = static_cast<float*>(dalloc(c, sizeof(float) * 9ull * n));
+    if (!d) return fail(c, SQ_ERR_OOM, "device allocation for %u triangles failed", n);
+    SQ_CUDA(c, cudaMemcpyAsync(d, tris, sizeof(float) * 9ull * n, cudaMemcpyHostToDevice, c->stream));
+    *dev = d;
+    *owned = d;
+    return SQ_OK;
+}
+
+// Morton / LBVH build into b (nodes allocated, tris set).
+sq_status build_morton(sq_ctx* c, sq_bvh* b, const sq_build_params& p)
+{
+    const uint32_t n = b->n;
+    uint32_t db = p.sort_digit_bits ? p.sort_digit_bits : 8u;
+    if (db != 6 && db != 8 && db != 10) return fail(c, SQ_ERR_INVALID, "sort_digit_bits must be 6, 8 or 10");
+    const uint32_t passes = sort_passes_for(30, db);
+    const size_t radix = (size_t)1 << db;
+    const size_t lb_words = sqk::sort_lookback_words(n, db, passes);
+    // zeroed region: box_ord[8] | hist[passes*radix] | counters[8] | lookback | flags[n]
+    const size_t z_box = 0, z_hist = 8, z_ctr = z_hist + passes * radix, z_lb = z_ctr + 8, z_flags = z_lb + lb_words;
+    const size_t z_words = z_flags + n;
+    uint32_t* zero = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * z_words));
+    uint32_t* alt = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * 2ull * n));
+    float4* info = static_cast<float4*>(dalloc(c, sizeof(float4) * 4ull * n));
+    b->codes = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * (size_t)n));
+    b->perm = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * (size_t)n));
+    if (!zero || !alt || !info || !b->codes || !b->perm) {
+        dfree(c, zero); dfree(c, alt); dfree(c, info);
+        return fail(c, SQ_ERR_OOM, "device workspace allocation failed (n=%u)", n);
+    }
+    uint32_t* err = c->ctrl;
+    cudaStream_t s = c->stream;
+    SQ_CUDA(c, cudaEventRecord(c->ev[0], s));
+    SQ_CUDA(c, cudaMemsetAsync(zero, 0, sizeof(uint32_t) * z_words, s));
+    // sorted result lands in buffer A when the pass count is even
+    uint32_t *ka, *va, *kb, *vb;
+    if (passes % 2 == 0) { ka = b->codes; va = b->perm; kb = alt; vb = alt + n; }
+    else { ka = alt; va = alt + n; kb = b->codes; vb = b->perm; }
+    sqk::scene_bounds(b->tris, n, p.morton_bounds, zero + z_box, s);
+    sqk::morton_codes(b->tris, n, p.morton_bounds, zero + z_box, ka, va, zero + z_hist, db, passes, s);
+    SQ_CUDA(c, cudaEventRecord(c->ev[1], s));
+    sqk::sort_passes(ka, va, kb, vb, n, zero + z_hist, zero + z_lb, zero + z_ctr, db, passes, err, s);
+    SQ_CUDA(c, cudaEventRecord(c->ev[2], s));
+    sqk::lbvh_climb(b->codes, b->perm, b->tris, n, b->nodes, zero + z_flags, info, err, s);
+    SQ_CUDA(c, cudaEventRecord(c->ev[3], s));
+    SQ_CUDA(c, cudaGetLastError());
+    c->build_timed = true;
+    dfree(c, zero);
+    dfree(c, alt);
+    dfree(c, info);
+    b->root = 0;
+    return SQ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+uint32_t sq_abi_version(void) { return SQ_ABI_VERSION; }
+
+sq_status sq_create(sq_ctx** out, const sq_options* options)
+{
+    if (!out) return SQ_ERR_INVALID;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return SQ_ERR_NO_DEVICE;
+    }
+    sq_ctx* c = new (std::nothrow) sq_ctx;
+    if (!c) return SQ_ERR_OOM;
+    c->device = options ? options->device : 0;
+    if (c->device < 0 || c->device >= count) {
+        delete c;
+        return SQ_ERR_INVALID;
+    }
+    Guard g(c->device);
+    if (options && options->stream) {
+        c->stream = static_cast<cudaStream_t>(options->stream);
+    } else {
+        if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            delete c;
+            return SQ_ERR_CUDA;
+        }
+        c->own_stream = true;
+    }
+    if (cudaMalloc(&c->ctrl, 64) != cudaSuccess || cudaMemset(c->ctrl, 0, 64) != cudaSuccess) {
+        if (c->own_stream) cudaStreamDestroy(c->stream);
+        delete c;
+        return SQ_ERR_OOM;
+    }
+    for (auto& e : c->ev) cudaEventCreate(&e);
+    *out = c;
+    return SQ_OK;
+}
+
+sq_status sq_destroy(sq_ctx* c)
+{
+    if (!c) return SQ_ERR_INVALID;
+    Guard g(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (auto& kv : c->free_blocks) cudaFree(kv.second);
+    for (auto& kv : c->live_blocks) cudaFree(kv.first);
+    for (auto& e : c->ev) cudaEventDestroy(e);
+    cudaFree(c->ctrl);
+    if (c->own_stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return SQ_OK;
+}
+
+const char* sq_last_error(const sq_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+sq_status sq_sync(sq_ctx* c, uint32_t* device_error)
+{
+    if (!c) return SQ_ERR_INVALID;
+    Guard g(c->device);
+    return check_device_error(c, device_error);
+}
+
+sq_status sq_build(sq_ctx* c, const sq_triangle* tris, uint32_t n, const sq_build_params* params, sq_bvh** out)
+{
+    if (!c || !out || !params || (n > 0 && !tris)) return fail(c, SQ_ERR_INVALID, "sq_build: null argument");
+    if (n > (1u << 29)) return fail(c, SQ_ERR_INVALID, "sq_build: n=%u exceeds 2^29", n);
+    *out = nullptr;
+    Guard g(c->device);
+    sq_build_params p = *params;
+    if (p.kind != SQ_BUILDER_MORTON && p.kind != SQ_BUILDER_SAH && p.kind != SQ_BUILDER_GRID)
+        return fail(c, SQ_ERR_INVALID, "sq_build: unknown builder kind %u", p.kind);
+    if (p.kind != SQ_BUILDER_MORTON) return fail(c, SQ_ERR_UNSUPPORTED, "sq_build: builder kind %u not built yet", p.kind);
+    const uint32_t cap = 3u * n + 2u;
+    sq_bvh* b = nullptr;
+    sq_status st = new_bvh(c, n, cap, &b);
+    if (st != SQ_OK) return st;
+    b->kind = p.kind;
+    st = device_tris(c, tris, n, &b->tris, &b->tris_own);
+    if (st != SQ_OK) { sq_bvh_free(b); return st; }
+    if (n == 0) {
+        Node root;
+        root.mnx = root.mny = root.mnz = FLT_MAX;
+        root.mxx = root.mxy = root.mxz = -FLT_MAX;
+        root.count_flags = sq::pack_cf(0, 0);
+        root.child = 2;
+        SQ_CUDA(c, cudaMemcpyAsync(b->nodes, &root, sizeof root, cudaMemcpyHostToDevice, c->stream));
+        SQ_CUDA(c, cudaStreamSynchronize(c->stream));
+        *out = b;
+        return SQ_OK;
+    }
+    st = build_morton(c, b, p);
+    if (st != SQ_OK) { sq_bvh_free(b); return st; }
+    *out = b;
+    return SQ_OK;
+}
+
+sq_status sq_bvh_free(sq_bvh* b)
+{
+    if (!b) return SQ_ERR_INVALID;
+    sq_ctx* c = b->ctx;
+    Guard g(c->device);
+    dfree(c, b->nodes);
+    dfree(c, b->tris_own);
+    dfree(c, b->codes);
+    dfree(c, b->perm);
+    delete b;
+    return SQ_OK;
+}
+
+sq_status sq_bvh_get_info(const sq_bvh* b, sq_bvh_info* info)
+{
+    if (!b || !info) return SQ_ERR_INVALID;
+    info->node_capacity = b->cap;
+    info->root = b->root;
+    info->tri_count = b->n;
+    info->kind = b->kind;
+    for (int k = 0; k < 3; ++k) { info->scene_min[k] = b->scene[k]; info->scene_max[k] = b->scene[3 + k]; }
+    return SQ_OK;
+}
+
+sq_status sq_bvh_export_node1(sq_bvh* b, sq_node1* nodes, uint32_t cap, uint32_t* node_count, uint32_t* root)
+{
+    if (!b) return SQ_ERR_INVALID;
+    sq_ctx* c = b->ctx;
+    Guard g(c->device);
+    if (node_count) *node_count = b->cap;
+    if (root) *root = b->root;
+    if (nodes) {
+        if (cap < b->cap) return fail(c, SQ_ERR_INVALID, "export: capacity %u < %u nodes", cap, b->cap);
+        SQ_CUDA(c, cudaMemcpyAsync(nodes, b->nodes, sizeof(Node) * (size_t)b->cap, cudaMemcpyDefault, c->stream));
+    }
+    return check_device_error(c, nullptr);
+}
+
+sq_status sq_bvh_export_sorted(sq_bvh* b, uint32_t* codes, uint32_t* perm)
+{
+    if (!b) return SQ_ERR_INVALID;
+    sq_ctx* c = b->ctx;
+    Guard g(c->device);
+    if (!b->codes) return fail(c, SQ_ERR_INVALID, "export_sorted: not a Morton build");
+    if (codes) SQ_CUDA(c, cudaMemcpyAsync(codes, b->codes, sizeof(uint32_t) * (size_t)b->n, cudaMemcpyDefault, c->stream));
+    if (perm) SQ_CUDA(c, cudaMemcpyAsync(perm, b->perm, sizeof(uint32_t) * (size_t)b->n, cudaMemcpyDefault, c->stream));
+    return check_device_error(c, nullptr);
+}
+
+sq_status sq_bvh_import_node1(sq_ctx* c, const sq_node1* nodes, uint32_t node_count, uint32_t root,
+                              const sq_triangle* tris, uint32_t n, sq_bvh** out)
+{
+    if (!c || !nodes || !out || (n > 0 && !tris) || root >= node_count)
+        return fail(c, SQ_ERR_INVALID, "sq_bvh_import_node1: bad argument");
+    *out = nullptr;
+    Guard g(c->device);
+    sq_bvh* b = nullptr;
+    sq_status st = new_bvh(c, n, node_count, &b);
+    if (st != SQ_OK) return st;
+    b->root = root;
+    b->kind = 0xFFFFFFFFu;
+    SQ_CUDA(c, cudaMemcpyAsync(b->nodes, nodes, sizeof(Node) * (size_t)node_count, cudaMemcpyDefault, c->stream));
+    if (n) {
+        float* d = static_cast<float*>(dalloc(c, sizeof(float) * 9ull * n));
+        if (!d) { sq_bvh_free(b); return fail(c, SQ_ERR_OOM, "import: triangle allocation failed"); }
+        SQ_CUDA(c, cudaMemcpyAsync(d, tris, sizeof(float) * 9ull * n, cudaMemcpyDefault, c->stream));
+        b->tris = d;
+        b->tris_own = d;
+    }
+    SQ_CUDA(c, cudaStreamSynchronize(c->stream));
+    *out = b;
+    return SQ_OK;
+}
+
+sq_status sq_morton_codes(sq_ctx* c, const sq_triangle* tris, uint32_t n, uint32_t bounds_mode, uint32_t* codes,
+                          float* scene_box)
+{
+    if (!c || (n > 0 && (!tris || !codes))) return fail(c, SQ_ERR_INVALID, "sq_morton_codes: null argument");
+    Guard g(c->device);
+    if (n == 0) return SQ_OK;
+    const float* dt = nullptr;
+    float* owned = nullptr;
+    sq_status st = device_tris(c, tris, n, &dt, &owned);
+    if (st != SQ_OK) return st;
+    const uint32_t passes = 4, db = 8;
+    const size_t z_words = 8 + passes * 256;
+    uint32_t* zero = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * z_words));
+    uint32_t* keys = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * 2ull * n));
+    if (!zero || !keys) { dfree(c, zero); dfree(c, keys); dfree(c, owned); return fail(c, SQ_ERR_OOM, "allocation failed"); }
+    cudaStream_t s = c->stream;
+    SQ_CUDA(c, cudaMemsetAsync(zero, 0, sizeof(uint32_t) * z_words, s));
+    sqk::scene_bounds(dt, n, bounds_mode, zero, s);
+    sqk::morton_codes(dt, n, bounds_mode, zero, keys, keys + n, zero + 8, db, passes, s);
+    SQ_CUDA(c, cudaMemcpyAsync(codes, keys, sizeof(uint32_t) * (size_t)n, cudaMemcpyDefault, s));
+    uint32_t ord[6];
+    SQ_CUDA(c, cudaMemcpyAsync(ord, zero, sizeof ord, cudaMemcpyDeviceToHost, s));
+    st = check_device_error(c, nullptr);
+    if (scene_box && st == SQ_OK) {
+        float box[6];
+        for (int k = 0; k < 3; ++k) {
+            box[k] = -sq::ordered_to_float(ord[k]);
+            box[3 + k] = sq::ordered_to_float(ord[3 + k]);
+        }
+        if (is_device_ptr(scene_box)) cudaMemcpy(scene_box, box, sizeof box, cudaMemcpyHostToDevice);
+        else memcpy(scene_box, box, sizeof box);
+    }
+    dfree(c, zero);
+    dfree(c, keys);
+    dfree(c, owned);
+    return st;
+}
+
+sq_status sq_radix_sort_pairs(sq_ctx* c, const uint32_t* keys_in, const uint32_t* values_in, uint32_t n,
+                              uint32_t key_bits, uint32_t digit_bits, uint32_t* keys_out, uint32_t* values_out)
+{
+    if (!c || (n > 0 && (!keys_in || !values_in || !keys_out || !values_out)))
+        return fail(c, SQ_ERR_INVALID, "sq_radix_sort_pairs: null argument");
+    if (key_bits < 1 || key_bits > 32) return fail(c, SQ_ERR_INVALID, "key_bits must be 1..32");
+    if (digit_bits == 0) digit_bits = 8;
+    if (digit_bits != 6 && digit_bits != 8 && digit_bits != 10) return fail(c, SQ_ERR_INVALID, "digit_bits must be 6, 8 or 10");
+    if (n >= (1u << 30)) return fail(c, SQ_ERR_INVALID, "n too large");
+    Guard g(c->device);
+    if (n == 0) return SQ_OK;
+    const uint32_t passes = sort_passes_for(key_bits, digit_bits);
+    const size_t radix = (size_t)1 << digit_bits;
+    const size_t lb_words = sqk::sort_lookback_words(n, digit_bits, passes);
+    const size_t z_hist = 0, z_ctr = passes * radix, z_lb = z_ctr + 8;
+    const size_t z_words = z_lb + lb_words;
+    uint32_t* zero = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * z_words));
+    uint32_t* buf = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * 4ull * n));
+    if (!zero || !buf) { dfree(c, zero); dfree(c, buf); return fail(c, SQ_ERR_OOM, "allocation failed"); }
+    cudaStream_t s = c->stream;
+    uint32_t *ka = buf, *va = buf + n, *kb = buf + 2ull * n, *vb = buf + 3ull * n;
+    SQ_CUDA(c, cudaMemcpyAsync(ka, keys_in, sizeof(uint32_t) * (size_t)n, cudaMemcpyDefault, s));
+    SQ_CUDA(c, cudaMemcpyAsync(va, values_in, sizeof(uint32_t) * (size_t)n, cudaMemcpyDefault, s));
+    SQ_CUDA(c, cudaMemsetAsync(zero, 0, sizeof(uint32_t) * z_words, s));
+    SQ_CUDA(c, cudaEventRecord(c->ev[1], s));
+    sqk::sort_histogram(ka, n, zero + z_hist, digit_bits, passes, s);
+    const int which = sqk::sort_passes(ka, va, kb, vb, n, zero + z_hist, zero + z_lb, zero + z_ctr, digit_bits, passes,
+                                       c->ctrl, s);
+    SQ_CUDA(c, cudaEventRecord(c->ev[2], s));
+    const uint32_t* rk = which ? kb : ka;
+    const uint32_t* rv = which ? vb : va;
+    SQ_CUDA(c, cudaMemcpyAsync(keys_out, rk, sizeof(uint32_t) * (size_t)n, cudaMemcpyDefault, s));
+    SQ_CUDA(c, cudaMemcpyAsync(values_out, rv, sizeof(uint32_t) * (size_t)n, cudaMemcpyDefault, s));
+    SQ_CUDA(c, cudaGetLastError());
+    const bool host_out = !is_device_ptr(keys_out) || !is_device_ptr(values_out);
+    sq_status st = SQ_OK;
+    if (host_out) st = check_device_error(c, nullptr);
+    dfree(c, zero);
+    dfree(c, buf);
+    return st;
+}
+
+sq_status sq_trace(sq_ctx* c, const sq_bvh* b, const sq_ray_source* rays, uint32_t mode, sq_hit* hits,
+                   uint8_t* heatmap_rgb)
+{
+    if (!c || !b || !rays) return fail(c, SQ_ERR_INVALID, "sq_trace: null argument");
+    if (mode > SQ_TRACE_ANYHIT) return fail(c, SQ_ERR_INVALID, "sq_trace: unknown mode %u", mode);
+    Guard g(c->device);
+    sqk::TraceArgs a;
+    memset(&a, 0, sizeof a);
+    a.nodes = b->nodes;
+    a.node_count = b->cap;
+    a.tri_count = b->n;
+    a.root = b->root;
+    a.tris = b->tris;
+    a.mode = mode;
+    a.ray_kind = rays->kind;
+    uint64_t count = 0;
+    float* rays_own = nullptr;
+    if (rays->kind == SQ_RAYS_REFERENCE_CAMERA || rays->kind == SQ_RAYS_PINHOLE) {
+        if (rays->width == 0 || rays->height == 0) return fail(c, SQ_ERR_INVALID, "sq_trace: empty image");
+        a.width = rays->width;
+        a.height = rays->height;
+        count = (uint64_t)rays->width * rays->height;
+        if (rays->kind == SQ_RAYS_REFERENCE_CAMERA) {
+            for (int k = 0; k < 3; ++k) a.cam[k] = rays->origin[k];
+        } else {
+            // pinhole basis in double, rounded to float
+            double f[3], r[3], u[3], up[3];
+            for (int k = 0; k < 3; ++k) { f[k] = (double)rays->target[k] - (double)rays->origin[k]; up[k] = rays->up[k]; }
+            const double fl = sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+            for (double& x : f) x /= fl;
+            r[0] = f[1] * up[2] - f[2] * up[1];
+            r[1] = f[2] * up[0] - f[0] * up[2];
+            r[2] = f[0] * up[1] - f[1] * up[0];
+            const double rl = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+            for (double& x : r) x /= rl;
+            u[0] = r[1] * f[2] - r[2] * f[1];
+            u[1] = r[2] * f[0] - r[0] * f[2];
+            u[2] = r[0] * f[1] - r[1] * f[0];
+            const double th = tan((double)rays->vfov_deg * 3.14159265358979323846 / 360.0);
+            for (int k = 0; k < 3; ++k) {
+                a.cam[k] = rays->origin[k];
+                a.cam[3 + k] = (float)f[k];
+                a.cam[6 + k] = (float)r[k];
+                a.cam[9 + k] = (float)u[k];
+            }
+            a.cam[12] = (float)(th * (double)rays->width / (double)rays->height);
+            a.cam[13] = (float)th;
+        }
+    } else if (rays->kind == SQ_RAYS_EXPLICIT) {
+        count = rays->ray_count;
+        a.ray_count = rays->ray_count;
+        if (count && !rays->rays) return fail(c, SQ_ERR_INVALID, "sq_trace: null ray array");
+        if (count && is_device_ptr(rays->rays) && (reinterpret_cast<uintptr_t>(rays->rays) & 15u) == 0) {
+            a.rays = reinterpret_cast<const float*>(rays->rays);
+        } else if (count) {
+            rays_own = static_cast<float*>(dalloc(c, sizeof(sq_ray) * count));
+            if (!rays_own) return fail(c, SQ_ERR_OOM, "ray allocation failed");
+            SQ_CUDA(c, cudaMemcpyAsync(rays_own, rays->rays, sizeof(sq_ray) * count, cudaMemcpyDefault, c->stream));
+            a.rays = rays_own;
+        }
+    } else {
+        return fail(c, SQ_ERR_INVALID, "sq_trace: unknown ray kind %u", rays->kind);
+    }
+    if (count > 0xFFFFFFFFull / 3) return fail(c, SQ_ERR_INVALID, "sq_trace: too many rays");
+    const bool hits_dev = hits && is_device_ptr(hits);
+    const bool heat_dev = heatmap_rgb && is_device_ptr(heatmap_rgb);
+    sq_hit* hits_tmp = nullptr;
+    uint8_t* heat_tmp = nullptr;
+    if (hits && !hits_dev) {
+        hits_tmp = static_cast<sq_hit*>(dalloc(c, sizeof(sq_hit) * count));
+        if (!hits_tmp) { dfree(c, rays_own); return fail(c, SQ_ERR_OOM, "hit buffer allocation failed"); }
+    }
+    if (heatmap_rgb && !heat_dev) {
+        heat_tmp = static_cast<uint8_t*>(dalloc(c, 3ull * count));
+        if (!heat_tmp) { dfree(c, rays_own); dfree(c, hits_tmp); return fail(c, SQ_ERR_OOM, "heatmap allocation failed"); }
+    }
+    a.hits = hits_dev ? hits : hits_tmp;
+    a.heat = heat_dev ? heatmap_rgb : heat_tmp;
+    a.work = c->ctrl + 1;
+    a.err = c->ctrl;
+    a.stats = reinterpret_cast<unsigned long long*>(c->ctrl + 4);
+    cudaStream_t s = c->stream;
+    SQ_CUDA(c, cudaMemsetAsync(c->ctrl + 1, 0, 7 * sizeof(uint32_t), s));
+    SQ_CUDA(c, cudaEventRecord(c->ev[4], s));
+    if (count > 0) sqk::trace(a, s);
+    SQ_CUDA(c, cudaEventRecord(c->ev[5], s));
+    SQ_CUDA(c, cudaGetLastError());
+    c->trace_timed = true;
+    if (hits_tmp) SQ_CUDA(c, cudaMemcpyAsync(hits, hits_tmp, sizeof(sq_hit) * count, cudaMemcpyDeviceToHost, s));
+    if (heat_tmp) SQ_CUDA(c, cudaMemcpyAsync(heatmap_rgb, heat_tmp, 3ull * count, cudaMemcpyDeviceToHost, s));
+    sq_status st = SQ_OK;
+    if (hits_tmp || heat_tmp) st = check_device_error(c, nullptr);
+    dfree(c, rays_own);
+    dfree(c, hits_tmp);
+    dfree(c, heat_tmp);
+    return st;
+}
+
+sq_status sq_last_timings(sq_ctx* c, float stage_ms[8])
+{
+    if (!c || !stage_ms) return SQ_ERR_INVALID;
+    Guard g(c->device);
+    for (int k = 0; k < 8; ++k) stage_ms[k] = -1.0f;
+    SQ_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (c->build_timed) {
+        cudaEventElapsedTime(&stage_ms[0], c->ev[0], c->ev[3]);
+        cudaEventElapsedTime(&stage_ms[1], c->ev[0], c->ev[1]);
+        cudaEventElapsedTime(&stage_ms[2], c->ev[1], c->ev[2]);
+        cudaEventElapsedTime(&stage_ms[3], c->ev[2], c->ev[3]);
+    }
+    if (c->trace_timed) {
+        cudaEventElapsedTime(&stage_ms[4], c->ev[4], c->ev[5]);
+        unsigned long long st[2] = {0, 0};
+        SQ_CUDA(c, cudaMemcpy(st, c->ctrl + 4, sizeof st, cudaMemcpyDeviceToHost));
+        stage_ms[5] = (float)st[0];
+        stage_ms[6] = (float)st[1];
+    }
+    cudaGetLastError();
+    return SQ_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,171 @@
+// sq_common.cuh -- shared device types and helpers of libsequoia_gpu.
+//
+// Floating point: the library is compiled with -fmad=false, so a*b+c is two
+// rounded operations everywhere, and `/`, sqrtf are IEEE round-to-nearest.
+// Min/max that must reproduce the reference bit for bit are written as the
+// reference's own comparisons (see ref_min / ref_max / simd_max below).
+#pragma once
+
+#include <cfloat>
+#include <cstdint>
+#include <cstring>
+#include <cuda_runtime.h>
+
+#include "../../include/sequoia_gpu.h"
+
+namespace sq {
+
+constexpr uint32_t kNoHit = 0xFFFFFFFFu;
+constexpr uint32_t kLeafFlag = 1u;
+
+// Node record, same bytes as sq_node1 / the reference's Node1.
+struct __align__(16) Node {
+    float mnx, mny, mnz;
+    uint32_t count_flags;  // count in the low 16 bits, flags in the high 16
+    float mxx, mxy, mxz;
+    uint32_t child;
+};
+static_assert(sizeof(Node) == 32, "Node must be 32 bytes");
+
+__host__ __device__ inline uint32_t node_count(uint32_t cf) { return cf & 0xFFFFu; }
+__host__ __device__ inline bool node_is_leaf(uint32_t cf) { return (cf >> 16) & kLeafFlag; }
+__host__ __device__ inline uint32_t pack_cf(uint32_t count, uint32_t flags) { return (count & 0xFFFFu) | (flags << 16); }
+
+// std::min(a, b) == (b < a) ? b : a  (src/vec3.h:179, src/simd_generic.h:164-168)
+__device__ __forceinline__ float ref_min(float a, float b) { return (b < a) ? b : a; }
+// std::max(a, b) == (a < b) ? b : a  (src/vec3.h:180)
+__device__ __forceinline__ float ref_max(float a, float b) { return (a < b) ? b : a; }
+// simd max: a > b ? a : b            (src/simd_generic.h:170-174)
+__device__ __forceinline__ float simd_max(float a, float b) { return (a > b) ? a : b; }
+
+// Order-preserving map float -> uint32 for atomicMax-based reductions.
+__device__ __forceinline__ uint32_t float_to_ordered(float f)
+{
+    uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__host__ __device__ inline float ordered_to_float(uint32_t u)
+{
+    uint32_t b = (u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u;
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(b);
+#else
+    float f;
+    memcpy(&f, &b, 4);
+    return f;
+#endif
+}
+
+struct Box {
+    float mn[3], mx[3];
+};
+
+__device__ __forceinline__ void box_reset(Box& b)
+{
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { b.mn[k] = FLT_MAX; b.mx[k] = -FLT_MAX; }
+}
+
+__device__ __forceinline__ void box_grow(Box& b, const Box& o)
+{
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { b.mn[k] = ref_min(b.mn[k], o.mn[k]); b.mx[k] = ref_max(b.mx[k], o.mx[k]); }
+}
+
+// Triangle AABB: min(min(v0, v1), v2), max(max(v0, v1), v2)  (src/builder.cpp:130-131)
+__device__ __forceinline__ Box tri_box(const float* t)
+{
+    Box b;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        b.mn[k] = ref_min(ref_min(t[k], t[3 + k]), t[6 + k]);
+        b.mx[k] = ref_max(ref_max(t[k], t[3 + k]), t[6 + k]);
+    }
+    return b;
+}
+
+__device__ __forceinline__ void load_tri(const float* __restrict__ tris, uint32_t i, float* t)
+{
+    const float* p = tris + 9ull * i;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) t[k] = __ldg(p + k);
+}
+
+__device__ __forceinline__ void store_node(Node* dst, const Box& b, uint32_t child, uint32_t count, uint32_t flags)
+{
+    float4 a = make_float4(b.mn[0], b.mn[1], b.mn[2], __uint_as_float(pack_cf(count, flags)));
+    float4 c = make_float4(b.mx[0], b.mx[1], b.mx[2], __uint_as_float(child));
+    reinterpret_cast<float4*>(dst)[0] = a;
+    reinterpret_cast<float4*>(dst)[1] = c;
+}
+
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p)
+{
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v)
+{
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t ld_volatile_u32(const uint32_t* p)
+{
+    uint32_t v;
+    asm volatile("ld.volatile.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void raise_error(uint32_t* err, uint32_t bit)
+{
+    if (err) atomicOr(err, bit);
+}
+
+constexpr int kNumSMs = 152;
+
+}  // namespace sq
+
+// ---------------------------------------------------------------------------
+// Host-side launchers implemented in the .cu files, called by sq_api.cu.
+namespace sqk {
+
+// LBVH (sq_lbvh.cu)
+void scene_bounds(const float* tris, uint32_t n, uint32_t mode, uint32_t* box_ord, cudaStream_t s);
+void morton_codes(const float* tris, uint32_t n, uint32_t mode, const uint32_t* box_ord, uint32_t* keys,
+                  uint32_t* vals, uint32_t* hist, uint32_t digit_bits, uint32_t passes, cudaStream_t s);
+void lbvh_climb(const uint32_t* codes, const uint32_t* perm, const float* tris, uint32_t n, sq::Node* nodes,
+                uint32_t* flags, float4* info, uint32_t* err, cudaStream_t s);
+
+// onesweep radix sort (sq_sort.cu)
+size_t sort_lookback_words(uint32_t n, uint32_t digit_bits, uint32_t passes);
+void sort_histogram(const uint32_t* keys, uint32_t n, uint32_t* hist, uint32_t digit_bits, uint32_t passes,
+                    cudaStream_t s);
+// Runs `passes` onesweep passes; hist/lookback/counters must be zeroed
+// before (lookback and counters) and filled (hist).  Returns which buffer
+// holds the result: 0 = (keys_a, vals_a), 1 = (keys_b, vals_b).
+int sort_passes(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b, uint32_t* vals_b, uint32_t n,
+                const uint32_t* hist, uint32_t* lookback, uint32_t* counters, uint32_t digit_bits,
+                uint32_t passes, uint32_t* err, cudaStream_t s);
+
+// traversal (sq_trace.cu)
+struct TraceArgs {
+    const sq::Node* nodes;
+    uint32_t node_count;  // indices are checked against these; a bad index
+    uint32_t tri_count;   // ends the ray and raises SQ_DEVERR_TOPOLOGY
+    uint32_t root;
+    const float* tris;
+    uint32_t mode;        // sq_trace_mode
+    uint32_t ray_kind;    // sq_ray_kind
+    uint32_t width, height;
+    float cam[14];        // reference camera: origin in [0..2]; pinhole: basis
+    const float* rays;    // explicit rays (8 floats each)
+    uint32_t ray_count;
+    sq_hit* hits;         // may be null
+    uint8_t* heat;        // may be null
+    uint32_t* work;       // persistent work counter (zeroed)
+    uint32_t* err;
+    unsigned long long* stats;  // {box tests, triangle tests}, accumulated
+};
+void trace(const TraceArgs& a, cudaStream_t s);
+
+}  // namespace sqk

@@ -1,0 +1,373 @@
+// sq_lbvh.cu -- Morton codes and LBVH emission on the GPU.
+//
+// Pipeline of a Morton build (Builder::build_hierarchy_morton,
+// src/builder.cpp:2474-2508):
+//   k_scene_bounds  union of the triangle AABBs (src/builder.cpp:2206-2215)
+//   k_morton        30-bit codes (src/builder.cpp:2217-2236) + the digit
+//                   histograms of every radix-sort pass, in one read
+//   onesweep sort   (sq_sort.cu)
+//   k_lbvh_climb    topology, bounds and node records in one bottom-up pass
+//
+// The climb builds the same logical tree as recurse_morton /
+// find_split_morton (src/builder.cpp:2281-2409): ranges of fewer than 8
+// triangles become leaf clusters, a range whose first and last codes are
+// equal is split after (count >> 1) + 1 triangles, and any other range is
+// split where the highest differing code bit flips.  The last rule is the
+// binary radix tree over the distinct codes, so runs of equal codes are its
+// leaves.  Each run head climbs that tree bottom-up (Apetrei, "Fast and
+// Simple Agglomerative LBVH Construction", 2014): the parent of a node over
+// [l, r) splits at whichever neighbouring boundary, l or r, has the smaller
+// code XOR, and the second thread to reach a parent continues with the union
+// of both children.  Records go to the range-tree layout described in
+// oracle/sq_oracle.c, so the GPU and the oracle write identical records.
+#include "sq_common.cuh"
+
+#include <cstdio>
+
+namespace {
+
+using namespace sq;
+
+constexpr int kTileTris = 256;  // triangles staged per block iteration
+
+// Stage triangles [first, first + count) of a 16-byte aligned array into
+// shared memory with float4 loads (first is a multiple of kTileTris, so the
+// tile start is 16-byte aligned: 256 * 36 bytes = 9216 bytes).
+__device__ __forceinline__ void stage_tris(const float* __restrict__ tris, uint32_t first, uint32_t count,
+                                           float* s, bool aligned)
+{
+    const uint32_t nf = count * 9u;
+    const float* src = tris + 9ull * first;
+    if (aligned) {
+        const uint32_t nv = nf >> 2;
+        const float4* src4 = reinterpret_cast<const float4*>(src);
+        float4* s4 = reinterpret_cast<float4*>(s);
+        for (uint32_t j = threadIdx.x; j < nv; j += blockDim.x) s4[j] = __ldg(src4 + j);
+        for (uint32_t j = (nv << 2) + threadIdx.x; j < nf; j += blockDim.x) s[j] = __ldg(src + j);
+    } else {
+        for (uint32_t j = threadIdx.x; j < nf; j += blockDim.x) s[j] = __ldg(src + j);
+    }
+}
+
+__device__ __forceinline__ float warp_min(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_max(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+    return v;
+}
+
+// box_ord[k] = ordered(-min_k), box_ord[3 + k] = ordered(max_k); zero-initialised.
+__global__ void __launch_bounds__(256) k_scene_bounds(const float* __restrict__ tris, uint32_t n, uint32_t mode,
+                                                      uint32_t* __restrict__ box_ord, bool aligned)
+{
+    __shared__ __align__(16) float s_tri[kTileTris * 9];
+    __shared__ float s_red[8][6];
+    float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (uint32_t first = blockIdx.x * kTileTris; first < n; first += gridDim.x * kTileTris) {
+        const uint32_t count = min((uint32_t)kTileTris, n - first);
+        __syncthreads();
+        stage_tris(tris, first, count, s_tri, aligned);
+        __syncthreads();
+        if (threadIdx.x < count) {
+            Box b = tri_box(s_tri + 9 * threadIdx.x);
+            if (mode == SQ_MORTON_BOUNDS_CENTROID) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    float c = (b.mn[k] + b.mx[k]) * 0.5f;
+                    mn[k] = fminf(mn[k], c);
+                    mx[k] = fmaxf(mx[k], c);
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) { mn[k] = fminf(mn[k], b.mn[k]); mx[k] = fmaxf(mx[k], b.mx[k]); }
+            }
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { mn[k] = warp_min(mn[k]); mx[k] = warp_max(mx[k]); }
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) { s_red[warp][k] = mn[k]; s_red[warp][3 + k] = mx[k]; }
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int k = threadIdx.x;
+        float v = s_red[0][k];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) v = (k < 3) ? fminf(v, s_red[w][k]) : fmaxf(v, s_red[w][k]);
+        atomicMax(box_ord + k, float_to_ordered(k < 3 ? -v : v));
+    }
+}
+
+// Spread the low 10 bits of v to every third bit (bit i -> bit 3i).
+__device__ __forceinline__ uint32_t spread10(uint32_t v)
+{
+    v &= 0x3FFu;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+__device__ __forceinline__ uint32_t f2u(float x) { return (x >= 0.0f) ? (uint32_t)x : 0u; }
+
+template <int DB, int PASSES>
+__global__ void __launch_bounds__(256) k_morton(const float* __restrict__ tris, uint32_t n, uint32_t mode,
+                                                const uint32_t* __restrict__ box_ord, uint32_t* __restrict__ keys,
+                                                uint32_t* __restrict__ vals, uint32_t* __restrict__ hist, bool aligned)
+{
+    constexpr int RADIX = 1 << DB;
+    __shared__ __align__(16) float s_tri[kTileTris * 9];
+    __shared__ uint32_t s_hist[PASSES * RADIX];
+    for (int j = threadIdx.x; j < PASSES * RADIX; j += blockDim.x) s_hist[j] = 0;
+    float smin[3], ext[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        smin[k] = -ordered_to_float(box_ord[k]);
+        const float smax = ordered_to_float(box_ord[3 + k]);
+        ext[k] = smax - smin[k];
+    }
+    (void)mode;
+    for (uint32_t first = blockIdx.x * kTileTris; first < n; first += gridDim.x * kTileTris) {
+        const uint32_t count = min((uint32_t)kTileTris, n - first);
+        __syncthreads();
+        stage_tris(tris, first, count, s_tri, aligned);
+        __syncthreads();
+        if (threadIdx.x < count) {
+            const Box b = tri_box(s_tri + 9 * threadIdx.x);
+            uint32_t q[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                // centre = (bb_min + bb_max) * 0.5f; (centre - min) / (max - min); * 0x3FF
+                const float c = (b.mn[k] + b.mx[k]) * 0.5f;
+                const float u = (c - smin[k]) / ext[k];
+                q[k] = f2u(u * 1023.0f);
+            }
+            const uint32_t code = spread10(q[0]) | (spread10(q[1]) << 1) | (spread10(q[2]) << 2);
+            const uint32_t i = first + threadIdx.x;
+            keys[i] = code;
+            vals[i] = i;
+#pragma unroll
+            for (int p = 0; p < PASSES; ++p) atomicAdd(&s_hist[p * RADIX + ((code >> (p * DB)) & (RADIX - 1))], 1u);
+        }
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < PASSES * RADIX; j += blockDim.x) {
+        const uint32_t c = s_hist[j];
+        if (c) atomicAdd(hist + j, c);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// climb
+
+struct RunFrame {
+    uint32_t b, e, slot, state;
+    Box acc;
+};
+
+// Halving subtree of a run of >= 8 equal codes over [b0, e0)
+// (find_split_morton's equal-codes case, src/builder.cpp:2288-2289).  Writes
+// every record strictly inside the run; returns the run's box and split.
+__device__ void run_subtree(uint32_t b0, uint32_t e0, uint32_t leaf0, Node* __restrict__ nodes, Box& out_box,
+                            uint32_t& out_split, uint32_t* err)
+{
+    RunFrame st[40];
+    int sp = 0;
+    st[0].b = b0; st[0].e = e0; st[0].slot = 0xFFFFFFFFu; st[0].state = 0;
+    box_reset(st[0].acc);
+    sp = 1;
+    while (sp > 0) {
+        RunFrame& f = st[sp - 1];
+        const uint32_t c = f.e - f.b;
+        if (c < 8) {
+            Box bb;
+            box_reset(bb);
+            for (uint32_t p = f.b; p < f.e; ++p) {
+                const float4 a = reinterpret_cast<const float4*>(nodes + leaf0 + p)[0];
+                const float4 z = reinterpret_cast<const float4*>(nodes + leaf0 + p)[1];
+                Box lb;
+                lb.mn[0] = a.x; lb.mn[1] = a.y; lb.mn[2] = a.z;
+                lb.mx[0] = z.x; lb.mx[1] = z.y; lb.mx[2] = z.z;
+                box_grow(bb, lb);
+            }
+            store_node(nodes + f.slot, bb, leaf0 + f.b, c, 0);
+            --sp;
+            box_grow(st[sp - 1].acc, bb);
+            continue;
+        }
+        const uint32_t q = f.b + (c >> 1) + 1u;
+        if (f.state == 0) {
+            f.state = 1;
+            if (sp >= 40) { raise_error(err, SQ_DEVERR_TOPOLOGY); return; }
+            RunFrame& g = st[sp++];
+            g.b = f.b; g.e = q; g.slot = 2u * q; g.state = 0;
+            box_reset(g.acc);
+        } else if (f.state == 1) {
+            f.state = 2;
+            if (sp >= 40) { raise_error(err, SQ_DEVERR_TOPOLOGY); return; }
+            RunFrame& g = st[sp++];
+            g.b = q; g.e = f.e; g.slot = 2u * q + 1u; g.state = 0;
+            box_reset(g.acc);
+        } else {
+            if (f.slot == 0xFFFFFFFFu) {
+                out_box = f.acc;
+                out_split = q;
+                return;
+            }
+            store_node(nodes + f.slot, f.acc, 2u * q, 2u, 0);
+            const Box done = f.acc;
+            --sp;
+            box_grow(st[sp - 1].acc, done);
+        }
+    }
+}
+
+// Record of a child over [cl, cr) (count cc) in the parent's slot.
+__device__ __forceinline__ void write_child(Node* __restrict__ nodes, uint32_t slot, uint32_t cl, uint32_t cr,
+                                            const Box& b, uint32_t split, uint32_t leaf0)
+{
+    const uint32_t cc = cr - cl;
+    if (cc >= 8) {
+        store_node(nodes + slot, b, 2u * split, 2u, 0);
+    } else if (cc >= 2) {
+        store_node(nodes + slot, b, leaf0 + cl, cc, 0);
+    } else {
+        const float4* src = reinterpret_cast<const float4*>(nodes + leaf0 + cl);
+        const float4 a = __ldcg(src), z = __ldcg(src + 1);
+        reinterpret_cast<float4*>(nodes + slot)[0] = a;
+        reinterpret_cast<float4*>(nodes + slot)[1] = z;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_lbvh_climb(const uint32_t* __restrict__ codes, const uint32_t* __restrict__ perm,
+                                                    const float* __restrict__ tris, uint32_t n, Node* __restrict__ nodes,
+                                                    uint32_t* __restrict__ flags, float4* __restrict__ info, uint32_t* err)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t code = codes[i];
+    if (i > 0 && codes[i - 1] == code) return;  // not a run head
+    uint32_t e = i + 1;
+    while (e < n && e < i + 8 && codes[e] == code) ++e;
+    if (e == i + 8 && e < n && codes[e] == code) {
+        uint32_t lo = e, hi = n;
+        while (lo < hi) {
+            const uint32_t mid = lo + ((hi - lo) >> 1);
+            if (codes[mid] == code) lo = mid + 1; else hi = mid;
+        }
+        e = lo;
+    }
+    const uint32_t leaf0 = 2u * n + 2u;
+    // leaf records of the run and the run box
+    Box box;
+    box_reset(box);
+    for (uint32_t p = i; p < e; ++p) {
+        const uint32_t t = perm[p];
+        float tv[9];
+        load_tri(tris, t, tv);
+        const Box b = tri_box(tv);
+        store_node(nodes + leaf0 + p, b, t, 1u, kLeafFlag);
+        box_grow(box, b);
+    }
+    uint32_t l = i, r = e, split = 0;
+    if (e - i >= 8) run_subtree(i, e, leaf0, nodes, box, split, err);
+
+    for (;;) {
+        if (l == 0 && r == n) {
+            if (n >= 8) store_node(nodes, box, 2u * split, 2u, 0);
+            else store_node(nodes, box, leaf0, n, 0);
+            return;
+        }
+        uint32_t p;
+        bool left;
+        if (l == 0) { p = r; left = true; }
+        else if (r == n) { p = l; left = false; }
+        else {
+            const uint32_t dl = codes[l - 1] ^ codes[l];
+            const uint32_t dr = codes[r - 1] ^ codes[r];
+            if (dr < dl) { p = r; left = true; } else { p = l; left = false; }
+        }
+        float4* mine = info + 2ull * (2ull * p + (left ? 0u : 1u));
+        mine[0] = make_float4(box.mn[0], box.mn[1], box.mn[2], __uint_as_float(left ? l : r));
+        mine[1] = make_float4(box.mx[0], box.mx[1], box.mx[2], __uint_as_float(split));
+        __threadfence();
+        const uint32_t old = atomicAdd(flags + p, 1u);
+        if (old == 0) return;
+        if (old != 1) { raise_error(err, SQ_DEVERR_TOPOLOGY); return; }
+        __threadfence();
+        const float4* sib = info + 2ull * (2ull * p + (left ? 1u : 0u));
+        const float4 s0 = __ldcg(sib), s1 = __ldcg(sib + 1);
+        Box sb;
+        sb.mn[0] = s0.x; sb.mn[1] = s0.y; sb.mn[2] = s0.z;
+        sb.mx[0] = s1.x; sb.mx[1] = s1.y; sb.mx[2] = s1.z;
+        const uint32_t s_end = __float_as_uint(s0.w), s_split = __float_as_uint(s1.w);
+        uint32_t ll, rr;
+        Box lb, rb;
+        uint32_t lsplit, rsplit;
+        if (left) { ll = l; rr = s_end; lb = box; rb = sb; lsplit = split; rsplit = s_split; }
+        else { ll = s_end; rr = r; lb = sb; rb = box; lsplit = s_split; rsplit = split; }
+        if (rr - ll >= 8) {
+            write_child(nodes, 2u * p, ll, p, lb, lsplit, leaf0);
+            write_child(nodes, 2u * p + 1u, p, rr, rb, rsplit, leaf0);
+        }
+        box = lb;
+        box_grow(box, rb);
+        l = ll;
+        r = rr;
+        split = p;
+    }
+}
+
+int g_sms = 0;
+int sms()
+{
+    if (!g_sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sms <= 0) g_sms = kNumSMs;
+    }
+    return g_sms;
+}
+
+}  // namespace
+
+namespace sqk {
+
+void scene_bounds(const float* tris, uint32_t n, uint32_t mode, uint32_t* box_ord, cudaStream_t s)
+{
+    if (n == 0) return;
+    const bool aligned = (reinterpret_cast<uintptr_t>(tris) & 15u) == 0;
+    const uint32_t tiles = (n + kTileTris - 1) / kTileTris;
+    const uint32_t grid = min(tiles, (uint32_t)sms() * 8u);
+    k_scene_bounds<<<grid, 256, 0, s>>>(tris, n, mode, box_ord, aligned);
+}
+
+void morton_codes(const float* tris, uint32_t n, uint32_t mode, const uint32_t* box_ord, uint32_t* keys, uint32_t* vals,
+                  uint32_t* hist, uint32_t digit_bits, uint32_t passes, cudaStream_t s)
+{
+    if (n == 0) return;
+    const bool aligned = (reinterpret_cast<uintptr_t>(tris) & 15u) == 0;
+    const uint32_t tiles = (n + kTileTris - 1) / kTileTris;
+    const uint32_t grid = min(tiles, (uint32_t)sms() * 4u);
+    if (digit_bits == 8 && passes == 4) k_morton<8, 4><<<grid, 256, 0, s>>>(tris, n, mode, box_ord, keys, vals, hist, aligned);
+    else if (digit_bits == 10 && passes == 3) k_morton<10, 3><<<grid, 256, 0, s>>>(tris, n, mode, box_ord, keys, vals, hist, aligned);
+    else if (digit_bits == 6 && passes == 5) k_morton<6, 5><<<grid, 256, 0, s>>>(tris, n, mode, box_ord, keys, vals, hist, aligned);
+}
+
+void lbvh_climb(const uint32_t* codes, const uint32_t* perm, const float* tris, uint32_t n, sq::Node* nodes,
+                uint32_t* flags, float4* info, uint32_t* err, cudaStream_t s)
+{
+    if (n == 0) return;
+    k_lbvh_climb<<<(n + 255) / 256, 256, 0, s>>>(codes, perm, tris, n, nodes, flags, info, err);
+}
+
+}  // namespace sqk

@@ -1,0 +1,287 @@
+// sq_sort.cu -- stable LSD radix sort of (key, value) pairs, onesweep style
+// (Adinets & Merrill, "Onesweep: A Faster Least Significant Digit Radix Sort
+// for GPUs", 2022).
+//
+// Replaces radix_sort / parallel_counting_sort (src/algorithms.h:41-113):
+// both are stable, so the sorted permutation is unique and must match bit for
+// bit.  One histogram pass counts every digit of every pass (fused into the
+// Morton kernel for builds); then one kernel per digit:
+//   - a block takes the next tile from an atomic counter, so tiles are
+//     processed in order and a tile's predecessors are always running;
+//   - warps rank their keys with __match_any_sync (stable: items are ranked
+//     in index order within the warp, warps in index order within the tile);
+//   - the tile publishes its per-digit counts and walks back over earlier
+//     tiles' published counts (decoupled look-back) for its global offsets;
+//     every wait is bounded and raises SQ_DEVERR_LOOKBACK_TIMEOUT instead of
+//     spinning forever;
+//   - keys and values are scattered into shared memory in digit order and
+//     written out so that consecutive threads write consecutive addresses.
+#include "sq_common.cuh"
+
+namespace {
+
+using namespace sq;
+
+constexpr int kBlock = 256;
+constexpr int kItems = 16;
+constexpr int kTile = kBlock * kItems;
+constexpr int kWarps = kBlock / 32;
+constexpr uint32_t kFlagAgg = 1u << 30;
+constexpr uint32_t kFlagInc = 2u << 30;
+constexpr uint32_t kCountMask = (1u << 30) - 1u;
+constexpr uint32_t kSpinLimit = 1u << 22;
+
+template <int RADIX>
+__device__ __forceinline__ void block_exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t* s_tmp)
+{
+    // RADIX values, kBlock threads; each thread owns a contiguous chunk.
+    constexpr int PER = (RADIX + kBlock - 1) / kBlock;
+    uint32_t v[PER];
+    uint32_t sum = 0;
+    const int t = threadIdx.x;
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+        const int d = t * PER + j;
+        v[j] = (d < RADIX) ? in[d] : 0u;
+        sum += v[j];
+    }
+    // exclusive scan of per-thread sums across the block
+    const int lane = t & 31, warp = t >> 5;
+    uint32_t x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_tmp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = (lane < kWarps) ? s_tmp[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < kWarps) s_tmp[lane] = w;
+    }
+    __syncthreads();
+    uint32_t run = x - sum + (warp > 0 ? s_tmp[warp - 1] : 0u);
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+        const int d = t * PER + j;
+        if (d < RADIX) out[d] = run;
+        run += v[j];
+    }
+    __syncthreads();
+}
+
+template <int DB>
+struct Smem {
+    static constexpr int RADIX = 1 << DB;
+    static constexpr size_t bytes = sizeof(uint32_t) * (2 * kTile + kWarps * RADIX + 3 * RADIX + 32);
+};
+
+template <int DB>
+__global__ void __launch_bounds__(kBlock) k_onesweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+                                                     uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n,
+                                                     uint32_t shift, const uint32_t* __restrict__ hist,
+                                                     uint32_t* __restrict__ lookback, uint32_t* __restrict__ counter,
+                                                     uint32_t* err)
+{
+    constexpr int RADIX = 1 << DB;
+    constexpr uint32_t MASK = RADIX - 1;
+    extern __shared__ __align__(16) uint32_t smem[];
+    uint32_t* s_keys = smem;
+    uint32_t* s_vals = s_keys + kTile;
+    uint32_t* s_whist = s_vals + kTile;          // [kWarps][RADIX]
+    uint32_t* s_gbase = s_whist + kWarps * RADIX;  // [RADIX]
+    uint32_t* s_lexcl = s_gbase + RADIX;           // [RADIX]
+    uint32_t* s_bcount = s_lexcl + RADIX;          // [RADIX]
+    uint32_t* s_tmp = s_bcount + RADIX;            // [32]
+    __shared__ uint32_t s_tile;
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) s_tile = atomicAdd(counter, 1u);
+    for (int j = tid; j < kWarps * RADIX; j += kBlock) s_whist[j] = 0;
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t base = tile * (uint32_t)kTile;
+
+    uint32_t k[kItems], v[kItems], rk[kItems];
+    const uint32_t wbase = base + (uint32_t)warp * (kItems * 32);
+#pragma unroll
+    for (int it = 0; it < kItems; ++it) {
+        const uint32_t idx = wbase + it * 32 + lane;
+        if (idx < n) { k[it] = kin[idx]; v[it] = vin[idx]; }
+        else { k[it] = 0xFFFFFFFFu; v[it] = 0; }
+    }
+    const uint32_t lt = (1u << lane) - 1u;
+    uint32_t* wh = s_whist + warp * RADIX;
+#pragma unroll
+    for (int it = 0; it < kItems; ++it) {
+        const uint32_t idx = wbase + it * 32 + lane;
+        const bool valid = idx < n;
+        const uint32_t d = valid ? ((k[it] >> shift) & MASK) : (uint32_t)RADIX;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+        const int leader = __ffs(peers) - 1;
+        uint32_t old = 0;
+        if (lane == leader && valid) {
+            old = wh[d];
+            wh[d] = old + __popc(peers);
+        }
+        old = __shfl_sync(0xFFFFFFFFu, old, leader);
+        rk[it] = old + __popc(peers & lt);
+        __syncwarp();
+    }
+    __syncthreads();
+    // exclusive offsets across warps per digit; block counts
+    for (int d = tid; d < RADIX; d += kBlock) {
+        uint32_t run = 0;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) {
+            const uint32_t c = s_whist[w * RADIX + d];
+            s_whist[w * RADIX + d] = run;
+            run += c;
+        }
+        s_bcount[d] = run;
+        st_release_u32(lookback + (size_t)tile * RADIX + d, (tile == 0 ? kFlagInc : kFlagAgg) | run);
+    }
+    __syncthreads();
+    block_exclusive_scan<RADIX>(hist, s_gbase, s_tmp);
+    block_exclusive_scan<RADIX>(s_bcount, s_lexcl, s_tmp);
+    // decoupled look-back, one digit per thread (or several)
+    for (int d = tid; d < RADIX; d += kBlock) {
+        uint32_t excl = 0;
+        if (tile > 0) {
+            int32_t j = (int32_t)tile - 1;
+            uint32_t spins = 0;
+            for (;;) {
+                const uint32_t w = ld_acquire_u32(lookback + (size_t)j * RADIX + d);
+                const uint32_t f = w & ~kCountMask;
+                if (f == 0) {
+                    if (++spins > kSpinLimit) { raise_error(err, SQ_DEVERR_LOOKBACK_TIMEOUT); break; }
+                    continue;
+                }
+                excl += w & kCountMask;
+                if (f == kFlagInc || j == 0) break;
+                --j;
+            }
+            st_release_u32(lookback + (size_t)tile * RADIX + d, kFlagInc | ((excl + s_bcount[d]) & kCountMask));
+        }
+        s_gbase[d] += excl;
+    }
+    __syncthreads();
+    // local scatter in digit order
+#pragma unroll
+    for (int it = 0; it < kItems; ++it) {
+        const uint32_t idx = wbase + it * 32 + lane;
+        if (idx < n) {
+            const uint32_t d = (k[it] >> shift) & MASK;
+            const uint32_t pos = s_lexcl[d] + wh[d] + rk[it];
+            s_keys[pos] = k[it];
+            s_vals[pos] = v[it];
+        }
+    }
+    __syncthreads();
+    const uint32_t valid_count = min((uint32_t)kTile, n - base);
+    for (uint32_t j = tid; j < valid_count; j += kBlock) {
+        const uint32_t key = s_keys[j];
+        const uint32_t d = (key >> shift) & MASK;
+        const uint32_t gp = s_gbase[d] + (j - s_lexcl[d]);
+        kout[gp] = key;
+        vout[gp] = s_vals[j];
+    }
+}
+
+template <int DB>
+__global__ void __launch_bounds__(256) k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n, uint32_t passes,
+                                                   uint32_t* __restrict__ hist)
+{
+    constexpr int RADIX = 1 << DB;
+    extern __shared__ uint32_t s_hist[];
+    const int total = (int)passes * RADIX;
+    for (int j = threadIdx.x; j < total; j += blockDim.x) s_hist[j] = 0;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t key = keys[i];
+        for (uint32_t p = 0; p < passes; ++p) atomicAdd(&s_hist[p * RADIX + ((key >> (p * DB)) & (RADIX - 1))], 1u);
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < total; j += blockDim.x) {
+        const uint32_t c = s_hist[j];
+        if (c) atomicAdd(hist + j, c);
+    }
+}
+
+template <int DB>
+void launch_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, uint32_t n, uint32_t shift,
+                 const uint32_t* hist, uint32_t* lookback, uint32_t* counter, uint32_t* err, cudaStream_t s)
+{
+    static bool configured = false;
+    const size_t bytes = Smem<DB>::bytes;
+    if (!configured) {
+        cudaFuncSetAttribute(k_onesweep<DB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        configured = true;
+    }
+    const uint32_t tiles = (n + kTile - 1) / kTile;
+    k_onesweep<DB><<<tiles, kBlock, bytes, s>>>(kin, vin, kout, vout, n, shift, hist, lookback, counter, err);
+}
+
+int g_sms = 0;
+int sms()
+{
+    if (!g_sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sms <= 0) g_sms = kNumSMs;
+    }
+    return g_sms;
+}
+
+}  // namespace
+
+namespace sqk {
+
+size_t sort_lookback_words(uint32_t n, uint32_t digit_bits, uint32_t passes)
+{
+    const size_t tiles = (n + kTile - 1) / kTile;
+    return tiles * ((size_t)1 << digit_bits) * passes;
+}
+
+void sort_histogram(const uint32_t* keys, uint32_t n, uint32_t* hist, uint32_t digit_bits, uint32_t passes,
+                    cudaStream_t s)
+{
+    if (n == 0) return;
+    const uint32_t grid = min((n + 255) / 256, (uint32_t)sms() * 4u);
+    const size_t bytes = sizeof(uint32_t) * passes * ((size_t)1 << digit_bits);
+    if (digit_bits == 8) k_sort_hist<8><<<grid, 256, bytes, s>>>(keys, n, passes, hist);
+    else if (digit_bits == 10) k_sort_hist<10><<<grid, 256, bytes, s>>>(keys, n, passes, hist);
+    else k_sort_hist<6><<<grid, 256, bytes, s>>>(keys, n, passes, hist);
+}
+
+int sort_passes(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b, uint32_t* vals_b, uint32_t n, const uint32_t* hist,
+                uint32_t* lookback, uint32_t* counters, uint32_t digit_bits, uint32_t passes, uint32_t* err,
+                cudaStream_t s)
+{
+    if (n == 0) return 0;
+    const size_t radix = (size_t)1 << digit_bits;
+    const size_t lb_words = sort_lookback_words(n, digit_bits, 1);
+    int cur = 0;
+    for (uint32_t p = 0; p < passes; ++p) {
+        const uint32_t* kin = cur ? keys_b : keys_a;
+        const uint32_t* vin = cur ? vals_b : vals_a;
+        uint32_t* kout = cur ? keys_a : keys_b;
+        uint32_t* vout = cur ? vals_a : vals_b;
+        const uint32_t shift = p * digit_bits;
+        const uint32_t* h = hist + p * radix;
+        uint32_t* lb = lookback + p * lb_words;
+        if (digit_bits == 8) launch_pass<8>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, s);
+        else if (digit_bits == 10) launch_pass<10>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, s);
+        else launch_pass<6>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, s);
+        cur ^= 1;
+    }
+    return cur;
+}
+
+}  // namespace sqk

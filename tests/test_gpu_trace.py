@@ -1,0 +1,96 @@
+"""GPU traversal against the reference's golden heatmaps and the oracle."""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name", ["ico3", "ico4", "soup3k", "dups2k"])
+def test_reference_tree_heatmap_golden(ctx, name):
+    """The reference's own SAH tree, uploaded unchanged and traced on the GPU
+    with the reference's camera: heatmap bytes identical to trace()."""
+    g = load_golden(name)
+    bvh = ctx.import_node1(g["sah8_nodes"], int(g["sah8_root"]), g["tris"])
+    w, h = int(g["w"]), int(g["h"])
+    hits, heat = ctx.trace(bvh, "ref", camera="reference", width=w, height=h, origin=g["cam"], heatmap=True)
+    assert np.array_equal(heat, g["heat"])
+    assert np.array_equal(hits["tests"], g["ref_tests"])
+    assert np.array_equal((hits["id"] != 0xFFFFFFFF).astype(np.uint32), g["ref_hit"])
+
+
+def test_drop_in_trace(lib_built):
+    """The reference-named interface: trace(hierarchy, w, h, origin)."""
+    import sequoia_gb300 as sq
+    g = load_golden("ico4")
+    hier = sq.Hierarchy(g["sah8_nodes"], int(g["sah8_root"]), g["tris"])
+    heat = sq.trace(hier, int(g["w"]), int(g["h"]), g["cam"])
+    assert np.array_equal(heat, g["heat"])
+
+
+def scenes_for_trace():
+    from sequoia_gb300 import scenes
+    return {
+        "ico4": scenes.displaced_icosphere(4, seed=1),
+        "soup20k": scenes.gaussian_soup(20_000, 8, seed=21),
+    }
+
+
+@pytest.mark.parametrize("name", ["ico4", "soup20k"])
+@pytest.mark.parametrize("mode", ["ref", "closest", "anyhit"])
+def test_trace_matches_oracle_pinhole(ctx, oracle, name, mode):
+    tris = scenes_for_trace()[name]
+    lo, hi = tris.reshape(-1, 3).min(0), tris.reshape(-1, 3).max(0)
+    eye = (0.0, 0.0, float(lo[2]) - 2.0 * float(hi[2] - lo[2]))
+    w, h = 320, 200
+    bvh = ctx.build(tris, "morton")
+    nodes, root = bvh.export_node1()
+    hits, heat = ctx.trace(bvh, mode, camera="pinhole", width=w, height=h, origin=eye, target=(0, 0, 0),
+                           up=(0, 1, 0), vfov=60.0, heatmap=True)
+    rays = oracle.rays_pinhole(w, h, eye, (0, 0, 0), (0, 1, 0), 60.0)
+    m = {"ref": 0, "closest": 1, "anyhit": 2}[mode]
+    ids, ts, tests = oracle.trace(nodes, root, tris, rays, m)
+    assert np.array_equal(hits["id"], ids)
+    assert np.array_equal(hits["tests"], tests)
+    assert np.array_equal(hits["t"], ts)
+    assert np.array_equal(heat, oracle.heatmap(tests))
+    if mode == "closest":
+        bids, bts = oracle.brute_closest(tris, rays[::7])
+        assert np.array_equal(hits["id"][::7], bids)
+
+
+def test_trace_explicit_random_rays(ctx, oracle):
+    from sequoia_gb300 import scenes
+    tris = scenes.gaussian_soup(50_000, 16, seed=31)
+    lo, hi = scenes.scene_box(tris)
+    rays = scenes.random_rays(100_000, lo, hi, seed=32)
+    bvh = ctx.build(tris, "morton")
+    nodes, root = bvh.export_node1()
+    for mode, m in (("closest", 1), ("anyhit", 2), ("ref", 0)):
+        hits, _ = ctx.trace(bvh, mode, rays=rays)
+        ids, ts, tests = oracle.trace(nodes, root, tris, rays, m)
+        assert np.array_equal(hits["id"], ids), mode
+        assert np.array_equal(hits["tests"], tests), mode
+        assert np.array_equal(hits["t"], ts), mode
+    bids, bts = oracle.brute_closest(tris, rays[:2000])
+    hits, _ = ctx.trace(bvh, "closest", rays=rays[:2000].copy())
+    assert np.array_equal(hits["id"], bids)
+    assert np.array_equal(hits["t"], bts)
+
+
+def test_closest_t_vs_fp64(ctx, oracle):
+    """t agrees with an FP64 re-intersection to within 1e-6 relative (stated
+    bound; the measured maximum is printed)."""
+    from sequoia_gb300 import scenes
+    tris = scenes.displaced_icosphere(5, seed=1)
+    w, h = 256, 256
+    bvh = ctx.build(tris, "morton")
+    hits, _ = ctx.trace(bvh, "closest", camera="pinhole", width=w, height=h, origin=(0, 0, 3), target=(0, 0, 0),
+                        up=(0, 1, 0), vfov=60.0)
+    rays = oracle.rays_pinhole(w, h, (0, 0, 3), (0, 0, 0), (0, 1, 0), 60.0)
+    t64 = oracle.reintersect_f64(tris, rays, hits["id"])
+    m = hits["id"] != 0xFFFFFFFF
+    rel = np.abs(hits["t"][m].astype(np.float64) - t64[m]) / np.abs(t64[m])
+    print("max rel t error vs FP64: %.3g, mean %.3g" % (rel.max(), rel.mean()))
+    assert rel.max() < 1e-6

@@ -1,0 +1,80 @@
+"""The CPU oracle against golden outputs of the Sequoia reference itself
+(tests/golden, produced by tests/golden/make_golden.py)."""
+import numpy as np
+
+from conftest import load_golden
+
+
+def canon(nodes, idx, depth=0):
+    nd = nodes[idx]
+    b = tuple(nd["min"].tolist()) + tuple(nd["max"].tolist())
+    if nd["flags"] & 1:
+        return ("L", int(nd["child"]), b)
+    ch = sorted((canon(nodes, int(nd["child"]) + k, depth + 1) for k in range(int(nd["count"]))), key=repr)
+    return ("N", b, tuple(ch))
+
+
+def test_morton_codes(oracle, golden):
+    codes, box = oracle.morton_codes(golden["tris"])
+    assert np.array_equal(codes, golden["codes"])
+    assert np.array_equal(box, golden["scene"])
+
+
+def test_radix_sort(oracle, golden):
+    n = len(golden["codes"])
+    k, v = oracle.sort_pairs(golden["codes"], golden["code_index"])
+    assert np.array_equal(k, golden["sorted_codes"])
+    assert np.array_equal(v, golden["sorted_index"])
+    # the sorted permutation is the unique stable one
+    order = np.lexsort((np.arange(n), golden["codes"]))
+    assert np.array_equal(v, order.astype(np.uint32))
+
+
+def test_find_split(oracle, golden):
+    sc = golden["sorted_codes"]
+    for a, b, s in zip(golden["splits_begin"], golden["splits_end"], golden["splits"]):
+        assert oracle.find_split_morton(sc[a:b]) == s
+
+
+def test_sah_tree_matches_reference(oracle, golden):
+    import sys
+    sys.setrecursionlimit(100000)
+    found = 0
+    for bins in (8, 16, 32):
+        key = "sah%d_nodes" % bins
+        if key not in golden:
+            continue
+        found += 1
+        rn, rroot = golden[key], int(golden["sah%d_root" % bins])
+        on, oroot, _ = oracle.build_sah(golden["tris"], bins, 8)
+        assert canon(rn, rroot) == canon(on, oroot), bins
+    assert found >= 1
+
+
+def test_grid_tree_matches_reference(oracle, golden):
+    import sys
+    sys.setrecursionlimit(100000)
+    if "grid_nodes" not in golden:
+        return
+    on, oroot, _ = oracle.build_grid(golden["tris"], 8, 8, scene_bounds_cells=True)
+    assert canon(golden["grid_nodes"], int(golden["grid_root"])) == canon(on, oroot)
+
+
+def test_reference_trace_heatmap(oracle, golden):
+    """trace() on the reference's own SAH tree: per-ray test counts, hit
+    flags and the heatmap bytes, bit-exact."""
+    w, h = int(golden["w"]), int(golden["h"])
+    rays = oracle.rays_reference_camera(w, h, golden["cam"])
+    nodes, root = golden["sah8_nodes"], int(golden["sah8_root"])
+    ids, _, tests = oracle.trace(nodes, root, golden["tris"], rays, 0)
+    assert np.array_equal(tests, golden["ref_tests"])
+    assert np.array_equal((ids != oracle.NO_HIT).astype(np.uint32), golden["ref_hit"])
+    assert np.array_equal(oracle.heatmap(tests), golden["heat"])
+
+
+def test_oracle_trees_valid(oracle, golden):
+    n = len(golden["tris"])
+    for build in (lambda t: oracle.build_morton(t)[:2], lambda t: oracle.build_sah(t, 16, 4)[:2],
+                  lambda t: oracle.build_grid(t, 8, 8)[:2]):
+        nodes, root = build(golden["tris"])
+        assert (oracle.leaf_reach(nodes, root, n) == 1).all()
