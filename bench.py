@@ -198,7 +198,8 @@ def main():
     tris = make_scene()
     n = len(tris)
     rays_total = w["width"] * w["height"]
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)  # torch work (L2 flush, events) and the library share one stream
     ctx = sq.Context(local, stream=stream.cuda_stream)
     d_tris = torch.from_numpy(tris).to("cuda")
     d_hits = torch.empty(rays_total * 3, dtype=torch.int32, device="cuda")

@@ -93,8 +93,11 @@ typedef struct sq_hit {
 typedef struct sq_options {
     int device;      /* CUDA device ordinal                                  */
     void* stream;    /* cudaStream_t to run on; NULL = context-owned stream  */
-    uint32_t flags;  /* reserved, 0                                          */
+    uint32_t flags;  /* SQ_OPT_*                                             */
 } sq_options;
+/* Run on options->stream exactly as given, even when it is NULL (the legacy
+ * default stream), instead of creating a context-owned stream.              */
+#define SQ_OPT_EXTERNAL_STREAM 0x1u
 
 typedef enum sq_builder_kind {
     SQ_BUILDER_MORTON = 0, /* Builder::build_hierarchy_morton (src/builder.cpp:2474) */

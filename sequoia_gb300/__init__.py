@@ -184,7 +184,7 @@ class Context:
 
     def __init__(self, device: int = 0, stream=None):
         L = load_library()
-        opt = _Options(device, stream if stream is not None else None, 0)
+        opt = _Options(device, stream if stream is not None else None, 1 if stream is not None else 0)
         h = C.c_void_p()
         st = L.sq_create(C.byref(h), C.byref(opt))
         if st != 0:

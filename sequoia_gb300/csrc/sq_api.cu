@@ -246,7 +246,7 @@ sq_status sq_create(sq_ctx** out, const sq_options* options)
         return SQ_ERR_INVALID;
     }
     Guard g(c->device);
-    if (options && options->stream) {
+    if (options && (options->stream || (options->flags & SQ_OPT_EXTERNAL_STREAM))) {
         c->stream = static_cast<cudaStream_t>(options->stream);
     } else {
         if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
