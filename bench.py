@@ -177,6 +177,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -256,9 +257,10 @@ def main():
     h_tris = torch.from_numpy(tris).pin_memory()
     h_hits = torch.empty(rays_total * 3, dtype=torch.int32).pin_memory()
     h_heat = torch.empty(rays_total * 3, dtype=torch.uint8).pin_memory()
-    step(h_tris, h_hits, h_heat).free()
     e2e_ms = []
-    for _ in range(args.steps):
+    if not args.no_e2e:
+        step(h_tris, h_hits, h_heat).free()
+    for _ in range(0 if args.no_e2e else args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -266,7 +268,7 @@ def main():
         torch.cuda.synchronize()
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
         bvh.free()
-    e2e_total = float(sum(e2e_ms))
+    e2e_total = float(sum(e2e_ms)) if e2e_ms else float("nan")
     if dist:
         t = torch.tensor([e2e_total], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)

@@ -40,7 +40,8 @@ typedef enum sq_status {
     SQ_ERR_OOM = 3,         /* device or pinned allocation failed             */
     SQ_ERR_DEVICE = 4,      /* a kernel raised the device error word          */
     SQ_ERR_UNSUPPORTED = 5, /* valid request this build does not implement    */
-    SQ_ERR_NO_DEVICE = 6    /* no CUDA device / extension unusable            */
+    SQ_ERR_NO_DEVICE = 6,   /* no CUDA device / extension unusable            */
+    SQ_ERR_TOO_LARGE = 7    /* request exceeds a fixed capacity (see below)   */
 } sq_status;
 
 /* Device error word bits (sq_device_error) */
@@ -218,6 +219,25 @@ sq_status sq_radix_sort_pairs(sq_ctx* ctx, const uint32_t* keys_in,
 /* The sorted Morton codes and triangle permutation of the last Morton build
  * of this BVH (n entries each).                                              */
 sq_status sq_bvh_export_sorted(sq_bvh* bvh, uint32_t* codes, uint32_t* perm);
+
+/* Radix sort that allocates nothing.  No counterpart in the reference: it is
+ * for callers that cannot call cudaMalloc / cudaFree (for example a host
+ * whose memory pool has already reserved the GPU's memory, or a loop that
+ * cannot afford cudaFree's implicit device synchronisation).  Same result as
+ * sq_radix_sort_pairs, but every pointer must be device memory of the current
+ * device, no context is used, and the sort's scratch is one fixed device
+ * array inside the library (about 12.6 MB, held on each GPU where the
+ * library's code is loaded until the process exits).  n above
+ * SQ_NOALLOC_MAX_KEYS returns SQ_ERR_TOO_LARGE before touching anything.
+ * Runs on `stream` (NULL = legacy default stream) and returns when the sort
+ * has finished.  The first call on a device looks up the scratch address
+ * there; make it before any stream capture.  Calls share the scratch, so
+ * calls that overlap on the GPU race and must not be issued.  keys_out /
+ * values_out may alias keys_in / values_in.                                */
+#define SQ_NOALLOC_MAX_KEYS (1u << 20)
+sq_status sq_radix_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* values_in, uint32_t n,
+                                      uint32_t key_bits, uint32_t digit_bits, uint32_t* keys_out,
+                                      uint32_t* values_out, void* stream);
 
 /* ---- trace -------------------------------------------------------------- */
 

@@ -31,7 +31,7 @@ HIT = np.dtype([("id", "<u4"), ("t", "<f4"), ("tests", "<u4")])
 MODES = {"ref": 0, "closest": 1, "anyhit": 2}
 BUILDERS = {"morton": 0, "sah": 1, "recursive": 1, "grid": 2}
 STATUS = {0: "OK", 1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "device error",
-          5: "unsupported", 6: "no CUDA device"}
+          5: "unsupported", 6: "no CUDA device", 7: "exceeds a fixed capacity"}
 
 
 class SequoiaError(RuntimeError):
