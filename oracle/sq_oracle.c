@@ -425,6 +425,19 @@ static inline float bin_k1(int nb, float ext)
     return num / ext;
 }
 
+/* leaf creation (src/builder.cpp:1075-1089): a cluster record over the
+ * leaf region, or the leaf record itself for one triangle below the root */
+static void sah_leaf(sah_job* j, uint32_t b, uint32_t cnt, const box* p, uint32_t slot, int is_root)
+{
+    if (cnt > 65535u) { j->fail = 1; return; }
+    if (cnt == 1 && !is_root) {
+        uint32_t t = j->ids[b];
+        write_leaf(&j->nodes[slot], &j->tb[t], t);
+        return;
+    }
+    write_inner(&j->nodes[slot], p, j->leaf0 + b, cnt);
+}
+
 /* recurse (src/builder.cpp:1053-1156): node over ids[b, e) with primitive box
  * p and centroid box c; writes its record into `slot`.  The partition is
  * stable; the reference's in-place swap partition (src/builder.cpp:599-628)
@@ -434,13 +447,7 @@ static void sah_range(sah_job* j, uint32_t b, uint32_t e, const box* p, const bo
 {
     uint32_t cnt = e - b;
     if (cnt <= j->leaf || box_sa(c) <= 0.0f) {
-        if (cnt > 65535u) { j->fail = 1; return; }
-        if (cnt == 1 && !is_root) {
-            uint32_t t = j->ids[b];
-            write_leaf(&j->nodes[slot], &j->tb[t], t);
-            return;
-        }
-        write_inner(&j->nodes[slot], p, j->leaf0 + b, cnt);
+        sah_leaf(j, b, cnt, p, slot, is_root);
         return;
     }
     int nb = (int)j->bins;
@@ -463,7 +470,7 @@ static void sah_range(sah_job* j, uint32_t b, uint32_t e, const box* p, const bo
     for (int i = 1; i < nb - 1; ++i) l2r[i] = bin_combine(&l2r[i - 1], &bins[i]);
     bin r2l = bins[nb - 1];
     float best = FLT_MAX;
-    int plane = 0;
+    int plane = 0, chosen = 0;
     box lp, rp, lc, rc;
     box_reset(&lp); box_reset(&rp); box_reset(&lc); box_reset(&rc);
     for (int i = nb - 2; i >= 0; --i) {
@@ -473,9 +480,17 @@ static void sah_range(sah_job* j, uint32_t b, uint32_t e, const box* p, const bo
         if (score < best) {
             best = score;
             plane = i;
+            chosen = 1;
             lp = l2r[i].p; rp = r2l.p; lc = l2r[i].c; rc = r2l.c;
         }
         r2l = bin_combine(&r2l, &bins[i]);
+    }
+    if (!chosen) {
+        /* no plane scored below FLT_MAX (only with coordinates near the float
+         * range); the reference would split with unset child boxes here.  Both
+         * this oracle and the GPU builder make the node a leaf instead. */
+        sah_leaf(j, b, cnt, p, slot, is_root);
+        return;
     }
     /* stable partition by bin <= plane */
     uint32_t nl = 0, nr = 0;
@@ -487,14 +502,9 @@ static void sah_range(sah_job* j, uint32_t b, uint32_t e, const box* p, const bo
     }
     memcpy(j->ids + b + nl, j->tmp + b, sizeof(uint32_t) * nr);
     if (nl == 0 || nr == 0) {
-        /* cannot happen for a plane with a finite score; keep going with a
-         * median cut so the oracle stays total (the reference would assert,
-         * src/builder.cpp:1112-1113) */
-        nl = cnt / 2;
-        nr = cnt - nl;
-        box_reset(&lp); box_reset(&rp); box_reset(&lc); box_reset(&rc);
-        for (uint32_t i = b; i < b + nl; ++i) { box_grow_box(&lp, &j->tb[j->ids[i]]); box_grow_pt(&lc, j->cen + 3 * (size_t)j->ids[i]); }
-        for (uint32_t i = b + nl; i < e; ++i) { box_grow_box(&rp, &j->tb[j->ids[i]]); box_grow_pt(&rc, j->cen + 3 * (size_t)j->ids[i]); }
+        /* cannot happen for a plane with a finite score */
+        j->fail = 1;
+        return;
     }
     uint32_t q = b + nl;
     uint32_t ls = j->base + 2u * q, rs = ls + 1u;

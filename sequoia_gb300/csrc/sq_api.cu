@@ -25,6 +25,7 @@ struct sq_ctx {
     std::map<void*, size_t> live_blocks;
     cudaEvent_t ev[8] = {};
     bool build_timed = false, trace_timed = false;
+    uint32_t* host_ctl = nullptr;  // pinned, 64 bytes: per-level task counts of the SAH build
 };
 
 struct sq_bvh {
@@ -223,6 +224,50 @@ sq_status build_morton(sq_ctx* c, sq_bvh* b, const sq_build_params& p)
     return SQ_OK;
 }
 
+// Binned SAH or grid build into b.
+sq_status build_sah(sq_ctx* c, sq_bvh* b, const sq_build_params& p, int grid)
+{
+    const uint32_t n = b->n;
+    const uint32_t nb = p.sah_bins ? p.sah_bins : 8u;
+    const uint32_t leaf = p.leaf_size ? p.leaf_size : 8u;
+    if (nb < 2 || nb > 32) return fail(c, SQ_ERR_INVALID, "sah_bins must be 2..32");
+    void* ws = dalloc(c, sqk::sah_workspace_bytes(n));
+    uint32_t* sortb = nullptr;
+    uint32_t* zero = nullptr;
+    size_t z_words = 0;
+    if (grid) {
+        sortb = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * 4ull * n));
+        z_words = 8 + sqk::sort_lookback_words(n, 6, 1);
+        zero = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * z_words));
+    }
+    float* scene = static_cast<float*>(dalloc(c, 64));
+    if (!ws || (grid && (!sortb || !zero)) || !scene) {
+        dfree(c, ws); dfree(c, sortb); dfree(c, zero); dfree(c, scene);
+        return fail(c, SQ_ERR_OOM, "SAH workspace allocation failed (n=%u)", n);
+    }
+    cudaStream_t s = c->stream;
+    SQ_CUDA(c, cudaEventRecord(c->ev[0], s));
+    if (grid) SQ_CUDA(c, cudaMemsetAsync(zero, 0, sizeof(uint32_t) * z_words, s));
+    SQ_CUDA(c, cudaEventRecord(c->ev[1], s));
+    const int rc = sqk::build_sah(b->tris, n, nb, leaf, grid, p.flags & SQ_BUILD_GRID_SCENE_BOUNDS, b->nodes, scene, ws,
+                                  sortb, grid ? sortb + n : nullptr, grid ? sortb + 2ull * n : nullptr,
+                                  grid ? sortb + 3ull * n : nullptr, grid ? zero + 8 : nullptr, zero, c->ctrl,
+                                  c->host_ctl, s);
+    if (rc != 0) {
+        dfree(c, ws); dfree(c, sortb); dfree(c, zero); dfree(c, scene);
+        return fail(c, SQ_ERR_CUDA, "SAH build: %s", cudaGetErrorString((cudaError_t)rc));
+    }
+    SQ_CUDA(c, cudaEventRecord(c->ev[2], s));
+    SQ_CUDA(c, cudaEventRecord(c->ev[3], s));
+    SQ_CUDA(c, cudaMemcpyAsync(c->host_ctl + 8, scene, 6 * sizeof(float), cudaMemcpyDeviceToHost, s));
+    SQ_CUDA(c, cudaStreamSynchronize(s));
+    memcpy(b->scene, c->host_ctl + 8, 6 * sizeof(float));
+    c->build_timed = true;
+    dfree(c, ws); dfree(c, sortb); dfree(c, zero); dfree(c, scene);
+    b->root = 0;
+    return SQ_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -261,6 +306,11 @@ sq_status sq_create(sq_ctx** out, const sq_options* options)
         return SQ_ERR_OOM;
     }
     for (auto& e : c->ev) cudaEventCreate(&e);
+    if (cudaHostAlloc(reinterpret_cast<void**>(&c->host_ctl), 64, cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        sq_destroy(c);
+        return SQ_ERR_OOM;
+    }
     *out = c;
     return SQ_OK;
 }
@@ -274,6 +324,7 @@ sq_status sq_destroy(sq_ctx* c)
     for (auto& kv : c->live_blocks) cudaFree(kv.first);
     for (auto& e : c->ev) cudaEventDestroy(e);
     cudaFree(c->ctrl);
+    if (c->host_ctl) cudaFreeHost(c->host_ctl);
     if (c->own_stream) cudaStreamDestroy(c->stream);
     delete c;
     return SQ_OK;
@@ -297,8 +348,7 @@ sq_status sq_build(sq_ctx* c, const sq_triangle* tris, uint32_t n, const sq_buil
     sq_build_params p = *params;
     if (p.kind != SQ_BUILDER_MORTON && p.kind != SQ_BUILDER_SAH && p.kind != SQ_BUILDER_GRID)
         return fail(c, SQ_ERR_INVALID, "sq_build: unknown builder kind %u", p.kind);
-    if (p.kind != SQ_BUILDER_MORTON) return fail(c, SQ_ERR_UNSUPPORTED, "sq_build: builder kind %u not built yet", p.kind);
-    const uint32_t cap = 3u * n + 2u;
+    const uint32_t cap = (p.kind == SQ_BUILDER_GRID ? 128u : 0u) + 3u * n + 2u;
     sq_bvh* b = nullptr;
     sq_status st = new_bvh(c, n, cap, &b);
     if (st != SQ_OK) return st;
@@ -316,7 +366,8 @@ sq_status sq_build(sq_ctx* c, const sq_triangle* tris, uint32_t n, const sq_buil
         *out = b;
         return SQ_OK;
     }
-    st = build_morton(c, b, p);
+    if (p.kind == SQ_BUILDER_MORTON) st = build_morton(c, b, p);
+    else st = build_sah(c, b, p, p.kind == SQ_BUILDER_GRID);
     if (st != SQ_OK) { sq_bvh_free(b); return st; }
     *out = b;
     return SQ_OK;

@@ -147,6 +147,13 @@ int sort_passes(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b, uint32_t* 
                 const uint32_t* hist, uint32_t* lookback, uint32_t* counters, uint32_t digit_bits,
                 uint32_t passes, uint32_t* err, cudaStream_t s);
 
+// binned SAH / grid builders (sq_sah.cu)
+size_t sah_workspace_bytes(uint32_t n);
+int build_sah(const float* tris, uint32_t n, uint32_t nb, uint32_t leaf_size, int grid, uint32_t scene_box_cells,
+              sq::Node* nodes, float* scene_out, void* ws, uint32_t* sort_keys, uint32_t* sort_vals,
+              uint32_t* sort_alt_keys, uint32_t* sort_alt_vals, uint32_t* sort_lookback, uint32_t* sort_counters,
+              uint32_t* err, uint32_t* host_ctl, cudaStream_t s);
+
 // traversal (sq_trace.cu)
 struct TraceArgs {
     const sq::Node* nodes;

@@ -1,0 +1,944 @@
+// sq_sah.cu -- binned SAH and grid BVH builders on the GPU.
+//
+// Same logical tree as the reference's binned SAH build (recurse /
+// recurse_omp / build_hierarchy, src/builder.cpp:1053-1156, 1365-1477,
+// 1576-1618) and grid build (src/builder.cpp:1665-1753, 2133-2194), with the
+// bin count and leaf size as parameters:
+//   leaf        count <= leaf_size, or centroid box area <= 0
+//   axis        choose_axis (src/builder.cpp:334-345)
+//   bins        bin = int(k1 * (c[axis] - cmin)), k1 = bins*(1-2^-23)/extent
+//               (src/builder.cpp:372-398)
+//   plane       left-to-right unions, right-to-left sweep, score
+//               sa(L)*nL + sa(R)*nR, strict <, ties to the higher plane
+//               (src/builder.cpp:488-523)
+//   partition   bin <= plane goes left.  The reference swaps in place
+//               (src/builder.cpp:599-628); this builder partitions stably.
+//               Both yield the same two sets, so the same tree.
+//   children    their primitive and centroid boxes come from the bins.
+// Records are written in the range-tree layout (oracle/sq_oracle.c), so the
+// result is record-for-record the oracle's.
+//
+// Schedule:
+//   large nodes (> kSmall triangles): level by level.  Chunks of kChunk
+//     triangles bin into per-warp shared bins (warp-aggregated with
+//     __match_any_sync + __reduce_max_sync on order-preserving integer
+//     encodings), then one atomic per bin value and block; one warp per node
+//     sweeps the planes; a count / scan / scatter triple partitions stably
+//     into the other id buffer.
+//   small nodes: one warp per subtree, smaller child first (stack depth
+//     O(log n)), binning and partitioning with warp intrinsics only.
+#include "sq_common.cuh"
+
+#include <utility>
+
+namespace {
+
+using namespace sq;
+
+constexpr uint32_t kChunk = 2048;
+constexpr uint32_t kSmall = 1024;
+constexpr int kMaxBins = 32;
+constexpr int kBinWords = 13;  // -pmin xyz, pmax xyz, -cmin xyz, cmax xyz (ordered ints), count
+constexpr int kStackDepth = 24;
+
+struct __align__(16) Task {
+    uint32_t begin, count, slot, flags;  // flags: bit0 = ids live in buffer B, bit1 = root-like record
+    float pmn[3], pmx[3], cmn[3], cmx[3];
+};
+static_assert(sizeof(Task) == 64, "Task is 64 bytes");
+
+struct LeafRange {
+    uint32_t begin, count, slot, flags;
+    float pmn[3], pmx[3];
+    uint32_t pad[2];
+};
+static_assert(sizeof(LeafRange) == 48, "LeafRange is 48 bytes");
+
+struct Split {
+    int plane;   // -1: no split (leaf)
+    int axis;
+    float k1, cmin;
+    uint32_t nl;
+    uint32_t pad[3];
+};
+
+struct Ctl {
+    uint32_t n_large_next, n_small, n_leaf, small_pop;
+    uint32_t err_bits, pad[3];
+};
+
+__device__ __forceinline__ float box_sa(const float* mn, const float* mx)
+{
+    const float lx = mx[0] - mn[0], ly = mx[1] - mn[1], lz = mx[2] - mn[2];
+    const float xy = lx * ly, xz = lx * lz, yz = ly * lz;
+    float s = xy + xz;
+    s = s + yz;
+    return s * 2.0f;
+}
+
+__device__ __forceinline__ int choose_axis(const float* mn, const float* mx)
+{
+    const float lx = mx[0] - mn[0], ly = mx[1] - mn[1], lz = mx[2] - mn[2];
+    int r = 0;
+    r += 2 * (lz > lx && lz > ly);
+    r += 1 * (ly > lx && ly >= lz);
+    return r;
+}
+
+__device__ __forceinline__ float bin_k1(int nb, float ext)
+{
+    const float eps = 1.1920929e-7f;
+    const float one_minus = 1.0f - eps;
+    const float num = (float)nb * one_minus;
+    return num / ext;
+}
+
+__device__ __forceinline__ int bin_of(float k1, float c, float cmin, int nb)
+{
+    const float d = c - cmin;
+    const float x = k1 * d;
+    int b = (x == x) ? (int)x : 0;  // cvt.rzi saturates; NaN -> 0
+    b = b < 0 ? 0 : b;
+    return b > nb - 1 ? nb - 1 : b;
+}
+
+__device__ __forceinline__ void load_box(const float4* __restrict__ tb, uint32_t id, float* mn, float* mx)
+{
+    const float4 a = __ldg(tb + 2ull * id), b = __ldg(tb + 2ull * id + 1);
+    mn[0] = a.x; mn[1] = a.y; mn[2] = a.z;
+    mx[0] = b.x; mx[1] = b.y; mx[2] = b.z;
+}
+
+__device__ __forceinline__ float sel(const float* v, int k) { return k == 0 ? v[0] : (k == 1 ? v[1] : v[2]); }
+
+// ---------------------------------------------------------------------------
+// setup: triangle boxes, identity ids, root boxes
+
+__global__ void __launch_bounds__(256) k_sah_setup(const float* __restrict__ tris, uint32_t n, float4* __restrict__ tb,
+                                                   uint32_t* __restrict__ ids, uint32_t* __restrict__ root_ord)
+{
+    float v[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) v[k] = -FLT_MAX;  // max of (-pmin, pmax, -cmin, cmax)
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float t[9];
+        load_tri(tris, i, t);
+        const Box b = tri_box(t);
+        tb[2ull * i] = make_float4(b.mn[0], b.mn[1], b.mn[2], 0.0f);
+        tb[2ull * i + 1] = make_float4(b.mx[0], b.mx[1], b.mx[2], 0.0f);
+        ids[i] = i;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float c = (b.mn[k] + b.mx[k]) * 0.5f;
+            v[k] = fmaxf(v[k], -b.mn[k]);
+            v[3 + k] = fmaxf(v[3 + k], b.mx[k]);
+            v[6 + k] = fmaxf(v[6 + k], -c);
+            v[9 + k] = fmaxf(v[9 + k], c);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] = fmaxf(v[k], __shfl_xor_sync(0xFFFFFFFFu, v[k], o));
+    }
+    __shared__ float s[8][12];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0)
+        for (int k = 0; k < 12; ++k) s[warp][k] = v[k];
+    __syncthreads();
+    if (threadIdx.x < 12) {
+        float m = s[0][threadIdx.x];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, s[w][threadIdx.x]);
+        atomicMax(root_ord + threadIdx.x, float_to_ordered(m));
+    }
+}
+
+__device__ __forceinline__ float dec_neg(uint32_t u) { return -ordered_to_float(u); }
+__device__ __forceinline__ float dec_pos(uint32_t u) { return ordered_to_float(u); }
+
+// Place a task: leaf (recorded in the leaf list), large, or small.
+__device__ void classify(const Task& t, uint32_t leaf_size, Task* __restrict__ large_next, Task* __restrict__ small,
+                         LeafRange* __restrict__ leaves, Ctl* ctl)
+{
+    const bool leaf = t.count <= leaf_size || !(box_sa(t.cmn, t.cmx) > 0.0f);
+    if (leaf) {
+        const uint32_t k = atomicAdd(&ctl->n_leaf, 1u);
+        LeafRange lr;
+        lr.begin = t.begin; lr.count = t.count; lr.slot = t.slot; lr.flags = t.flags;
+        for (int a = 0; a < 3; ++a) { lr.pmn[a] = t.pmn[a]; lr.pmx[a] = t.pmx[a]; }
+        lr.pad[0] = lr.pad[1] = 0;
+        leaves[k] = lr;
+    } else if (t.count > kSmall) {
+        large_next[atomicAdd(&ctl->n_large_next, 1u)] = t;
+    } else {
+        small[atomicAdd(&ctl->n_small, 1u)] = t;
+    }
+}
+
+__global__ void k_root_task(const uint32_t* __restrict__ root_ord, uint32_t n, uint32_t leaf_size, Task* large,
+                            Task* small, LeafRange* leaves, Ctl* ctl, float* scene_out)
+{
+    Task t;
+    t.begin = 0; t.count = n; t.slot = 0; t.flags = 2u;
+    for (int k = 0; k < 3; ++k) {
+        t.pmn[k] = dec_neg(root_ord[k]);
+        t.pmx[k] = dec_pos(root_ord[3 + k]);
+        t.cmn[k] = dec_neg(root_ord[6 + k]);
+        t.cmx[k] = dec_pos(root_ord[9 + k]);
+        scene_out[k] = t.pmn[k];
+        scene_out[3 + k] = t.pmx[k];
+    }
+    classify(t, leaf_size, large, small, leaves, ctl);
+}
+
+// ---------------------------------------------------------------------------
+// grid: cells, Morton order, cell tasks
+
+// Morton slot of grid cell (x, y, z) in a 4x4x4 grid: bits x0 y0 z0 x1 y1 z1
+// (the inverse of compact_1_by_2, src/builder.cpp:27-35, 1726-1728).
+__device__ __forceinline__ uint32_t cell_slot(uint32_t x, uint32_t y, uint32_t z)
+{
+    return (x & 1u) | ((y & 1u) << 1) | ((z & 1u) << 2) | ((x & 2u) << 2) | ((y & 2u) << 3) | ((z & 2u) << 4);
+}
+
+__global__ void __launch_bounds__(256) k_grid_bin(const float4* __restrict__ tb, uint32_t n,
+                                                  const uint32_t* __restrict__ root_ord, uint32_t* __restrict__ keys,
+                                                  uint32_t* __restrict__ cell_ord, uint32_t* __restrict__ hist)
+{
+    __shared__ uint32_t s_cell[64 * kBinWords];
+    for (int j = threadIdx.x; j < 64 * kBinWords; j += blockDim.x) s_cell[j] = 0;
+    __syncthreads();
+    float cmn[3], k1[3];
+    for (int a = 0; a < 3; ++a) {
+        cmn[a] = dec_neg(root_ord[6 + a]);
+        const float cmx = dec_pos(root_ord[9 + a]);
+        k1[a] = bin_k1(4, cmx - cmn[a]);
+    }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float mn[3], mx[3], c[3];
+        load_box(tb, i, mn, mx);
+        uint32_t g[3];
+        for (int a = 0; a < 3; ++a) {
+            c[a] = (mn[a] + mx[a]) * 0.5f;
+            g[a] = (uint32_t)bin_of(k1[a], c[a], cmn[a], 4);
+        }
+        const uint32_t m = cell_slot(g[0], g[1], g[2]);
+        keys[i] = m;
+        uint32_t* cb = s_cell + m * kBinWords;
+        for (int a = 0; a < 3; ++a) {
+            atomicMax(cb + a, float_to_ordered(-mn[a]));
+            atomicMax(cb + 3 + a, float_to_ordered(mx[a]));
+            atomicMax(cb + 6 + a, float_to_ordered(-c[a]));
+            atomicMax(cb + 9 + a, float_to_ordered(c[a]));
+        }
+        atomicAdd(cb + 12, 1u);
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < 64 * kBinWords; j += blockDim.x) {
+        const uint32_t v = s_cell[j];
+        if ((j % kBinWords) == 12) {
+            if (v) { atomicAdd(cell_ord + j, v); atomicAdd(hist + j / kBinWords, v); }
+        } else if (v) {
+            atomicMax(cell_ord + j, v);
+        }
+    }
+}
+
+__global__ void k_grid_tasks(const uint32_t* __restrict__ cell_ord, const uint32_t* __restrict__ root_ord, uint32_t n,
+                             uint32_t leaf_size, uint32_t scene_box_cells, Task* large, Task* small,
+                             LeafRange* leaves, Ctl* ctl, float* scene_out)
+{
+    // one thread per cell, in Morton order; cell m covers [begin_m, begin_m + count_m)
+    __shared__ uint32_t s_begin[65];
+    const uint32_t m = threadIdx.x;
+    if (m == 0) {
+        uint32_t sum = 0;
+        for (int j = 0; j < 64; ++j) { s_begin[j] = sum; sum += cell_ord[j * kBinWords + 12]; }
+        s_begin[64] = sum;
+        for (int k = 0; k < 3; ++k) { scene_out[k] = dec_neg(root_ord[k]); scene_out[3 + k] = dec_pos(root_ord[3 + k]); }
+    }
+    __syncthreads();
+    if (m >= 64) return;
+    const uint32_t* cb = cell_ord + m * kBinWords;
+    Task t;
+    t.begin = s_begin[m];
+    t.count = cb[12];
+    t.slot = 63u + m;
+    t.flags = 2u;
+    for (int k = 0; k < 3; ++k) {
+        if (t.count) {
+            t.pmn[k] = dec_neg(cb[k]); t.pmx[k] = dec_pos(cb[3 + k]);
+            t.cmn[k] = dec_neg(cb[6 + k]); t.cmx[k] = dec_pos(cb[9 + k]);
+        } else {
+            t.pmn[k] = FLT_MAX; t.pmx[k] = -FLT_MAX; t.cmn[k] = FLT_MAX; t.cmx[k] = -FLT_MAX;
+        }
+    }
+    if (scene_box_cells) {
+        // the plain grid builder gives every cell node the scene box (src/builder.cpp:2173-2174)
+        for (int k = 0; k < 3; ++k) { t.pmn[k] = dec_neg(root_ord[k]); t.pmx[k] = dec_pos(root_ord[3 + k]); }
+    }
+    classify(t, leaf_size, large, small, leaves, ctl);
+}
+
+// heap of 63 inner nodes above the 64 cell nodes (src/builder.cpp:2181-2188)
+__global__ void k_grid_heap(Node* __restrict__ nodes)
+{
+    if (threadIdx.x != 0) return;
+    for (int i = 62; i >= 0; --i) {
+        const Node a = nodes[2 * i + 1], b = nodes[2 * i + 2];
+        Box u;
+        u.mn[0] = ref_min(a.mnx, b.mnx); u.mn[1] = ref_min(a.mny, b.mny); u.mn[2] = ref_min(a.mnz, b.mnz);
+        u.mx[0] = ref_max(a.mxx, b.mxx); u.mx[1] = ref_max(a.mxy, b.mxy); u.mx[2] = ref_max(a.mxz, b.mxz);
+        store_node(nodes + i, u, 2u * i + 1u, 2u, 0);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// warp-level binning and plane choice
+
+// Merge one element per lane (bin = nb for inactive lanes) into warp bins.
+__device__ __forceinline__ void warp_bin_add(uint32_t* __restrict__ wb, int bin, int nb, const float* mn, const float* mx,
+                                             const float* c)
+{
+    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, (uint32_t)bin);
+    const int leader = __ffs(peers) - 1;
+    const int lane = threadIdx.x & 31;
+    uint32_t e[12];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        e[a] = float_to_ordered(-mn[a]);
+        e[3 + a] = float_to_ordered(mx[a]);
+        e[6 + a] = float_to_ordered(-c[a]);
+        e[9 + a] = float_to_ordered(c[a]);
+    }
+#pragma unroll
+    for (int k = 0; k < 12; ++k) e[k] = __reduce_max_sync(peers, e[k]);
+    if (lane == leader && bin < nb) {
+        uint32_t* b = wb + bin * kBinWords;
+#pragma unroll
+        for (int k = 0; k < 12; ++k) b[k] = max(b[k], e[k]);
+        b[12] += __popc(peers);
+    }
+    __syncwarp();
+}
+
+struct PlaneResult {
+    int plane;  // -1 if none
+    uint32_t nl;
+    float lp[6], rp[6], lc[6], rc[6];  // min xyz, max xyz
+};
+
+// choose_plane (src/builder.cpp:488-523) over nb bins held as encoded words
+// (one bin per lane); every lane returns the result.
+__device__ PlaneResult warp_choose_plane(const uint32_t* __restrict__ bins, int nb)
+{
+    const int lane = threadIdx.x & 31;
+    float p[6], c[6];
+    uint32_t cnt = 0;
+    if (lane < nb) {
+        const uint32_t* b = bins + lane * kBinWords;
+        cnt = b[12];
+        if (cnt) {
+            for (int a = 0; a < 3; ++a) {
+                p[a] = dec_neg(b[a]); p[3 + a] = dec_pos(b[3 + a]);
+                c[a] = dec_neg(b[6 + a]); c[3 + a] = dec_pos(b[9 + a]);
+            }
+        }
+    }
+    if (lane >= nb || !cnt) {
+        for (int a = 0; a < 3; ++a) { p[a] = FLT_MAX; p[3 + a] = -FLT_MAX; c[a] = FLT_MAX; c[3 + a] = -FLT_MAX; }
+    }
+    // inclusive prefix (l2r) and suffix unions
+    float lp[6], lc[6], sp[6], sc[6];
+    uint32_t lcnt = cnt, scnt = cnt;
+    for (int k = 0; k < 6; ++k) { lp[k] = p[k]; lc[k] = c[k]; sp[k] = p[k]; sc[k] = c[k]; }
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        float yp[6], yc[6], zp[6], zc[6];
+        for (int k = 0; k < 6; ++k) {
+            yp[k] = __shfl_up_sync(0xFFFFFFFFu, lp[k], o);
+            yc[k] = __shfl_up_sync(0xFFFFFFFFu, lc[k], o);
+            zp[k] = __shfl_down_sync(0xFFFFFFFFu, sp[k], o);
+            zc[k] = __shfl_down_sync(0xFFFFFFFFu, sc[k], o);
+        }
+        const uint32_t ycnt = __shfl_up_sync(0xFFFFFFFFu, lcnt, o);
+        const uint32_t zcnt = __shfl_down_sync(0xFFFFFFFFu, scnt, o);
+        if (lane >= o) {
+            for (int k = 0; k < 3; ++k) {
+                lp[k] = fminf(lp[k], yp[k]); lp[3 + k] = fmaxf(lp[3 + k], yp[3 + k]);
+                lc[k] = fminf(lc[k], yc[k]); lc[3 + k] = fmaxf(lc[3 + k], yc[3 + k]);
+            }
+            lcnt += ycnt;
+        }
+        if (lane + o < 32) {
+            for (int k = 0; k < 3; ++k) {
+                sp[k] = fminf(sp[k], zp[k]); sp[3 + k] = fmaxf(sp[3 + k], zp[3 + k]);
+                sc[k] = fminf(sc[k], zc[k]); sc[3 + k] = fmaxf(sc[3 + k], zc[3 + k]);
+            }
+            scnt += zcnt;
+        }
+    }
+    // right side of plane i = suffix(i + 1)
+    float rp[6], rc[6];
+    for (int k = 0; k < 6; ++k) {
+        rp[k] = __shfl_down_sync(0xFFFFFFFFu, sp[k], 1);
+        rc[k] = __shfl_down_sync(0xFFFFFFFFu, sc[k], 1);
+    }
+    const uint32_t rcnt = __shfl_down_sync(0xFFFFFFFFu, scnt, 1);
+    bool valid = false;
+    float score = 0.0f;
+    if (lane <= nb - 2) {
+        const float sl = box_sa(lp, lp + 3) * (float)lcnt;
+        const float sr = box_sa(rp, rp + 3) * (float)rcnt;
+        score = sl + sr;
+        valid = score < FLT_MAX;
+    }
+    // best: smallest score, ties to the highest plane
+    int best = valid ? lane : -1;
+    float bs = score;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const int ob = __shfl_xor_sync(0xFFFFFFFFu, best, o);
+        const float os = __shfl_xor_sync(0xFFFFFFFFu, bs, o);
+        if (ob >= 0 && (best < 0 || os < bs || (os == bs && ob > best))) { best = ob; bs = os; }
+    }
+    PlaneResult r;
+    r.plane = best;
+    r.nl = 0;
+    if (best >= 0) {
+        r.nl = __shfl_sync(0xFFFFFFFFu, lcnt, best);
+        for (int k = 0; k < 6; ++k) {
+            r.lp[k] = __shfl_sync(0xFFFFFFFFu, lp[k], best);
+            r.lc[k] = __shfl_sync(0xFFFFFFFFu, lc[k], best);
+            r.rp[k] = __shfl_sync(0xFFFFFFFFu, rp[k], best);
+            r.rc[k] = __shfl_sync(0xFFFFFFFFu, rc[k], best);
+        }
+    }
+    return r;
+}
+
+__device__ __forceinline__ Task child_task(uint32_t begin, uint32_t count, uint32_t slot, uint32_t buf, const float* p,
+                                           const float* c)
+{
+    Task t;
+    t.begin = begin; t.count = count; t.slot = slot; t.flags = buf;
+    for (int k = 0; k < 3; ++k) { t.pmn[k] = p[k]; t.pmx[k] = p[3 + k]; t.cmn[k] = c[k]; t.cmx[k] = c[3 + k]; }
+    return t;
+}
+
+// ---------------------------------------------------------------------------
+// large phase
+
+__global__ void k_large_prep(const Task* __restrict__ tasks, uint32_t nt, int nb, Split* __restrict__ split,
+                             uint32_t* __restrict__ chunk_start)
+{
+    // single block: chunk counts and their exclusive scan
+    __shared__ uint32_t s_sum[1024];
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < nt; base += blockDim.x) {
+        const uint32_t t = base + threadIdx.x;
+        uint32_t ch = 0;
+        if (t < nt) {
+            const Task& tk = tasks[t];
+            ch = (tk.count + kChunk - 1) / kChunk;
+            Split s;
+            s.axis = choose_axis(tk.cmn, tk.cmx);
+            s.cmin = sel(tk.cmn, s.axis);
+            s.k1 = bin_k1(nb, sel(tk.cmx, s.axis) - s.cmin);
+            s.plane = -1;
+            s.nl = 0;
+            s.pad[0] = s.pad[1] = s.pad[2] = 0;
+            split[t] = s;
+        }
+        s_sum[threadIdx.x] = ch;
+        __syncthreads();
+        for (uint32_t o = 1; o < blockDim.x; o <<= 1) {
+            const uint32_t v = threadIdx.x >= o ? s_sum[threadIdx.x - o] : 0u;
+            __syncthreads();
+            s_sum[threadIdx.x] += v;
+            __syncthreads();
+        }
+        if (t < nt) chunk_start[t] = carry + s_sum[threadIdx.x] - ch;
+        carry += s_sum[blockDim.x - 1];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) chunk_start[nt] = carry;
+}
+
+__device__ __forceinline__ uint32_t task_of_chunk(const uint32_t* __restrict__ chunk_start, uint32_t nt, uint32_t c)
+{
+    uint32_t lo = 0, hi = nt;  // largest t with chunk_start[t] <= c
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(chunk_start + mid) <= c) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(256) k_large_bin(const Task* __restrict__ tasks, uint32_t nt,
+                                                   const Split* __restrict__ split, const uint32_t* __restrict__ chunk_start,
+                                                   const uint32_t* __restrict__ ids_a, const uint32_t* __restrict__ ids_b,
+                                                   const float4* __restrict__ tb, int nb, uint32_t* __restrict__ bins_g)
+{
+    __shared__ uint32_t s_wb[8][kMaxBins * kBinWords];
+    const uint32_t c = blockIdx.x;
+    if (c >= __ldg(chunk_start + nt)) return;
+    const uint32_t t = task_of_chunk(chunk_start, nt, c);
+    const Task tk = tasks[t];
+    const Split sp = split[t];
+    const uint32_t off = (c - chunk_start[t]) * kChunk;
+    const uint32_t len = min(kChunk, tk.count - off);
+    const uint32_t* ids = (tk.flags & 1u) ? ids_b : ids_a;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t* wb = s_wb[warp];
+    for (int j = lane; j < kMaxBins * kBinWords; j += 32) wb[j] = 0;
+    __syncwarp();
+    for (uint32_t base = warp * 32; base < len; base += 256) {
+        const uint32_t j = base + lane;
+        float mn[3], mx[3], cc[3];
+        int bin = nb;
+        if (j < len) {
+            load_box(tb, ids[tk.begin + off + j], mn, mx);
+            for (int a = 0; a < 3; ++a) cc[a] = (mn[a] + mx[a]) * 0.5f;
+            bin = bin_of(sp.k1, sel(cc, sp.axis), sp.cmin, nb);
+        } else {
+            for (int a = 0; a < 3; ++a) { mn[a] = mx[a] = cc[a] = 0.0f; }
+        }
+        warp_bin_add(wb, bin, nb, mn, mx, cc);
+    }
+    __syncthreads();
+    uint32_t* g = bins_g + (size_t)t * kMaxBins * kBinWords;
+    for (int j = threadIdx.x; j < nb * kBinWords; j += blockDim.x) {
+        uint32_t v = s_wb[0][j];
+        const bool is_count = (j % kBinWords) == 12;
+        for (int w = 1; w < 8; ++w) v = is_count ? v + s_wb[w][j] : max(v, s_wb[w][j]);
+        if (v) {
+            if (is_count) atomicAdd(g + j, v); else atomicMax(g + j, v);
+        }
+    }
+}
+
+__global__ void k_large_split(const Task* __restrict__ tasks, uint32_t nt, Split* __restrict__ split,
+                              const uint32_t* __restrict__ bins_g, int nb, uint32_t base, uint32_t leaf_size,
+                              Node* __restrict__ nodes, Task* large_next, Task* small, LeafRange* leaves, Ctl* ctl)
+{
+    const uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (t >= nt) return;
+    const Task tk = tasks[t];
+    const PlaneResult r = warp_choose_plane(bins_g + (size_t)t * kMaxBins * kBinWords, nb);
+    if (lane != 0) return;
+    if (r.plane < 0 || r.nl == 0 || r.nl == tk.count) {
+        // no plane scored below FLT_MAX: the node becomes a leaf
+        Task leaf = tk;
+        leaf.count = tk.count;
+        const uint32_t k = atomicAdd(&ctl->n_leaf, 1u);
+        LeafRange lr;
+        lr.begin = tk.begin; lr.count = tk.count; lr.slot = tk.slot; lr.flags = tk.flags;
+        for (int a = 0; a < 3; ++a) { lr.pmn[a] = tk.pmn[a]; lr.pmx[a] = tk.pmx[a]; }
+        lr.pad[0] = lr.pad[1] = 0;
+        leaves[k] = lr;
+        (void)leaf;
+        return;
+    }
+    Split s = split[t];
+    s.plane = r.plane;
+    s.nl = r.nl;
+    split[t] = s;
+    const uint32_t q = tk.begin + r.nl;
+    Box pb;
+    for (int a = 0; a < 3; ++a) { pb.mn[a] = tk.pmn[a]; pb.mx[a] = tk.pmx[a]; }
+    store_node(nodes + tk.slot, pb, base + 2u * q, 2u, 0);
+    const uint32_t buf = (tk.flags & 1u) ^ 1u;
+    classify(child_task(tk.begin, r.nl, base + 2u * q, buf, r.lp, r.lc), leaf_size, large_next, small, leaves, ctl);
+    classify(child_task(q, tk.count - r.nl, base + 2u * q + 1u, buf, r.rp, r.rc), leaf_size, large_next, small, leaves,
+             ctl);
+}
+
+__global__ void __launch_bounds__(256) k_large_count(const Task* __restrict__ tasks, uint32_t nt,
+                                                     const Split* __restrict__ split,
+                                                     const uint32_t* __restrict__ chunk_start,
+                                                     const uint32_t* __restrict__ ids_a, const uint32_t* __restrict__ ids_b,
+                                                     const float4* __restrict__ tb, int nb,
+                                                     uint32_t* __restrict__ chunk_left)
+{
+    const uint32_t c = blockIdx.x;
+    if (c >= __ldg(chunk_start + nt)) return;
+    const uint32_t t = task_of_chunk(chunk_start, nt, c);
+    const Split sp = split[t];
+    if (sp.plane < 0) return;
+    const Task tk = tasks[t];
+    const uint32_t off = (c - chunk_start[t]) * kChunk;
+    const uint32_t len = min(kChunk, tk.count - off);
+    const uint32_t* ids = (tk.flags & 1u) ? ids_b : ids_a;
+    uint32_t cnt = 0;
+    for (uint32_t j = threadIdx.x; j < len; j += blockDim.x) {
+        float mn[3], mx[3];
+        load_box(tb, ids[tk.begin + off + j], mn, mx);
+        const float cc = (sel(mn, sp.axis) + sel(mx, sp.axis)) * 0.5f;
+        cnt += bin_of(sp.k1, cc, sp.cmin, nb) <= sp.plane;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xFFFFFFFFu, cnt, o);
+    __shared__ uint32_t s[8];
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t total = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) total += s[w];
+        chunk_left[c] = total;
+    }
+}
+
+// exclusive scan of the left counts over each task's chunks (one warp per task)
+__global__ void k_large_scan(const Split* __restrict__ split, uint32_t nt, const uint32_t* __restrict__ chunk_start,
+                             uint32_t* __restrict__ chunk_left)
+{
+    const uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (t >= nt || split[t].plane < 0) return;
+    uint32_t carry = 0;
+    for (uint32_t c0 = chunk_start[t]; c0 < chunk_start[t + 1]; c0 += 32) {
+        const uint32_t c = c0 + lane;
+        const uint32_t v = c < chunk_start[t + 1] ? chunk_left[c] : 0u;
+        uint32_t x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (c < chunk_start[t + 1]) chunk_left[c] = carry + x - v;
+        carry += __shfl_sync(0xFFFFFFFFu, x, 31);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_large_scatter(const Task* __restrict__ tasks, uint32_t nt,
+                                                       const Split* __restrict__ split,
+                                                       const uint32_t* __restrict__ chunk_start,
+                                                       uint32_t* __restrict__ ids_a, uint32_t* __restrict__ ids_b,
+                                                       const float4* __restrict__ tb, int nb,
+                                                       const uint32_t* __restrict__ chunk_left)
+{
+    constexpr int kPer = kChunk / 256;  // 8 consecutive elements per thread
+    const uint32_t c = blockIdx.x;
+    if (c >= __ldg(chunk_start + nt)) return;
+    const uint32_t t = task_of_chunk(chunk_start, nt, c);
+    const Split sp = split[t];
+    if (sp.plane < 0) return;
+    const Task tk = tasks[t];
+    const uint32_t off = (c - chunk_start[t]) * kChunk;
+    const uint32_t len = min(kChunk, tk.count - off);
+    const uint32_t* in = (tk.flags & 1u) ? ids_b : ids_a;
+    uint32_t* out = (tk.flags & 1u) ? ids_a : ids_b;
+    uint32_t idv[kPer];
+    bool left[kPer];
+    uint32_t cnt = 0;
+#pragma unroll
+    for (int k = 0; k < kPer; ++k) {
+        const uint32_t j = threadIdx.x * kPer + k;
+        left[k] = false;
+        idv[k] = 0;
+        if (j < len) {
+            idv[k] = in[tk.begin + off + j];
+            float mn[3], mx[3];
+            load_box(tb, idv[k], mn, mx);
+            const float cc = (sel(mn, sp.axis) + sel(mx, sp.axis)) * 0.5f;
+            left[k] = bin_of(sp.k1, cc, sp.cmin, nb) <= sp.plane;
+            cnt += left[k];
+        }
+    }
+    // block exclusive scan of per-thread left counts
+    __shared__ uint32_t s_w[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_w[warp] = x;
+    __syncthreads();
+    uint32_t wsum = 0;
+    for (int w = 0; w < warp; ++w) wsum += s_w[w];
+    uint32_t lrank = wsum + x - cnt;                    // left elements before this thread in the chunk
+    const uint32_t left_before = chunk_left[c];          // left elements before this chunk in the task
+    const uint32_t lbase = tk.begin + left_before;
+    const uint32_t rbase = tk.begin + sp.nl + (off - left_before);
+#pragma unroll
+    for (int k = 0; k < kPer; ++k) {
+        const uint32_t j = threadIdx.x * kPer + k;
+        if (j < len) {
+            if (left[k]) { out[lbase + lrank] = idv[k]; lrank++; }
+            else out[rbase + (j - lrank)] = idv[k];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// leaves
+
+// Leaf-region records for [b, b+c) and the range's own record at its slot.
+__device__ void warp_emit_leaf(const uint32_t* __restrict__ ids, uint32_t b, uint32_t c, uint32_t slot, uint32_t flags,
+                               const float* pmn, const float* pmx, const float4* __restrict__ tb, Node* __restrict__ nodes,
+                               uint32_t leaf0, uint32_t* err)
+{
+    const int lane = threadIdx.x & 31;
+    for (uint32_t j = lane; j < c; j += 32) {
+        const uint32_t id = ids[b + j];
+        Box bb;
+        load_box(tb, id, bb.mn, bb.mx);
+        store_node(nodes + leaf0 + b + j, bb, id, 1u, kLeafFlag);
+        if (c == 1 && !(flags & 2u)) store_node(nodes + slot, bb, id, 1u, kLeafFlag);
+    }
+    if (lane == 0 && (c != 1 || (flags & 2u))) {
+        if (c > 65535u) { raise_error(err, SQ_DEVERR_NODE_COUNT); return; }
+        Box pb;
+        for (int a = 0; a < 3; ++a) { pb.mn[a] = pmn[a]; pb.mx[a] = pmx[a]; }
+        store_node(nodes + slot, pb, leaf0 + b, c, 0);
+    }
+}
+
+__global__ void k_emit_leaves(const LeafRange* __restrict__ leaves, const Ctl* __restrict__ ctl,
+                              const uint32_t* __restrict__ ids_a, const uint32_t* __restrict__ ids_b,
+                              const float4* __restrict__ tb, Node* __restrict__ nodes, uint32_t leaf0, uint32_t* err)
+{
+    const uint32_t nl = ctl->n_leaf;
+    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nl; w += (gridDim.x * blockDim.x) >> 5) {
+        const LeafRange lr = leaves[w];
+        const uint32_t* ids = (lr.flags & 1u) ? ids_b : ids_a;
+        warp_emit_leaf(ids, lr.begin, lr.count, lr.slot, lr.flags, lr.pmn, lr.pmx, tb, nodes, leaf0, err);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// small phase: one warp per subtree
+
+__global__ void __launch_bounds__(128) k_small(const Task* __restrict__ small, Ctl* ctl, uint32_t* __restrict__ ids_a,
+                                               uint32_t* __restrict__ ids_b, const float4* __restrict__ tb, int nb,
+                                               uint32_t leaf_size, uint32_t base, Node* __restrict__ nodes,
+                                               uint32_t leaf0, uint32_t* err)
+{
+    __shared__ uint32_t s_bins[4][kMaxBins * kBinWords];
+    __shared__ Task s_stack[4][kStackDepth];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t* wb = s_bins[warp];
+    Task* st = s_stack[warp];
+    const uint32_t total = ctl->n_small;
+    const uint32_t lt = (1u << lane) - 1u;
+    for (;;) {
+        uint32_t ti = 0;
+        if (lane == 0) ti = atomicAdd(&ctl->small_pop, 1u);
+        ti = __shfl_sync(0xFFFFFFFFu, ti, 0);
+        if (ti >= total) return;
+        Task cur = small[ti];
+        int sp = 0;
+        for (;;) {
+            // cur is splittable (count > leaf_size, centroid area > 0)
+            const uint32_t* in = (cur.flags & 1u) ? ids_b : ids_a;
+            uint32_t* out = (cur.flags & 1u) ? ids_a : ids_b;
+            const int axis = choose_axis(cur.cmn, cur.cmx);
+            const float cmin = sel(cur.cmn, axis);
+            const float k1 = bin_k1(nb, sel(cur.cmx, axis) - cmin);
+            for (int j = lane; j < kMaxBins * kBinWords; j += 32) wb[j] = 0;
+            __syncwarp();
+            for (uint32_t j0 = 0; j0 < cur.count; j0 += 32) {
+                const uint32_t j = j0 + lane;
+                float mn[3], mx[3], cc[3];
+                int bin = nb;
+                if (j < cur.count) {
+                    load_box(tb, in[cur.begin + j], mn, mx);
+                    for (int a = 0; a < 3; ++a) cc[a] = (mn[a] + mx[a]) * 0.5f;
+                    bin = bin_of(k1, sel(cc, axis), cmin, nb);
+                } else {
+                    for (int a = 0; a < 3; ++a) { mn[a] = mx[a] = cc[a] = 0.0f; }
+                }
+                warp_bin_add(wb, bin, nb, mn, mx, cc);
+            }
+            const PlaneResult r = warp_choose_plane(wb, nb);
+            __syncwarp();
+            bool have_next = false;
+            if (r.plane < 0 || r.nl == 0 || r.nl == cur.count) {
+                // no plane scored below FLT_MAX: leaf
+                warp_emit_leaf(in, cur.begin, cur.count, cur.slot, cur.flags, cur.pmn, cur.pmx, tb, nodes, leaf0, err);
+            } else {
+                const uint32_t q = cur.begin + r.nl;
+                if (lane == 0) {
+                    Box pb;
+                    for (int a = 0; a < 3; ++a) { pb.mn[a] = cur.pmn[a]; pb.mx[a] = cur.pmx[a]; }
+                    store_node(nodes + cur.slot, pb, base + 2u * q, 2u, 0);
+                }
+                // stable partition into the other buffer
+                uint32_t lc = 0, rc = 0;
+                for (uint32_t j0 = 0; j0 < cur.count; j0 += 32) {
+                    const uint32_t j = j0 + lane;
+                    const bool valid = j < cur.count;
+                    uint32_t id = 0;
+                    bool left = false;
+                    if (valid) {
+                        id = in[cur.begin + j];
+                        float mn[3], mx[3];
+                        load_box(tb, id, mn, mx);
+                        const float cc = (sel(mn, axis) + sel(mx, axis)) * 0.5f;
+                        left = bin_of(k1, cc, cmin, nb) <= r.plane;
+                    }
+                    const uint32_t lb = __ballot_sync(0xFFFFFFFFu, valid && left);
+                    const uint32_t rb = __ballot_sync(0xFFFFFFFFu, valid && !left);
+                    if (valid) {
+                        if (left) out[cur.begin + lc + __popc(lb & lt)] = id;
+                        else out[q + rc + __popc(rb & lt)] = id;
+                    }
+                    lc += __popc(lb);
+                    rc += __popc(rb);
+                }
+                __syncwarp();
+                const uint32_t buf = (cur.flags & 1u) ^ 1u;
+                Task ch[2] = {child_task(cur.begin, r.nl, base + 2u * q, buf, r.lp, r.lc),
+                              child_task(q, cur.count - r.nl, base + 2u * q + 1u, buf, r.rp, r.rc)};
+                bool split_ch[2];
+                for (int k = 0; k < 2; ++k) {
+                    split_ch[k] = !(ch[k].count <= leaf_size || !(box_sa(ch[k].cmn, ch[k].cmx) > 0.0f));
+                    if (!split_ch[k])
+                        warp_emit_leaf(out, ch[k].begin, ch[k].count, ch[k].slot, ch[k].flags, ch[k].pmn, ch[k].pmx, tb,
+                                       nodes, leaf0, err);
+                }
+                if (split_ch[0] && split_ch[1]) {
+                    const int small_k = ch[0].count <= ch[1].count ? 0 : 1;
+                    if (sp >= kStackDepth) {
+                        raise_error(err, SQ_DEVERR_SAH_QUEUE);
+                        return;
+                    }
+                    if (lane == 0) st[sp] = ch[1 - small_k];
+                    sp++;
+                    __syncwarp();
+                    cur = ch[small_k];
+                    have_next = true;
+                } else if (split_ch[0] || split_ch[1]) {
+                    cur = split_ch[0] ? ch[0] : ch[1];
+                    have_next = true;
+                }
+            }
+            if (!have_next) {
+                if (sp == 0) break;
+                --sp;
+                __syncwarp();
+                cur = st[sp];
+                __syncwarp();
+            }
+        }
+    }
+}
+
+int g_sms = 0;
+int sms()
+{
+    if (!g_sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sms <= 0) g_sms = kNumSMs;
+    }
+    return g_sms;
+}
+
+}  // namespace
+
+namespace sqk {
+
+size_t sah_workspace_bytes(uint32_t n)
+{
+    const size_t tasks = n / kSmall + 2;
+    size_t b = 0;
+    b += sizeof(float4) * 2ull * n;            // triangle boxes
+    b += sizeof(uint32_t) * 2ull * n;          // ids A/B
+    b += sizeof(Task) * 2 * tasks;             // large lists (cur/next)
+    b += sizeof(Task) * ((size_t)n / 2 + 2);   // small list
+    b += sizeof(LeafRange) * ((size_t)n + 66); // leaf list (+64 empty grid cells)
+    b += sizeof(Split) * tasks;
+    b += sizeof(uint32_t) * (tasks + 1);       // chunk starts
+    b += sizeof(uint32_t) * ((size_t)n / kChunk + tasks + 1);  // chunk left counts
+    b += sizeof(uint32_t) * (size_t)kMaxBins * kBinWords * tasks;  // bins
+    b += sizeof(uint32_t) * 64 * kBinWords + 64 * 4 + 64;         // grid cells, hist, root
+    b += sizeof(Ctl) + 4096;
+    return b;
+}
+
+// Builds a SAH (grid = 0) or grid (grid = 1) BVH.  ws: workspace of
+// sah_workspace_bytes(n) bytes; keys/vals/alt: 4n-word sort buffers (grid
+// only); sort_ws: zeroed onesweep state for one 6-bit pass (grid only).
+// host_ctl: pinned 32-byte buffer.  Returns 0 or a cudaError_t.
+int build_sah(const float* tris, uint32_t n, uint32_t nb, uint32_t leaf_size, int grid, uint32_t scene_box_cells,
+              sq::Node* nodes, float* scene_out, void* ws, uint32_t* sort_keys, uint32_t* sort_vals,
+              uint32_t* sort_alt_keys, uint32_t* sort_alt_vals, uint32_t* sort_lookback, uint32_t* sort_counters,
+              uint32_t* err, uint32_t* host_ctl, cudaStream_t s)
+{
+    const size_t tasks = n / kSmall + 2;
+    char* p = static_cast<char*>(ws);
+    auto take = [&](size_t bytes) { char* r = p; p += (bytes + 255) / 256 * 256; return r; };
+    float4* tb = reinterpret_cast<float4*>(take(sizeof(float4) * 2ull * n));
+    uint32_t* ids_a = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * (size_t)n));
+    uint32_t* ids_b = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * (size_t)n));
+    Task* lcur = reinterpret_cast<Task*>(take(sizeof(Task) * tasks));
+    Task* lnext = reinterpret_cast<Task*>(take(sizeof(Task) * tasks));
+    Task* small = reinterpret_cast<Task*>(take(sizeof(Task) * ((size_t)n / 2 + 2)));
+    LeafRange* leaves = reinterpret_cast<LeafRange*>(take(sizeof(LeafRange) * ((size_t)n + 66)));
+    Split* split = reinterpret_cast<Split*>(take(sizeof(Split) * tasks));
+    uint32_t* chunk_start = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * (tasks + 1)));
+    uint32_t* chunk_left = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * ((size_t)n / kChunk + tasks + 1)));
+    uint32_t* bins = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * (size_t)kMaxBins * kBinWords * tasks));
+    uint32_t* cells = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * 64 * kBinWords));
+    uint32_t* hist = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * 64));
+    uint32_t* root_ord = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * 16));
+    Ctl* ctl = reinterpret_cast<Ctl*>(take(sizeof(Ctl)));
+    const uint32_t base = grid ? 128u : 0u;
+    const uint32_t leaf0 = base + 2u * n + 2u;
+    cudaError_t e;
+#define SQ_TRY(x) do { if ((e = (x)) != cudaSuccess) return (int)e; } while (0)
+    SQ_TRY(cudaMemsetAsync(cells, 0, sizeof(uint32_t) * 64 * kBinWords, s));
+    SQ_TRY(cudaMemsetAsync(hist, 0, sizeof(uint32_t) * 64, s));
+    SQ_TRY(cudaMemsetAsync(root_ord, 0, sizeof(uint32_t) * 16, s));
+    SQ_TRY(cudaMemsetAsync(ctl, 0, sizeof(Ctl), s));
+    const uint32_t g = min((n + 255) / 256, (uint32_t)sms() * 8u);
+    k_sah_setup<<<g, 256, 0, s>>>(tris, n, tb, ids_a, root_ord);
+    Task* proc = lcur;  // large tasks of the current level
+    Task* outl = lnext; // their large children
+    if (!grid) {
+        k_root_task<<<1, 1, 0, s>>>(root_ord, n, leaf_size, proc, small, leaves, ctl, scene_out);
+    } else {
+        // bin into 64 cells keyed by Morton slot, then stable sort by slot
+        k_grid_bin<<<g, 256, 0, s>>>(tb, n, root_ord, sort_keys, cells, hist);
+        SQ_TRY(cudaMemcpyAsync(sort_vals, ids_a, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToDevice, s));
+        const int which = sort_passes(sort_keys, sort_vals, sort_alt_keys, sort_alt_vals, n, hist, sort_lookback,
+                                      sort_counters, 6, 1, err, s);
+        SQ_TRY(cudaMemcpyAsync(ids_a, which ? sort_alt_vals : sort_vals, sizeof(uint32_t) * (size_t)n,
+                               cudaMemcpyDeviceToDevice, s));
+        k_grid_tasks<<<1, 64, 0, s>>>(cells, root_ord, n, leaf_size, scene_box_cells, proc, small, leaves, ctl,
+                                      scene_out);
+    }
+    // large phase, one level per iteration (the host reads the task count)
+    for (;;) {
+        SQ_TRY(cudaMemcpyAsync(host_ctl, ctl, sizeof(uint32_t) * 4, cudaMemcpyDeviceToHost, s));
+        SQ_TRY(cudaStreamSynchronize(s));
+        const uint32_t nt = host_ctl[0];
+        if (nt == 0) break;
+        SQ_TRY(cudaMemsetAsync(&ctl->n_large_next, 0, sizeof(uint32_t), s));
+        SQ_TRY(cudaMemsetAsync(bins, 0, sizeof(uint32_t) * (size_t)kMaxBins * kBinWords * nt, s));
+        k_large_prep<<<1, 1024, 0, s>>>(proc, nt, (int)nb, split, chunk_start);
+        const uint32_t max_chunks = (uint32_t)((size_t)n / kChunk + nt + 1);
+        k_large_bin<<<max_chunks, 256, 0, s>>>(proc, nt, split, chunk_start, ids_a, ids_b, tb, (int)nb, bins);
+        k_large_split<<<(nt + 3) / 4, 128, 0, s>>>(proc, nt, split, bins, (int)nb, base, leaf_size, nodes, outl, small,
+                                                   leaves, ctl);
+        k_large_count<<<max_chunks, 256, 0, s>>>(proc, nt, split, chunk_start, ids_a, ids_b, tb, (int)nb, chunk_left);
+        k_large_scan<<<(nt + 3) / 4, 128, 0, s>>>(split, nt, chunk_start, chunk_left);
+        k_large_scatter<<<max_chunks, 256, 0, s>>>(proc, nt, split, chunk_start, ids_a, ids_b, tb, (int)nb, chunk_left);
+        std::swap(proc, outl);
+    }
+    // small phase and leaves
+    const uint32_t sg = (uint32_t)sms() * 8u;
+    k_small<<<sg, 128, 0, s>>>(small, ctl, ids_a, ids_b, tb, (int)nb, leaf_size, base, nodes, leaf0, err);
+    k_emit_leaves<<<sg, 256, 0, s>>>(leaves, ctl, ids_a, ids_b, tb, nodes, leaf0, err);
+    if (grid) k_grid_heap<<<1, 32, 0, s>>>(nodes);
+    return (int)cudaGetLastError();
+#undef SQ_TRY
+}
+
+}  // namespace sqk
