@@ -275,6 +275,22 @@ def main():
         e2e_total = float(t.item())
     e2e_value = world * rays_total * args.steps / (e2e_total / 1e3) / 1e6
 
+    # every builder once on the same scene (not part of the timed steps)
+    builders = {}
+    for name, kw in (("morton", {}), ("sah32_leaf4", dict(bins=32, leaf=4)), ("sah8_leaf8", dict(bins=8, leaf=8)),
+                     ("grid", dict(bins=8, leaf=8))):
+        kind = "morton" if name == "morton" else ("grid" if name == "grid" else "sah")
+        ctx.build(d_tris, kind, **kw).free()  # warm
+        flush.zero_()
+        bvh = ctx.build(d_tris, kind, **kw)
+        tb = ctx.timings()["build"]
+        flush.zero_()
+        ctx.trace(bvh, "closest", hits=d_hits, heatmap=d_heat, **cam)
+        tm = ctx.timings()
+        builders[name] = {"build_ms": tb, "trace_ms": tm["trace"], "box_tests_per_ray": tm["box_tests"] / rays_total,
+                          "tri_tests_per_ray": tm["tri_tests"] / rays_total}
+        bvh.free()
+
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -323,6 +339,7 @@ def main():
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": n * 36,
                 "d2h_bytes_per_step": rays_total * 15, "ms_per_step": e2e_total / args.steps},
+        "builders": builders,
         "gpu_launches": KERNELS_PER_STEP * args.steps,
         "clocks": clk,
     }

@@ -116,6 +116,10 @@ typedef enum sq_builder_kind {
 #define SQ_BUILD_GRID_SCENE_BOUNDS 0x1u /* grid: give cell nodes the scene box,
                                            as the plain reference grid builder
                                            does (src/builder.cpp:2173-2174)      */
+#define SQ_BUILD_WIDE8 0x2u             /* also collapse the binary tree into an
+                                           8-wide BVH with 8-bit quantised child
+                                           boxes (rounded outward); closest and
+                                           any-hit traces then use it          */
 
 typedef struct sq_build_params {
     uint32_t kind;            /* sq_builder_kind                                  */
@@ -133,6 +137,7 @@ typedef struct sq_bvh_info {
     uint32_t kind;            /* sq_builder_kind, or 0xFFFFFFFF for imported trees */
     float scene_min[3];
     float scene_max[3];
+    uint32_t wide_nodes;      /* 8-wide quantised nodes (0 if none)               */
 } sq_bvh_info;
 
 typedef enum sq_trace_mode {
@@ -142,6 +147,9 @@ typedef enum sq_trace_mode {
     SQ_TRACE_CLOSEST = 1, /* near-child order, t shrink, watertight test         */
     SQ_TRACE_ANYHIT = 2   /* as CLOSEST, stops at the first accepted hit         */
 } sq_trace_mode;
+/* OR into the mode: trace the binary (Node1) tree even when the BVH also has
+ * an 8-wide quantised tree.                                                  */
+#define SQ_TRACE_FORCE_BINARY 0x100u
 
 typedef enum sq_ray_kind {
     SQ_RAYS_REFERENCE_CAMERA = 0, /* trace()'s camera (src/tracer.cpp:202-216)   */
@@ -253,7 +261,8 @@ sq_status sq_trace(sq_ctx* ctx, const sq_bvh* bvh, const sq_ray_source* rays,
  * in milliseconds, measured with CUDA events on the context stream
  * (synchronises).  stage_ms[0] = build total, [1] = bounds+codes, [2] = sort,
  * [3] = topology+refit, [4] = trace; [5] and [6] are the last trace's total
- * ray-box and ray-triangle test counts (as floats).                          */
+ * ray-box and ray-triangle test counts (as floats); [7] = the 8-wide
+ * collapse (included in [0]).                                                */
 sq_status sq_last_timings(sq_ctx* ctx, float stage_ms[8]);
 
 #ifdef __cplusplus

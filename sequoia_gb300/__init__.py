@@ -51,7 +51,8 @@ class _BuildParams(C.Structure):
 
 class _BvhInfo(C.Structure):
     _fields_ = [("node_capacity", C.c_uint32), ("root", C.c_uint32), ("tri_count", C.c_uint32),
-                ("kind", C.c_uint32), ("scene_min", C.c_float * 3), ("scene_max", C.c_float * 3)]
+                ("kind", C.c_uint32), ("scene_min", C.c_float * 3), ("scene_max", C.c_float * 3),
+                ("wide_nodes", C.c_uint32)]
 
 
 class _RaySource(C.Structure):
@@ -212,8 +213,10 @@ class Context:
         self._check(load_library().sq_sync(self.handle, C.byref(bits)))
         return bits.value
 
-    def build(self, tris, builder="morton", bins=8, leaf=8, digit_bits=8, morton_bounds=0, flags=0):
+    def build(self, tris, builder="morton", bins=8, leaf=8, digit_bits=8, morton_bounds=0, flags=0, wide=False):
         n = _len(tris, 9)
+        if wide:
+            flags |= 2
         p = _BuildParams(BUILDERS[builder] if isinstance(builder, str) else int(builder), bins, leaf,
                          digit_bits, morton_bounds, flags)
         h = C.c_void_p()
@@ -264,21 +267,22 @@ class Context:
         return src, width * height
 
     def trace(self, bvh, mode="closest", rays=None, camera=None, width=0, height=0, origin=(0, 0, 0),
-              target=(0, 0, -1), up=(0, 1, 0), vfov=60.0, hits=True, heatmap=False):
+              target=(0, 0, -1), up=(0, 1, 0), vfov=60.0, hits=True, heatmap=False, binary=False):
         """Trace rays; returns (hits structured array or None, heatmap bytes or None).
-        `hits` / `heatmap` may also be device buffers to write into."""
+        `hits` / `heatmap` may also be device buffers to write into.  `binary`
+        forces the binary tree when the BVH also has an 8-wide one."""
         src, count = self._ray_source(rays, camera, width, height, origin, target, up, vfov)
         h_arr = np.empty(count, HIT) if hits is True else (hits if hits is not False else None)
         m_arr = np.empty(count * 3, np.uint8) if heatmap is True else (heatmap if heatmap is not False else None)
-        self._check(load_library().sq_trace(self.handle, bvh.handle, C.byref(src), MODES[mode],
-                                            _addr(h_arr), _addr(m_arr)))
+        m = MODES[mode] | (0x100 if binary else 0)
+        self._check(load_library().sq_trace(self.handle, bvh.handle, C.byref(src), m, _addr(h_arr), _addr(m_arr)))
         return h_arr, m_arr
 
     def timings(self):
         arr = (C.c_float * 8)()
         self._check(load_library().sq_last_timings(self.handle, C.byref(arr)))
         return {"build": arr[0], "codes": arr[1], "sort": arr[2], "topology": arr[3], "trace": arr[4],
-                "box_tests": arr[5], "tri_tests": arr[6]}
+                "box_tests": arr[5], "tri_tests": arr[6], "wide": arr[7]}
 
 
 # ---------------------------------------------------------------------------

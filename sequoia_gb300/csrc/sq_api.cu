@@ -40,6 +40,10 @@ struct sq_bvh {
     float scene[6] = {0, 0, 0, 0, 0, 0};
     uint32_t* codes = nullptr;  // sorted codes (Morton builds)
     uint32_t* perm = nullptr;   // sorted permutation
+    void* nodes8 = nullptr;     // 8-wide quantised nodes (SQ_BUILD_WIDE8)
+    void* tris8 = nullptr;      // their 48-byte triangles
+    uint32_t n8 = 0;
+    uint32_t leaf0 = 0;         // first leaf-region slot of the binary tree
 };
 
 namespace {
@@ -268,6 +272,24 @@ sq_status build_sah(sq_ctx* c, sq_bvh* b, const sq_build_params& p, int grid)
     return SQ_OK;
 }
 
+sq_status build_wide(sq_ctx* c, sq_bvh* b)
+{
+    const uint32_t n = b->n;
+    b->nodes8 = dalloc(c, sqk::bvh8_node_bytes(n));
+    b->tris8 = dalloc(c, sqk::bvh8_tri_bytes(n));
+    uint32_t* ws = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * (4ull * (n + 2) + 8)));
+    if (!b->nodes8 || !b->tris8 || !ws) {
+        dfree(c, ws);
+        return fail(c, SQ_ERR_OOM, "8-wide BVH allocation failed (n=%u)", n);
+    }
+    const uint32_t cnt = sqk::build_bvh8(b->nodes, b->root, b->leaf0, b->tris, n, b->nodes8, b->tris8, ws, c->host_ctl,
+                                         c->ctrl, c->stream);
+    dfree(c, ws);
+    if (cnt == 0xFFFFFFFFu) return fail(c, SQ_ERR_CUDA, "8-wide collapse: %s", cudaGetErrorString(cudaGetLastError()));
+    b->n8 = cnt;
+    return SQ_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -366,9 +388,15 @@ sq_status sq_build(sq_ctx* c, const sq_triangle* tris, uint32_t n, const sq_buil
         *out = b;
         return SQ_OK;
     }
+    b->leaf0 = (p.kind == SQ_BUILDER_GRID ? 128u : 0u) + 2u * n + 2u;
     if (p.kind == SQ_BUILDER_MORTON) st = build_morton(c, b, p);
     else st = build_sah(c, b, p, p.kind == SQ_BUILDER_GRID);
     if (st != SQ_OK) { sq_bvh_free(b); return st; }
+    if (p.flags & SQ_BUILD_WIDE8) {
+        st = build_wide(c, b);
+        if (st != SQ_OK) { sq_bvh_free(b); return st; }
+    }
+    SQ_CUDA(c, cudaEventRecord(c->ev[6], c->stream));
     *out = b;
     return SQ_OK;
 }
@@ -382,6 +410,8 @@ sq_status sq_bvh_free(sq_bvh* b)
     dfree(c, b->tris_own);
     dfree(c, b->codes);
     dfree(c, b->perm);
+    dfree(c, b->nodes8);
+    dfree(c, b->tris8);
     delete b;
     return SQ_OK;
 }
@@ -394,6 +424,7 @@ sq_status sq_bvh_get_info(const sq_bvh* b, sq_bvh_info* info)
     info->tri_count = b->n;
     info->kind = b->kind;
     for (int k = 0; k < 3; ++k) { info->scene_min[k] = b->scene[k]; info->scene_max[k] = b->scene[3 + k]; }
+    info->wide_nodes = b->n8;
     return SQ_OK;
 }
 
@@ -531,6 +562,8 @@ sq_status sq_trace(sq_ctx* c, const sq_bvh* b, const sq_ray_source* rays, uint32
                    uint8_t* heatmap_rgb)
 {
     if (!c || !b || !rays) return fail(c, SQ_ERR_INVALID, "sq_trace: null argument");
+    const bool force_binary = (mode & SQ_TRACE_FORCE_BINARY) != 0;
+    mode &= ~SQ_TRACE_FORCE_BINARY;
     if (mode > SQ_TRACE_ANYHIT) return fail(c, SQ_ERR_INVALID, "sq_trace: unknown mode %u", mode);
     Guard g(c->device);
     sqk::TraceArgs a;
@@ -611,7 +644,29 @@ sq_status sq_trace(sq_ctx* c, const sq_bvh* b, const sq_ray_source* rays, uint32
     cudaStream_t s = c->stream;
     SQ_CUDA(c, cudaMemsetAsync(c->ctrl + 1, 0, 7 * sizeof(uint32_t), s));
     SQ_CUDA(c, cudaEventRecord(c->ev[4], s));
-    if (count > 0) sqk::trace(a, s);
+    if (count > 0) {
+        if (b->nodes8 && mode != SQ_TRACE_REF && !force_binary) {
+            sqk::Trace8Args w;
+            memset(&w, 0, sizeof w);
+            w.nodes = b->nodes8;
+            w.tris8 = static_cast<const float4*>(b->tris8);
+            w.mode = mode;
+            w.ray_kind = a.ray_kind;
+            w.width = a.width;
+            w.height = a.height;
+            memcpy(w.cam, a.cam, sizeof w.cam);
+            w.rays = a.rays;
+            w.ray_count = a.ray_count;
+            w.hits = a.hits;
+            w.heat = a.heat;
+            w.work = a.work;
+            w.err = a.err;
+            w.stats = a.stats;
+            sqk::trace8(w, s);
+        } else {
+            sqk::trace(a, s);
+        }
+    }
     SQ_CUDA(c, cudaEventRecord(c->ev[5], s));
     SQ_CUDA(c, cudaGetLastError());
     c->trace_timed = true;
@@ -632,7 +687,8 @@ sq_status sq_last_timings(sq_ctx* c, float stage_ms[8])
     for (int k = 0; k < 8; ++k) stage_ms[k] = -1.0f;
     SQ_CUDA(c, cudaStreamSynchronize(c->stream));
     if (c->build_timed) {
-        cudaEventElapsedTime(&stage_ms[0], c->ev[0], c->ev[3]);
+        cudaEventElapsedTime(&stage_ms[0], c->ev[0], c->ev[6]);
+        cudaEventElapsedTime(&stage_ms[7], c->ev[3], c->ev[6]);
         cudaEventElapsedTime(&stage_ms[1], c->ev[0], c->ev[1]);
         cudaEventElapsedTime(&stage_ms[2], c->ev[1], c->ev[2]);
         cudaEventElapsedTime(&stage_ms[3], c->ev[2], c->ev[3]);

@@ -1,0 +1,584 @@
+// sq_bvh8.cu -- 8-wide BVH with 8-bit quantised child boxes (the precision
+// form), built by collapsing a binary range-tree BVH, and its traversal.
+//
+// Node (80 bytes, five 16-byte loads):
+//   origin xyz (float), exponents (3 bytes, biased by 127) + inner-child mask,
+//   first inner child node, first leaf triangle, 4-bit triangle count per
+//   child slot, and per child slot qlo xyz / qhi xyz (8 bits each).
+// Child box on axis a: [origin_a + qlo * 2^e_a, origin_a + qhi * 2^e_a], each
+// bound computed exactly as the traversal computes it (one rounded add of an
+// exact product) and moved outward until it contains the binary node's FP32
+// box, so a quantised box is never smaller than the FP32 box it replaces.
+// This is the compressed wide BVH idea of Ylitie, Karras and Laine
+// ("Efficient Incoherent Ray Traversal on GPUs Through Compressed Wide
+// BVHs", HPG 2017), laid out our own way.
+//
+// Collapse: each 8-wide node starts from a binary inner record's two children
+// and repeatedly opens the inner child of largest surface area until it has 8
+// children or no inner child is left.  Leaf-cluster records (and single leaf
+// records) become leaf children; their triangles are copied into a 48-byte
+// triangle array in leaf order, with the original triangle index in the
+// fourth float of the first vertex.
+//
+// Traversal (closest / any-hit): the node's eight child boxes are decoded and
+// tested with the same conservative slab test as the FP32 traversal; hits are
+// ordered by entry distance; inner children are pushed, leaf children are
+// pushed as triangle ranges; the nearest is taken next.  Because every
+// quantised box contains its FP32 box and the slab test is monotone in the
+// box, this traversal visits every triangle the FP32 2-wide traversal visits,
+// so both report the same closest hit (id and t, same watertight test).
+#include "sq_common.cuh"
+
+#include <algorithm>
+#include <utility>
+
+namespace {
+
+using namespace sq;
+
+constexpr float kRobust = 0x1.000008p+0f;  // same factor as the FP32 traversal
+constexpr int kStack8 = 64;
+
+struct __align__(16) Node8 {
+    float ox, oy, oz;
+    uint32_t exps_imask;  // e_x | e_y << 8 | e_z << 16 | imask << 24 (exponents biased by 127)
+    uint32_t child_base;
+    uint32_t tri_base;
+    uint32_t counts;      // 4 bits per child slot: triangles of a leaf child (0: inner or empty)
+    uint32_t valid;       // bit per child slot: slot used
+    uint8_t qlo[3][8];
+    uint8_t qhi[3][8];
+};
+static_assert(sizeof(Node8) == 80, "Node8 is 80 bytes");
+
+__device__ __forceinline__ float pow2f(int e) { return __uint_as_float((uint32_t)(e + 127) << 23); }
+
+__device__ __forceinline__ float node_sa(const Node& r)
+{
+    const float lx = r.mxx - r.mnx, ly = r.mxy - r.mny, lz = r.mxz - r.mnz;
+    return lx * ly + lx * lz + ly * lz;
+}
+
+struct Entry {
+    uint32_t rec;  // binary record index
+    float sa;
+    bool inner;    // a binary inner record (count 2, not a cluster)
+};
+
+// Exponent of the quantisation step so that origin + 255 * 2^e >= hi.
+__device__ int quant_exp(float lo, float hi)
+{
+    const float ext = hi - lo;
+    int e = -126;
+    if (ext > 0.0f) {
+        int ex;
+        frexpf(ext, &ex);  // ext in [2^(ex-1), 2^ex)
+        e = ex - 8;        // 255 * 2^e >= 2^(ex-1) * 255/128 ... adjusted below
+        if (e < -126) e = -126;
+        while (e > -126 && fmaf(255.0f, pow2f(e - 1), lo) >= hi) --e;
+        while (fmaf(255.0f, pow2f(e), lo) < hi && e < 127) ++e;
+    }
+    return e;
+}
+
+__device__ __forceinline__ uint8_t quant_lo(float v, float origin, int e)
+{
+    const float s = pow2f(e);
+    float q = floorf((v - origin) / s);
+    int qi = q < 0.0f ? 0 : (q > 255.0f ? 255 : (int)q);
+    while (qi > 0 && fmaf((float)qi, s, origin) > v) --qi;
+    return (uint8_t)qi;
+}
+
+__device__ __forceinline__ uint8_t quant_hi(float v, float origin, int e)
+{
+    const float s = pow2f(e);
+    float q = ceilf((v - origin) / s);
+    int qi = q < 0.0f ? 0 : (q > 255.0f ? 255 : (int)q);
+    while (qi < 255 && fmaf((float)qi, s, origin) < v) ++qi;
+    return (uint8_t)qi;
+}
+
+// A binary inner record (as opposed to a leaf record or a leaf cluster): not
+// a leaf and its children are not in the leaf region.
+__device__ __forceinline__ bool is_inner(const Node& r, uint32_t leaf0)
+{
+    return !node_is_leaf(r.count_flags) && r.child < leaf0 && node_count(r.count_flags) > 0;
+}
+
+// One thread per 8-wide node: `tasks[i]` = binary record whose children the
+// node holds; `task_node[i]` = index of the node to write.
+__global__ void k_collapse(const Node* __restrict__ rec, uint32_t leaf0, const float* __restrict__ tris,
+                           const uint32_t* __restrict__ tasks, const uint32_t* __restrict__ task_node, uint32_t ntasks,
+                           Node8* __restrict__ nodes8, float4* __restrict__ tris8, uint32_t* __restrict__ counters,
+                           uint32_t* __restrict__ next_tasks, uint32_t* __restrict__ next_node, uint32_t* err)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ntasks) return;
+    const Node self = rec[tasks[i]];
+    Entry ch[8];
+    int nc = 0;
+    const uint32_t c0 = self.child, cn = node_count(self.count_flags);
+    if (cn > 8) { raise_error(err, SQ_DEVERR_NODE_COUNT); return; }
+    // the start set: a binary record's two children, or a cluster's leaves
+    for (uint32_t k = 0; k < cn; ++k) {
+        const Node r = rec[c0 + k];
+        ch[nc].rec = c0 + k;
+        ch[nc].sa = node_sa(r);
+        ch[nc].inner = is_inner(r, leaf0);
+        nc++;
+    }
+    // open the inner child of largest area until there are 8 children
+    for (;;) {
+        if (nc >= 8) break;
+        int best = -1;
+        for (int k = 0; k < nc; ++k)
+            if (ch[k].inner && (best < 0 || ch[k].sa > ch[best].sa)) best = k;
+        if (best < 0) break;
+        const Node r = rec[ch[best].rec];
+        Entry ea, eb;
+        ea.rec = r.child;
+        eb.rec = r.child + 1;
+        const Node xa = rec[ea.rec], xb = rec[eb.rec];
+        ea.sa = node_sa(xa); ea.inner = is_inner(xa, leaf0);
+        eb.sa = node_sa(xb); eb.inner = is_inner(xb, leaf0);
+        ch[best] = ea;
+        ch[nc++] = eb;
+    }
+    // allocate inner children and leaf triangles (children with an empty box,
+    // i.e. empty grid cells and subtrees of them, take no slot)
+    uint32_t n_inner = 0, n_tris = 0;
+    uint32_t cnt[8];
+    bool ok[8];
+    for (int k = 0; k < nc; ++k) {
+        const Node r = rec[ch[k].rec];
+        ok[k] = r.mnx <= r.mxx && r.mny <= r.mxy && r.mnz <= r.mxz;
+        cnt[k] = 0;
+        if (!ok[k]) continue;
+        if (ch[k].inner) n_inner++;
+        else {
+            cnt[k] = node_count(r.count_flags);
+            if (cnt[k] > 15u) { raise_error(err, SQ_DEVERR_NODE_COUNT); return; }
+            n_tris += cnt[k];
+        }
+    }
+    const uint32_t child_base = n_inner ? atomicAdd(counters + 0, n_inner) : 0u;
+    const uint32_t tri_base = n_tris ? atomicAdd(counters + 1, n_tris) : 0u;
+    const uint32_t task_base = n_inner ? atomicAdd(counters + 2, n_inner) : 0u;
+    // node box = union of the children (the record's own box)
+    const float lo[3] = {self.mnx, self.mny, self.mnz}, hi[3] = {self.mxx, self.mxy, self.mxz};
+    Node8 nd;
+    nd.ox = lo[0]; nd.oy = lo[1]; nd.oz = lo[2];
+    int e[3];
+    for (int a = 0; a < 3; ++a) e[a] = quant_exp(lo[a], hi[a]);
+    uint32_t imask = 0, counts = 0, valid = 0;
+    uint32_t inner_rank = 0, tri_off = 0;
+    for (int k = 0; k < 8; ++k) {
+        for (int a = 0; a < 3; ++a) { nd.qlo[a][k] = 255; nd.qhi[a][k] = 0; }
+    }
+    for (int k = 0; k < nc; ++k) {
+        const Node r = rec[ch[k].rec];
+        const float cl[3] = {r.mnx, r.mny, r.mnz}, chh[3] = {r.mxx, r.mxy, r.mxz};
+        if (!ok[k]) continue;  // empty box: slot unused
+        valid |= 1u << k;
+        for (int a = 0; a < 3; ++a) {
+            nd.qlo[a][k] = quant_lo(cl[a], lo[a], e[a]);
+            nd.qhi[a][k] = quant_hi(chh[a], lo[a], e[a]);
+        }
+        if (ch[k].inner) {
+            imask |= 1u << k;
+            next_tasks[task_base + inner_rank] = ch[k].rec;
+            next_node[task_base + inner_rank] = child_base + inner_rank;
+            inner_rank++;
+        } else {
+            counts |= cnt[k] << (4 * k);
+            // copy the leaf's triangles (a cluster's leaf records, or the leaf itself)
+            if (node_is_leaf(r.count_flags)) {
+                for (uint32_t j = 0; j < cnt[k]; ++j) {
+                    const uint32_t id = r.child + j;
+                    float t[9];
+                    load_tri(tris, id, t);
+                    float4* d = tris8 + 3ull * (tri_base + tri_off + j);
+                    d[0] = make_float4(t[0], t[1], t[2], __uint_as_float(id));
+                    d[1] = make_float4(t[3], t[4], t[5], 0.0f);
+                    d[2] = make_float4(t[6], t[7], t[8], 0.0f);
+                }
+            } else {
+                for (uint32_t j = 0; j < cnt[k]; ++j) {
+                    const Node lf = rec[r.child + j];
+                    const uint32_t id = lf.child;
+                    float t[9];
+                    load_tri(tris, id, t);
+                    float4* d = tris8 + 3ull * (tri_base + tri_off + j);
+                    d[0] = make_float4(t[0], t[1], t[2], __uint_as_float(id));
+                    d[1] = make_float4(t[3], t[4], t[5], 0.0f);
+                    d[2] = make_float4(t[6], t[7], t[8], 0.0f);
+                }
+            }
+            tri_off += cnt[k];
+        }
+    }
+    nd.exps_imask = (uint32_t)(e[0] + 127) | ((uint32_t)(e[1] + 127) << 8) | ((uint32_t)(e[2] + 127) << 16) | (imask << 24);
+    nd.child_base = child_base;
+    nd.tri_base = tri_base;
+    nd.counts = counts;
+    nd.valid = valid;
+    nodes8[task_node[i]] = nd;
+}
+
+// ---------------------------------------------------------------------------
+// traversal
+
+struct Ray8 {
+    float o[3], d[3], tmin, tmax;
+};
+
+struct Pre8 {
+    float o[3], inv[3], tmin, tmax;
+    int kx, ky, kz;
+    float sx, sy, sz;
+};
+
+__device__ __forceinline__ void prep8(const Ray8& r, Pre8& p)
+{
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { p.o[k] = r.o[k]; p.inv[k] = 1.0f / r.d[k]; }
+    p.tmin = r.tmin;
+    p.tmax = r.tmax;
+    const float ax = fabsf(r.d[0]), ay = fabsf(r.d[1]), az = fabsf(r.d[2]);
+    int kz = 0;
+    float m = ax;
+    if (ay > m) { kz = 1; m = ay; }
+    if (az > m) { kz = 2; }
+    int kx = kz + 1; if (kx == 3) kx = 0;
+    int ky = kx + 1; if (ky == 3) ky = 0;
+    const float dkz = r.d[kz];
+    if (dkz < 0.0f) { const int t = kx; kx = ky; ky = t; }
+    p.kx = kx; p.ky = ky; p.kz = kz;
+    p.sx = r.d[kx] / dkz;
+    p.sy = r.d[ky] / dkz;
+    p.sz = 1.0f / dkz;
+}
+
+__device__ __forceinline__ float sel3(const float* v, int k) { return k == 0 ? v[0] : (k == 1 ? v[1] : v[2]); }
+
+// watertight test (same operations as the FP32 traversal)
+__device__ __forceinline__ bool tri8(const float4* __restrict__ t8, uint32_t k, const Pre8& r, float tmax, float& tout,
+                                     uint32_t& id)
+{
+    const float4 a = __ldg(t8 + 3ull * k), b = __ldg(t8 + 3ull * k + 1), c = __ldg(t8 + 3ull * k + 2);
+    id = __float_as_uint(a.w);
+    float A[3] = {a.x - r.o[0], a.y - r.o[1], a.z - r.o[2]};
+    float B[3] = {b.x - r.o[0], b.y - r.o[1], b.z - r.o[2]};
+    float C[3] = {c.x - r.o[0], c.y - r.o[1], c.z - r.o[2]};
+    const float Akz = sel3(A, r.kz), Bkz = sel3(B, r.kz), Ckz = sel3(C, r.kz);
+    const float Ax = sel3(A, r.kx) - r.sx * Akz, Ay = sel3(A, r.ky) - r.sy * Akz;
+    const float Bx = sel3(B, r.kx) - r.sx * Bkz, By = sel3(B, r.ky) - r.sy * Bkz;
+    const float Cx = sel3(C, r.kx) - r.sx * Ckz, Cy = sel3(C, r.ky) - r.sy * Ckz;
+    float U = Cx * By - Cy * Bx;
+    float V = Ax * Cy - Ay * Cx;
+    float W = Bx * Ay - By * Ax;
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        const double u = (double)Cx * (double)By - (double)Cy * (double)Bx;
+        const double v = (double)Ax * (double)Cy - (double)Ay * (double)Cx;
+        const double w = (double)Bx * (double)Ay - (double)By * (double)Ax;
+        U = (float)u; V = (float)v; W = (float)w;
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    float det = U + V;
+    det = det + W;
+    if (det == 0.0f) return false;
+    const float Az = r.sz * Akz, Bz = r.sz * Bkz, Cz = r.sz * Ckz;
+    float T = U * Az + V * Bz;
+    T = T + W * Cz;
+    const float t = T / det;
+    if (!(t >= r.tmin) || !(t <= tmax)) return false;
+    tout = t;
+    return true;
+}
+
+struct Res8 {
+    uint32_t id;
+    float t;
+    uint32_t tests, tri_tests;
+    bool overflow;
+};
+
+template <bool ANY>
+__device__ Res8 trace8(const Node8* __restrict__ nodes, const float4* __restrict__ t8, const Ray8& ray)
+{
+    Pre8 rp;
+    prep8(ray, rp);
+    float best_t = rp.tmax;
+    uint32_t best = kNoHit;
+    uint32_t tests = 0, ttests = 0;
+    bool overflow = false;
+    uint32_t st_e[kStack8];
+    float st_t[kStack8];
+    int sp = 0;
+    uint32_t cur = 0;  // root node
+    bool have = true;
+    while (have) {
+        const float4* p = reinterpret_cast<const float4*>(nodes + cur);
+        const float4 w0 = __ldg(p), w1 = __ldg(p + 1), w2 = __ldg(p + 2), w3 = __ldg(p + 3), w4 = __ldg(p + 4);
+        const float org[3] = {w0.x, w0.y, w0.z};
+        const uint32_t ei = __float_as_uint(w0.w);
+        const float sc[3] = {pow2f((int)(ei & 0xFFu) - 127), pow2f((int)((ei >> 8) & 0xFFu) - 127),
+                             pow2f((int)((ei >> 16) & 0xFFu) - 127)};
+        const uint32_t imask = ei >> 24;
+        const uint32_t child_base = __float_as_uint(w1.x), tri_base = __float_as_uint(w1.y);
+        const uint32_t counts = __float_as_uint(w1.z), valid = __float_as_uint(w1.w);
+        const uint32_t q[12] = {__float_as_uint(w2.x), __float_as_uint(w2.y), __float_as_uint(w2.z), __float_as_uint(w2.w),
+                                __float_as_uint(w3.x), __float_as_uint(w3.y), __float_as_uint(w3.z), __float_as_uint(w3.w),
+                                __float_as_uint(w4.x), __float_as_uint(w4.y), __float_as_uint(w4.z), __float_as_uint(w4.w)};
+        // q words: qlo x (2 words: slots 0-3, 4-7), qlo y, qlo z, qhi x, qhi y, qhi z
+        uint32_t hn[8];
+        float ht[8];
+        int nh = 0;
+        uint32_t inner_rank = 0, tri_off = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const uint32_t cnt = (counts >> (4 * k)) & 0xFu;
+            const bool is_inner = (imask >> k) & 1u;
+            if ((valid >> k) & 1u) {
+                const int w = k >> 2, sh = (k & 3) * 8;
+                float lo[3], hi[3];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    const float ql = (float)((q[a * 2 + w] >> sh) & 0xFFu);
+                    const float qh = (float)((q[6 + a * 2 + w] >> sh) & 0xFFu);
+                    lo[a] = fmaf(ql, sc[a], org[a]);
+                    hi[a] = fmaf(qh, sc[a], org[a]);
+                }
+                tests++;
+                const float t0x = (lo[0] - rp.o[0]) * rp.inv[0];
+                const float t1x = (hi[0] - rp.o[0]) * rp.inv[0];
+                const float t0y = (lo[1] - rp.o[1]) * rp.inv[1];
+                const float t1y = (hi[1] - rp.o[1]) * rp.inv[1];
+                const float t0z = (lo[2] - rp.o[2]) * rp.inv[2];
+                const float t1z = (hi[2] - rp.o[2]) * rp.inv[2];
+                const float n = fmaxf(fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z)), rp.tmin);
+                float f = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+                f = f * kRobust;
+                if (n <= f && n <= best_t * kRobust) {
+                    const uint32_t ent = is_inner ? (child_base + inner_rank)
+                                                  : (0x80000000u | (cnt << 27) | (tri_base + tri_off));
+                    int b = nh - 1;
+                    while (b >= 0 && ht[b] > n) { hn[b + 1] = hn[b]; ht[b + 1] = ht[b]; --b; }
+                    hn[b + 1] = ent;
+                    ht[b + 1] = n;
+                    nh++;
+                }
+            }
+            inner_rank += is_inner;
+            tri_off += cnt;
+        }
+        if (sp + nh > kStack8) { overflow = true; break; }
+        for (int a = nh - 1; a >= 0; --a) { st_e[sp] = hn[a]; st_t[sp] = ht[a]; sp++; }
+        have = false;
+        bool done = false;
+        while (sp > 0) {
+            --sp;
+            const uint32_t e = st_e[sp];
+            if (st_t[sp] > best_t * kRobust) continue;
+            if (e & 0x80000000u) {
+                const uint32_t cnt = (e >> 27) & 0xFu, first = e & 0x07FFFFFFu;
+                for (uint32_t j = 0; j < cnt; ++j) {
+                    float t;
+                    uint32_t id;
+                    ttests++;
+                    if (tri8(t8, first + j, rp, best_t, t, id)) {
+                        if (t < best_t || (t == best_t && id < best)) { best_t = t; best = id; }
+                        if (ANY) { done = true; break; }
+                    }
+                }
+                if (done) break;
+                continue;
+            }
+            cur = e;
+            have = true;
+            break;
+        }
+        if (done) break;
+    }
+    Res8 r;
+    r.id = best;
+    r.t = best == kNoHit ? 0.0f : best_t;
+    r.tests = tests;
+    r.tri_tests = ttests;
+    r.overflow = overflow;
+    return r;
+}
+
+__device__ __forceinline__ uint32_t f2u(float x) { return (x >= 0.0f) ? (uint32_t)x : 0u; }
+
+template <int MODE>
+__global__ void __launch_bounds__(128) k_trace8(const sqk::Trace8Args a, uint32_t batches)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const bool camera = a.ray_kind != SQ_RAYS_EXPLICIT;
+    const uint32_t tiles_x = (a.width + 7u) >> 3;
+    for (;;) {
+        uint32_t b = 0;
+        if (lane == 0) b = atomicAdd(a.work, 1u);
+        b = __shfl_sync(0xFFFFFFFFu, b, 0);
+        if (b >= batches) return;
+        Ray8 r;
+        uint32_t rid = 0;
+        bool active;
+        if (camera) {
+            const uint32_t x = (b % tiles_x) * 8u + (lane & 7u);
+            const uint32_t y = (b / tiles_x) * 4u + (lane >> 3);
+            active = x < a.width && y < a.height;
+            rid = y * a.width + x;
+            if (active && a.ray_kind == SQ_RAYS_REFERENCE_CAMERA) {
+                // src/tracer.cpp:207-216 (same arithmetic as the FP32 traversal)
+                const float aspect = (float)a.width / (float)a.height;
+                float nx = ((float)x + 0.5f) / (float)a.width;
+                nx = nx * 2.0f;
+                nx = nx - 1.0f;
+                float ny = ((float)y + 0.5f) / (float)a.height;
+                ny = ny * 2.0f;
+                ny = ny - 1.0f;
+                nx = nx * aspect;
+                float l2 = nx * nx + ny * ny;
+                l2 = l2 + 1.0f * 1.0f;
+                const float len = sqrtf(l2);
+                r.o[0] = a.cam[0]; r.o[1] = a.cam[1]; r.o[2] = a.cam[2];
+                r.d[0] = nx / len; r.d[1] = ny / len; r.d[2] = 1.0f / len;
+                r.tmin = 0.0f;
+                r.tmax = 10000.0f;
+            } else if (active) {
+                // pinhole camera (same arithmetic as the FP32 traversal)
+                const float* bs = a.cam;
+                float px = ((float)x + 0.5f) / (float)a.width;
+                px = px * 2.0f;
+                px = px - 1.0f;
+                float py = ((float)y + 0.5f) / (float)a.height;
+                py = py * 2.0f;
+                py = py - 1.0f;
+                px = px * bs[12];
+                py = py * bs[13];
+                float d[3];
+                for (int k = 0; k < 3; ++k) {
+                    const float s = bs[3 + k] + px * bs[6 + k];
+                    d[k] = s + py * bs[9 + k];
+                }
+                float l2 = d[0] * d[0] + d[1] * d[1];
+                l2 = l2 + d[2] * d[2];
+                const float len = sqrtf(l2);
+                r.o[0] = bs[0]; r.o[1] = bs[1]; r.o[2] = bs[2];
+                r.d[0] = d[0] / len; r.d[1] = d[1] / len; r.d[2] = d[2] / len;
+                r.tmin = 0.0f;
+                r.tmax = FLT_MAX;
+            }
+        } else {
+            rid = b * 32u + lane;
+            active = rid < a.ray_count;
+            if (active) {
+                const float4* p = reinterpret_cast<const float4*>(a.rays) + 2ull * rid;
+                const float4 x0 = __ldg(p), x1 = __ldg(p + 1);
+                r.o[0] = x0.x; r.o[1] = x0.y; r.o[2] = x0.z; r.tmin = x0.w;
+                r.d[0] = x1.x; r.d[1] = x1.y; r.d[2] = x1.z; r.tmax = x1.w;
+            }
+        }
+        Res8 res;
+        res.tests = 0;
+        res.tri_tests = 0;
+        if (active) {
+            res = trace8<MODE == SQ_TRACE_ANYHIT>(static_cast<const Node8*>(a.nodes), a.tris8, r);
+            if (res.overflow) raise_error(a.err, SQ_DEVERR_STACK_OVERFLOW);
+        }
+        if (a.stats) {
+            unsigned long long bt = res.tests, tt = res.tri_tests;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                bt += __shfl_xor_sync(0xFFFFFFFFu, bt, o);
+                tt += __shfl_xor_sync(0xFFFFFFFFu, tt, o);
+            }
+            if (lane == 0) { atomicAdd(a.stats, bt); atomicAdd(a.stats + 1, tt); }
+        }
+        if (!active) continue;
+        if (a.hits) {
+            uint32_t* h = reinterpret_cast<uint32_t*>(a.hits) + 3ull * rid;
+            h[0] = res.id;
+            h[1] = __float_as_uint(res.t);
+            h[2] = res.tests;
+        }
+        if (a.heat) {
+            float x = (float)res.tests / 200.0f;
+            x = (x < 1.0f) ? x : 1.0f;
+            const uint8_t v = (uint8_t)f2u(x * 255.0f);
+            uint8_t* hp = a.heat + 3ull * rid;
+            hp[0] = v; hp[1] = v; hp[2] = v;
+        }
+    }
+}
+
+template <int MODE>
+void launch8(const sqk::Trace8Args& a, cudaStream_t s)
+{
+    uint32_t batches;
+    if (a.ray_kind == SQ_RAYS_EXPLICIT) batches = (a.ray_count + 31u) / 32u;
+    else batches = ((a.width + 7u) / 8u) * ((a.height + 3u) / 4u);
+    if (batches == 0) return;
+    static int per_sm = 0, sms = 0;
+    if (!per_sm) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace8<MODE>, 128, 0);
+        if (per_sm <= 0) per_sm = 1;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = kNumSMs;
+    }
+    uint32_t grid = (uint32_t)(per_sm * sms);
+    const uint32_t need = (batches + 3u) / 4u;
+    if (grid > need) grid = need;
+    k_trace8<MODE><<<grid, 128, 0, s>>>(a, batches);
+}
+
+}  // namespace
+
+namespace sqk {
+
+size_t bvh8_node_bytes(uint32_t n) { return sizeof(Node8) * ((size_t)n + 2); }
+size_t bvh8_tri_bytes(uint32_t n) { return sizeof(float4) * 3ull * ((size_t)n + 1); }
+
+// Collapse the binary tree rooted at record `root` (an inner record) into
+// nodes8 / tris8.  ws: 4 * (n + 2) words.  host_ctl: pinned 16 words.
+// Returns the 8-wide node count, or 0xFFFFFFFF on a CUDA error.
+uint32_t build_bvh8(const Node* rec, uint32_t root, uint32_t leaf0, const float* tris, uint32_t n, void* nodes8,
+                    void* tris8, uint32_t* ws, uint32_t* host_ctl, uint32_t* err, cudaStream_t s)
+{
+    uint32_t* counters = ws;                 // [0] nodes used, [1] tris used, [2] next task count
+    uint32_t* ta = ws + 8;                   // task lists (record index, node index), ping-pong
+    uint32_t* na = ta + (n + 2);
+    uint32_t* tb = na + (n + 2);
+    uint32_t* nb = tb + (n + 2);
+    // level 0: the root record -> node 0
+    const uint32_t init[4] = {1u, 0u, 0u, 0u};
+    if (cudaMemcpyAsync(counters, init, sizeof init, cudaMemcpyHostToDevice, s) != cudaSuccess) return 0xFFFFFFFFu;
+    const uint32_t first[2] = {root, 0u};
+    if (cudaMemcpyAsync(ta, &first[0], 4, cudaMemcpyHostToDevice, s) != cudaSuccess) return 0xFFFFFFFFu;
+    if (cudaMemcpyAsync(na, &first[1], 4, cudaMemcpyHostToDevice, s) != cudaSuccess) return 0xFFFFFFFFu;
+    uint32_t ntasks = 1;
+    while (ntasks) {
+        if (cudaMemsetAsync(counters + 2, 0, 4, s) != cudaSuccess) return 0xFFFFFFFFu;
+        k_collapse<<<(ntasks + 127) / 128, 128, 0, s>>>(rec, leaf0, tris, ta, na, ntasks, static_cast<Node8*>(nodes8),
+                                                        static_cast<float4*>(tris8), counters, tb, nb, err);
+        if (cudaMemcpyAsync(host_ctl, counters, 12, cudaMemcpyDeviceToHost, s) != cudaSuccess) return 0xFFFFFFFFu;
+        if (cudaStreamSynchronize(s) != cudaSuccess) return 0xFFFFFFFFu;
+        ntasks = host_ctl[2];
+        std::swap(ta, tb);
+        std::swap(na, nb);
+    }
+    return host_ctl[0];
+}
+
+void trace8(const Trace8Args& a, cudaStream_t s)
+{
+    if (a.mode == SQ_TRACE_ANYHIT) launch8<SQ_TRACE_ANYHIT>(a, s);
+    else launch8<SQ_TRACE_CLOSEST>(a, s);
+}
+
+}  // namespace sqk

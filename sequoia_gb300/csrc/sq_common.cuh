@@ -175,4 +175,24 @@ struct TraceArgs {
 };
 void trace(const TraceArgs& a, cudaStream_t s);
 
+// 8-wide quantised BVH (sq_bvh8.cu)
+struct Trace8Args {
+    const void* nodes;     // 80-byte wide nodes
+    const float4* tris8;   // 48-byte triangles in leaf order, id in v0.w
+    uint32_t mode, ray_kind, width, height;
+    float cam[14];
+    const float* rays;
+    uint32_t ray_count;
+    sq_hit* hits;
+    uint8_t* heat;
+    uint32_t* work;
+    uint32_t* err;
+    unsigned long long* stats;
+};
+size_t bvh8_node_bytes(uint32_t n);
+size_t bvh8_tri_bytes(uint32_t n);
+uint32_t build_bvh8(const sq::Node* rec, uint32_t root, uint32_t leaf0, const float* tris, uint32_t n, void* nodes8,
+                    void* tris8, uint32_t* ws, uint32_t* host_ctl, uint32_t* err, cudaStream_t s);
+void trace8(const Trace8Args& a, cudaStream_t s);
+
 }  // namespace sqk
