@@ -62,7 +62,8 @@ __device__ __forceinline__ float node_sa(const Node& r)
 struct Entry {
     uint32_t rec;  // binary record index
     float sa;
-    bool inner;    // a binary inner record (count 2, not a cluster)
+    uint32_t kind; // 0: binary inner record, 1: leaf cluster, 2: single-triangle leaf
+    uint32_t cnt;  // children of the record (2, cluster size, or 1)
 };
 
 // Exponent of the quantisation step so that origin + 255 * 2^e >= hi.
@@ -99,11 +100,19 @@ __device__ __forceinline__ uint8_t quant_hi(float v, float origin, int e)
     return (uint8_t)qi;
 }
 
-// A binary inner record (as opposed to a leaf record or a leaf cluster): not
-// a leaf and its children are not in the leaf region.
-__device__ __forceinline__ bool is_inner(const Node& r, uint32_t leaf0)
+// Kind of a record in the range-tree layout: a binary inner record (children
+// outside the leaf region), a leaf cluster (children in the leaf region) or a
+// single-triangle leaf record.
+__device__ __forceinline__ Entry make_entry(const Node* __restrict__ rec, uint32_t i, uint32_t leaf0)
 {
-    return !node_is_leaf(r.count_flags) && r.child < leaf0 && node_count(r.count_flags) > 0;
+    const Node r = rec[i];
+    Entry e;
+    e.rec = i;
+    e.sa = node_sa(r);
+    e.cnt = node_count(r.count_flags);
+    if (node_is_leaf(r.count_flags)) e.kind = 2;
+    else e.kind = (r.child < leaf0 && e.cnt > 0) ? 0u : 1u;
+    return e;
 }
 
 // One thread per 8-wide node: `tasks[i]` = binary record whose children the
@@ -121,30 +130,28 @@ __global__ void k_collapse(const Node* __restrict__ rec, uint32_t leaf0, const f
     const uint32_t c0 = self.child, cn = node_count(self.count_flags);
     if (cn > 8) { raise_error(err, SQ_DEVERR_NODE_COUNT); return; }
     // the start set: a binary record's two children, or a cluster's leaves
-    for (uint32_t k = 0; k < cn; ++k) {
-        const Node r = rec[c0 + k];
-        ch[nc].rec = c0 + k;
-        ch[nc].sa = node_sa(r);
-        ch[nc].inner = is_inner(r, leaf0);
-        nc++;
-    }
-    // open the inner child of largest area until there are 8 children
+    for (uint32_t k = 0; k < cn; ++k) ch[nc++] = make_entry(rec, c0 + k, leaf0);
+    // Open the child of largest area until no child can be opened within 8
+    // slots: a binary record opens into its two children, a leaf cluster into
+    // its single-triangle leaves (so each triangle keeps its own box).
     for (;;) {
-        if (nc >= 8) break;
         int best = -1;
-        for (int k = 0; k < nc; ++k)
-            if (ch[k].inner && (best < 0 || ch[k].sa > ch[best].sa)) best = k;
+        for (int k = 0; k < nc; ++k) {
+            const bool can = ch[k].kind == 0 ? (nc + 1 <= 8) : (ch[k].kind == 1 && nc + (int)ch[k].cnt - 1 <= 8);
+            if (can && (best < 0 || ch[k].sa > ch[best].sa)) best = k;
+        }
         if (best < 0) break;
         const Node r = rec[ch[best].rec];
-        Entry ea, eb;
-        ea.rec = r.child;
-        eb.rec = r.child + 1;
-        const Node xa = rec[ea.rec], xb = rec[eb.rec];
-        ea.sa = node_sa(xa); ea.inner = is_inner(xa, leaf0);
-        eb.sa = node_sa(xb); eb.inner = is_inner(xb, leaf0);
-        ch[best] = ea;
-        ch[nc++] = eb;
+        const uint32_t m = ch[best].kind == 0 ? 2u : ch[best].cnt;
+        if (m == 0) { ch[best] = ch[--nc]; continue; }
+        ch[best] = make_entry(rec, r.child, leaf0);
+        for (uint32_t j = 1; j < m; ++j) ch[nc++] = make_entry(rec, r.child + j, leaf0);
     }
+    // A cluster of 2..8 triangles that did not fit becomes a wide child node
+    // of its own (its triangles one per slot), so every triangle keeps its
+    // own box; larger clusters stay leaf children of up to 15 triangles.
+    for (int k = 0; k < nc; ++k)
+        if (ch[k].kind == 1 && ch[k].cnt >= 2 && ch[k].cnt <= 8) ch[k].kind = 0;
     // allocate inner children and leaf triangles (children with an empty box,
     // i.e. empty grid cells and subtrees of them, take no slot)
     uint32_t n_inner = 0, n_tris = 0;
@@ -155,7 +162,7 @@ __global__ void k_collapse(const Node* __restrict__ rec, uint32_t leaf0, const f
         ok[k] = r.mnx <= r.mxx && r.mny <= r.mxy && r.mnz <= r.mxz;
         cnt[k] = 0;
         if (!ok[k]) continue;
-        if (ch[k].inner) n_inner++;
+        if (ch[k].kind == 0) n_inner++;
         else {
             cnt[k] = node_count(r.count_flags);
             if (cnt[k] > 15u) { raise_error(err, SQ_DEVERR_NODE_COUNT); return; }
@@ -185,7 +192,7 @@ __global__ void k_collapse(const Node* __restrict__ rec, uint32_t leaf0, const f
             nd.qlo[a][k] = quant_lo(cl[a], lo[a], e[a]);
             nd.qhi[a][k] = quant_hi(chh[a], lo[a], e[a]);
         }
-        if (ch[k].inner) {
+        if (ch[k].kind == 0) {
             imask |= 1u << k;
             next_tasks[task_base + inner_rank] = ch[k].rec;
             next_node[task_base + inner_rank] = child_base + inner_rank;
