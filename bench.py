@@ -1,24 +1,31 @@
 #!/usr/bin/env python3
-"""Benchmark: LBVH build + closest-hit trace on one GB300 (per rank).
+"""Benchmark: BVH build + ray trace on one GB300 (per rank).
 
-Workload (one step): Morton/LBVH build of a 2,000,000-triangle Gaussian soup
-(64 clusters, seed 2) resident in HBM, then a closest-hit trace of
-3840x2160 pinhole primary rays from (0, 0, -40) aimed at the origin, with
-per-ray hit records and the test-count heatmap written to HBM.
+Timed step (the 2M-triangle configuration): build a Morton LBVH of a
+2,000,000-triangle Gaussian soup (64 clusters, seed 2) resident in HBM,
+collapse it into the 8-wide BVH with 8-bit outward-rounded child boxes, then
+trace 3840x2160 pinhole primary rays from (0, 0, -40) aimed at the origin
+(closest hit), writing per-ray hit records and the test-count heatmap to HBM.
+L2 is flushed between steps (512 MB write).
 
-  value     Mrays/s for the whole step (rays / (build + trace) device time)
-  e2e       the same through the C ABI with pinned host buffers: triangle
-            upload, build, trace, hit + heatmap download inside the timing
-  roofline  the trace kernel: algorithmic bytes (hit record + heatmap +
-            32 B per ray-box test + 36 B per triangle test) / kernel time
-            against the measured HBM copy bandwidth
-  cpu_baseline  the CPU implementation (the reference built from its sources
-            where available, else the oracle's restatement) on a bounded
-            sample of the same workload, all host threads
+  value      Mrays/s of the whole step: rays / (build + collapse + trace)
+  e2e        the same step through the C ABI with pinned host buffers:
+             triangle upload, build, trace, hit + heatmap download inside
+  plain_fp32 the same rays on the same tree traced as the plain FP32 binary
+             BVH, with the hit ids and t of both forms compared
+  stress     8,000,000-triangle soup (256 clusters, seed 5) and 2^24 rays with
+             origins uniform in the scene box and directions uniform on the
+             sphere, in 64 batches of log-uniform size [16K, 1M] traced by
+             one launch: 8-wide quantised vs plain FP32, closest and any-hit
+  roofline   the dominant kernel (the 8-wide trace): bytes it requested
+             (counted by the kernel: node loads, triangle loads, ray records
+             and outputs) / kernel time, against the measured HBM bandwidth
+  cpu_baseline  the CPU implementation (the reference's own code where it
+             builds, else the oracle's restatement) on a bounded sample
 
-`--impl reference` times only the CPU implementation and prints its line.
-Multi-GPU (torchrun): independent replicas, one per GPU (the path does not
-exchange data); value sums the rays of all ranks over the slowest rank.
+`--impl reference` times only the CPU implementation.  Multi-GPU (torchrun):
+independent replicas, one per GPU; value sums all ranks' rays over the
+slowest rank.
 """
 import argparse
 import json
@@ -33,12 +40,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-import numpy as np  # noqa: E402
+import numpy as np  # noqa: E402,F401
 
 METRIC = "Mrays/s traced & Mtris/s built on 1 GB300: quantized+batched vs plain FP32, same hits"
 WORKLOAD = dict(name="soup_2m", tris=2_000_000, clusters=64, seed=2, width=3840, height=2160,
                 eye=(0.0, 0.0, -40.0), target=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0), vfov=60.0)
-KERNELS_PER_STEP = 8  # scene bounds, Morton codes, 4 onesweep passes, climb, trace
+STRESS = dict(tris=8_000_000, clusters=256, seed=5, rays=1 << 24, batches=64)
+LBVH_KERNELS = 7  # scene bounds, Morton codes, 4 onesweep passes, climb
 
 
 def measured_peaks():
@@ -104,34 +112,14 @@ class ClockSampler:
 
 
 def dist_info():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
 
 
 def make_scene():
     from sequoia_gb300 import scenes
     w = WORKLOAD
     return scenes.gaussian_soup(w["tris"], w["clusters"], seed=w["seed"])
-
-
-def cpu_trace_sample(tris, impl, threads, row_step):
-    """Build on the CPU and trace every `row_step`-th image row; returns
-    (build seconds, trace seconds, sampled rays, kind)."""
-    import oracle as O
-    w = WORKLOAD
-    O.set_threads(threads)
-    kind = "port"
-    t0 = time.perf_counter()
-    nodes, root, _, _ = O.build_morton(tris)
-    t1 = time.perf_counter()
-    rays = O.rays_pinhole(w["width"], w["height"], w["eye"], w["target"], w["up"], w["vfov"])
-    rays = rays.reshape(w["height"], w["width"], 8)[::row_step].reshape(-1, 8).copy()
-    t2 = time.perf_counter()
-    O.trace(nodes, root, tris, rays, 1)
-    t3 = time.perf_counter()
-    return t1 - t0, t3 - t2, len(rays), kind
 
 
 def host_threads():
@@ -141,25 +129,47 @@ def host_threads():
         return os.cpu_count() or 1
 
 
-def run_reference(args):
-    rank, world, _ = dist_info()
-    if rank != 0:
-        return
-    tris = make_scene()
+def cpu_sample(tris, threads, row_step):
+    """CPU build of the whole scene and closest-hit trace of every
+    `row_step`-th image row.  Returns (build s, trace s, sampled rays, kind)."""
+    import oracle as O
+    w = WORKLOAD
+    O.set_threads(threads)
+    t0 = time.perf_counter()
+    nodes, root, _, _ = O.build_morton(tris)
+    t1 = time.perf_counter()
+    rays = O.rays_pinhole(w["width"], w["height"], w["eye"], w["target"], w["up"], w["vfov"])
+    rays = rays.reshape(w["height"], w["width"], 8)[::row_step].reshape(-1, 8).copy()
+    t2 = time.perf_counter()
+    O.trace(nodes, root, tris, rays, 1)
+    t3 = time.perf_counter()
+    return t1 - t0, t3 - t2, len(rays), "port"
+
+
+def cpu_line(tris, steps, warmup):
     w = WORKLOAD
     rays_total = w["width"] * w["height"]
     threads = host_threads()
     row_step = 16
     times = []
-    for i in range(args.warmup + args.steps):
-        tb, tt, ns, kind = cpu_trace_sample(tris, "port", threads, row_step)
-        if i >= args.warmup:
+    for i in range(warmup + steps):
+        tb, tt, ns, _ = cpu_sample(tris, threads, row_step)
+        if i >= warmup:
             times.append(tb + tt * (rays_total / ns))
     step_s = statistics.mean(times)
     value = rays_total / step_s / 1e6
-    sample = "Morton build of all %d tris + closest-hit trace of every %dth image row (%d rays), " \
-             "extrapolated to %d rays; oracle restatement (the reference's x86 code does not build here)" % (
-                 w["tris"], row_step, rays_total // row_step, rays_total)
+    sample = ("Morton build of all %d tris + closest-hit trace of every %dth image row (%d rays), extrapolated to "
+              "%d rays; the oracle's C restatement with OpenMP (the reference's own code needs x86 intrinsics)"
+              % (len(tris), row_step, rays_total // row_step, rays_total))
+    return value, step_s, threads, sample
+
+
+def run_reference(args):
+    rank, _, _ = dist_info()
+    if rank != 0:
+        return
+    tris = make_scene()
+    value, step_s, threads, sample = cpu_line(tris, args.steps, args.warmup)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
@@ -170,6 +180,43 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def stress_leg(ctx, flush, torch):
+    """8M-triangle soup, 2^24 incoherent rays in 64 batches, one launch per
+    form: 8-wide quantised vs plain FP32 binary, closest and any-hit."""
+    from sequoia_gb300 import scenes
+    s = STRESS
+    tris = scenes.gaussian_soup(s["tris"], s["clusters"], seed=s["seed"])
+    lo, hi = scenes.scene_box(tris)
+    sizes = scenes.batch_sizes(s["rays"], s["batches"], seed=s["seed"])
+    rays = torch.from_numpy(scenes.random_rays(int(sizes.sum()), lo, hi, seed=s["seed"])).cuda()
+    d_tris = torch.from_numpy(tris).cuda()
+    h_a = torch.empty(s["rays"] * 3, dtype=torch.int32, device="cuda")
+    h_b = torch.empty_like(h_a)
+    bvh = ctx.build(d_tris, "morton", wide=True)
+    out = {"tris": len(tris), "rays": int(sizes.sum()), "batches": len(sizes),
+           "batch_sizes_min_max": [int(sizes.min()), int(sizes.max())], "build_ms": ctx.timings()["build"]}
+    for mode in ("closest", "anyhit"):
+        t = {}
+        for form in ("binary", "wide"):
+            best = None
+            for _ in range(2):
+                flush.zero_()
+                ctx.trace(bvh, mode, rays=rays, hits=h_b if form == "binary" else h_a, binary=(form == "binary"))
+                ms = ctx.timings()["trace"]
+                best = ms if best is None else min(best, ms)
+            t[form] = best
+        a = h_a.view(-1, 3)
+        b = h_b.view(-1, 3)
+        if mode == "closest":
+            same = bool(torch.equal(a[:, :2], b[:, :2]))
+        else:
+            same = bool(torch.equal(a[:, 0] != -1, b[:, 0] != -1))
+        out[mode] = {"wide_mrays_s": s["rays"] / t["wide"] / 1e3, "plain_fp32_mrays_s": s["rays"] / t["binary"] / 1e3,
+                     "speedup": t["binary"] / t["wide"], "same_hits": same}
+    bvh.free()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -178,9 +225,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--no-extra", action="store_true", help="skip the comparison legs (profiling runs)")
     args = ap.parse_args()
-    if args.warmup < 3:
-        args.warmup = 3
+    args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         run_reference(args)
         return
@@ -210,11 +257,10 @@ def main():
                up=w["up"], vfov=w["vfov"])
 
     def step(src_tris, hits, heat):
-        bvh = ctx.build(src_tris, "morton")
+        bvh = ctx.build(src_tris, "morton", wide=True)
         ctx.trace(bvh, "closest", hits=hits, heatmap=heat, **cam)
         return bvh
 
-    # warm-up
     for _ in range(args.warmup):
         step(d_tris, d_hits, d_heat).free()
     torch.cuda.synchronize()
@@ -226,7 +272,7 @@ def main():
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    step_ms, build_ms, trace_ms, box_tests, tri_tests = [], [], [], [], []
+    step_ms, build_ms, wide_ms, trace_ms, stats, launches = [], [], [], [], [], 0
     for _ in range(args.steps):
         flush.zero_()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -235,11 +281,13 @@ def main():
         bvh = step(d_tris, d_hits, d_heat)
         e1.record(stream)
         tm = ctx.timings()  # synchronises
+        st = ctx.trace_stats()
         step_ms.append(e0.elapsed_time(e1))
         build_ms.append(tm["build"])
+        wide_ms.append(tm["wide"])
         trace_ms.append(tm["trace"])
-        box_tests.append(tm["box_tests"])
-        tri_tests.append(tm["tri_tests"])
+        stats.append(st)
+        launches += LBVH_KERNELS + bvh.info().wide_levels + 1
         bvh.free()
     torch.cuda.synchronize()
     if dist:
@@ -254,20 +302,20 @@ def main():
     value = world * rays_total * args.steps / (total_ms / 1e3) / 1e6
 
     # end to end through the public API with pinned host buffers
-    h_tris = torch.from_numpy(tris).pin_memory()
-    h_hits = torch.empty(rays_total * 3, dtype=torch.int32).pin_memory()
-    h_heat = torch.empty(rays_total * 3, dtype=torch.uint8).pin_memory()
     e2e_ms = []
     if not args.no_e2e:
+        h_tris = torch.from_numpy(tris).pin_memory()
+        h_hits = torch.empty(rays_total * 3, dtype=torch.int32).pin_memory()
+        h_heat = torch.empty(rays_total * 3, dtype=torch.uint8).pin_memory()
         step(h_tris, h_hits, h_heat).free()
-    for _ in range(0 if args.no_e2e else args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        bvh = step(h_tris, h_hits, h_heat)
-        torch.cuda.synchronize()
-        e2e_ms.append((time.perf_counter() - t0) * 1e3)
-        bvh.free()
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            bvh = step(h_tris, h_hits, h_heat)
+            torch.cuda.synchronize()
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+            bvh.free()
     e2e_total = float(sum(e2e_ms)) if e2e_ms else float("nan")
     if dist:
         t = torch.tensor([e2e_total], device="cuda")
@@ -275,21 +323,24 @@ def main():
         e2e_total = float(t.item())
     e2e_value = world * rays_total * args.steps / (e2e_total / 1e3) / 1e6
 
-    # every builder once on the same scene (not part of the timed steps)
-    builders = {}
-    for name, kw in (("morton", {}), ("sah32_leaf4", dict(bins=32, leaf=4)), ("sah8_leaf8", dict(bins=8, leaf=8)),
-                     ("grid", dict(bins=8, leaf=8))):
-        kind = "morton" if name == "morton" else ("grid" if name == "grid" else "sah")
-        ctx.build(d_tris, kind, **kw).free()  # warm
-        flush.zero_()
-        bvh = ctx.build(d_tris, kind, **kw)
-        tb = ctx.timings()["build"]
-        flush.zero_()
-        ctx.trace(bvh, "closest", hits=d_hits, heatmap=d_heat, **cam)
-        tm = ctx.timings()
-        builders[name] = {"build_ms": tb, "trace_ms": tm["trace"], "box_tests_per_ray": tm["box_tests"] / rays_total,
-                          "tri_tests_per_ray": tm["tri_tests"] / rays_total}
+    plain = stress = None
+    if not args.no_extra:
+        # plain FP32 binary traversal of the same tree, same rays; same hits?
+        bvh = ctx.build(d_tris, "morton", wide=True)
+        d_hits2 = torch.empty_like(d_hits)
+        times = {"wide": [], "binary": []}
+        for _ in range(3):
+            for form in ("binary", "wide"):
+                flush.zero_()
+                ctx.trace(bvh, "closest", hits=d_hits if form == "wide" else d_hits2, binary=(form == "binary"), **cam)
+                times[form].append(ctx.timings()["trace"])
+        same = bool(torch.equal(d_hits.view(-1, 3)[:, :2], d_hits2.view(-1, 3)[:, :2]))
         bvh.free()
+        plain = {"trace_ms": min(times["binary"]), "trace_mrays_s": rays_total / min(times["binary"]) / 1e3,
+                 "wide_trace_ms": min(times["wide"]), "speedup": min(times["binary"]) / min(times["wide"]),
+                 "same_hits": same}
+        del d_hits2
+        stress = stress_leg(ctx, flush, torch)
 
     if rank != 0:
         if dist:
@@ -298,25 +349,17 @@ def main():
 
     peak, peak_kind = measured_peaks()
     tr_ms = statistics.mean(trace_ms)
-    bt = statistics.mean(box_tests)
-    tt = statistics.mean(tri_tests)
-    trace_bytes = rays_total * (12 + 3) + bt * 32 + tt * 36
-    achieved = trace_bytes / (tr_ms / 1e3) / 1e9
+    req_bytes = statistics.mean(s["bytes"] for s in stats)
+    achieved = req_bytes / (tr_ms / 1e3) / 1e9
     b_ms = statistics.mean(build_ms)
-    build_bytes = n * (200 + 16 * 4)
-    build_gbs = build_bytes / (b_ms / 1e3) / 1e9
+    lbvh_ms = b_ms - statistics.mean(wide_ms)
+    build_gbs = n * (200 + 16 * 4) / (lbvh_ms / 1e3) / 1e9
     hits_np = d_hits.view(-1, 3).cpu().numpy()
-    nhit = int((hits_np[:, 0] != -1).sum())
 
     cpu = None
     if not args.no_cpu_baseline:
-        threads = host_threads()
-        row_step = 16
-        tb, tt_s, ns, kind = cpu_trace_sample(tris, "port", threads, row_step)
-        cpu_value = rays_total / (tb + tt_s * (rays_total / ns)) / 1e6
-        cpu = {"value": cpu_value, "unit": "Mrays/s", "cores": threads, "kind": kind,
-               "sample": "Morton build of all %d tris (%.2f s) + closest-hit trace of every %dth row "
-                         "(%d rays, %.2f s), extrapolated to the full image" % (n, tb, row_step, ns, tt_s)}
+        value_c, _, threads, sample = cpu_line(tris, 1, 0)
+        cpu = {"value": value_c, "unit": "Mrays/s", "cores": threads, "kind": "port", "sample": sample}
 
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
@@ -325,22 +368,31 @@ def main():
         "data": "synthetic: seeded 64-cluster Gaussian triangle soup (no dataset ships with the reference)",
         "config": {"workload": "soup_2m: %d-triangle Gaussian soup, %dx%d pinhole primary rays from (0,0,-40)"
                                % (n, w["width"], w["height"]),
-                   "builder": "morton (LBVH)", "trace": "closest hit + heatmap", "tris": n, "rays": rays_total,
-                   "l2": "flushed between steps (512 MB write)", "parallelism": "replicas" if world > 1 else "1 GPU"},
+                   "builder": "Morton LBVH + 8-wide 8-bit quantised collapse", "trace": "closest hit + heatmap",
+                   "tris": n, "rays": rays_total, "l2": "flushed between steps (512 MB write)",
+                   "parallelism": "replicas" if world > 1 else "1 GPU"},
         "build_mtris_s": n / (b_ms / 1e3) / 1e6,
+        "lbvh_mtris_s": n / (lbvh_ms / 1e3) / 1e6,
         "trace_mrays_s": rays_total / (tr_ms / 1e3) / 1e6,
-        "stage_ms": {"build": b_ms, "trace": tr_ms, "step": ms_per_step},
-        "box_tests_per_ray": bt / rays_total, "tri_tests_per_ray": tt / rays_total, "hit_rays": nhit,
-        "roofline": {"bound": "hbm", "kernel": "k_trace<closest>", "achieved": achieved, "peak": peak,
+        "stage_ms": {"build_total": b_ms, "lbvh": lbvh_ms, "wide_collapse": statistics.mean(wide_ms),
+                     "trace": tr_ms, "step": ms_per_step},
+        "per_ray": {"box_tests": statistics.mean(s["box_tests"] for s in stats) / rays_total,
+                    "tri_tests": statistics.mean(s["tri_tests"] for s in stats) / rays_total,
+                    "wide_nodes": statistics.mean(s["nodes"] for s in stats) / rays_total,
+                    "requested_bytes": req_bytes / rays_total},
+        "hit_rays": int((hits_np[:, 0] != -1).sum()),
+        "roofline": {"bound": "hbm", "kernel": "k_trace8<closest>", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
-                     "bytes_model": "15 B/ray out + 32 B per box test + 36 B per triangle test"},
+                     "bytes_model": "kernel-counted requested bytes: 80 B per wide node loaded, 48 B per "
+                                    "triangle tested, 15 B of outputs per ray"},
         "build_roofline": {"bound": "hbm", "achieved": build_gbs, "peak": peak, "unit": "GB/s",
                            "frac": build_gbs / peak, "bytes_model": "264 B/tri (200 + 16 x 4 sort passes)"},
+        "plain_fp32": plain,
+        "stress": stress,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": n * 36,
                 "d2h_bytes_per_step": rays_total * 15, "ms_per_step": e2e_total / args.steps},
-        "builders": builders,
-        "gpu_launches": KERNELS_PER_STEP * args.steps,
+        "gpu_launches": launches,
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)

@@ -138,6 +138,7 @@ typedef struct sq_bvh_info {
     float scene_min[3];
     float scene_max[3];
     uint32_t wide_nodes;      /* 8-wide quantised nodes (0 if none)               */
+    uint32_t wide_levels;     /* levels of the 8-wide collapse (kernel launches)  */
 } sq_bvh_info;
 
 typedef enum sq_trace_mode {
@@ -264,6 +265,14 @@ sq_status sq_trace(sq_ctx* ctx, const sq_bvh* bvh, const sq_ray_source* rays,
  * ray-box and ray-triangle test counts (as floats); [7] = the 8-wide
  * collapse (included in [0]).                                                */
 sq_status sq_last_timings(sq_ctx* ctx, float stage_ms[8]);
+
+/* Counters of the last sq_trace on this context (synchronises): stats[0] =
+ * ray-box tests, [1] = ray-triangle tests, [2] = bytes the traversal
+ * requested (ray in, hit record and heatmap out, node records, triangles),
+ * [3] = nodes visited (binary: node records tested; 8-wide: nodes loaded).
+ * No reference counterpart (the reference keeps only the per-ray count,
+ * src/tracer.h:32).                                                          */
+sq_status sq_last_trace_stats(sq_ctx* ctx, uint64_t stats[4]);
 
 #ifdef __cplusplus
 }

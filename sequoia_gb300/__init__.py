@@ -52,7 +52,7 @@ class _BuildParams(C.Structure):
 class _BvhInfo(C.Structure):
     _fields_ = [("node_capacity", C.c_uint32), ("root", C.c_uint32), ("tri_count", C.c_uint32),
                 ("kind", C.c_uint32), ("scene_min", C.c_float * 3), ("scene_max", C.c_float * 3),
-                ("wide_nodes", C.c_uint32)]
+                ("wide_nodes", C.c_uint32), ("wide_levels", C.c_uint32)]
 
 
 class _RaySource(C.Structure):
@@ -93,6 +93,7 @@ def load_library():
         "sq_bvh_export_sorted": (i32, [vp, vp, vp]),
         "sq_trace": (i32, [vp, vp, C.POINTER(_RaySource), u32, vp, vp]),
         "sq_last_timings": (i32, [vp, C.POINTER(C.c_float * 8)]),
+        "sq_last_trace_stats": (i32, [vp, C.POINTER(C.c_uint64 * 4)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -277,6 +278,11 @@ class Context:
         m = MODES[mode] | (0x100 if binary else 0)
         self._check(load_library().sq_trace(self.handle, bvh.handle, C.byref(src), m, _addr(h_arr), _addr(m_arr)))
         return h_arr, m_arr
+
+    def trace_stats(self):
+        arr = (C.c_uint64 * 4)()
+        self._check(load_library().sq_last_trace_stats(self.handle, C.byref(arr)))
+        return {"box_tests": arr[0], "tri_tests": arr[1], "bytes": arr[2], "nodes": arr[3]}
 
     def timings(self):
         arr = (C.c_float * 8)()

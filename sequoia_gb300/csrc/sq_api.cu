@@ -20,7 +20,7 @@ struct sq_ctx {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     std::string err;
-    uint32_t* ctrl = nullptr;  // [0] device error word, [1] work counter, [4..7] trace stats (2 x u64)
+    uint32_t* ctrl = nullptr;  // [0] device error word, [1] work counter, [4..11] trace stats (4 x u64)
     std::multimap<size_t, void*> free_blocks;
     std::map<void*, size_t> live_blocks;
     cudaEvent_t ev[8] = {};
@@ -43,6 +43,8 @@ struct sq_bvh {
     void* nodes8 = nullptr;     // 8-wide quantised nodes (SQ_BUILD_WIDE8)
     void* tris8 = nullptr;      // their 48-byte triangles
     uint32_t n8 = 0;
+    uint32_t levels8 = 0;       // collapse kernel launches
+    uint32_t* ws8 = nullptr;    // collapse queue state (its first word = nodes reserved)
     uint32_t leaf0 = 0;         // first leaf-region slot of the binary tree
 };
 
@@ -277,16 +279,15 @@ sq_status build_wide(sq_ctx* c, sq_bvh* b)
     const uint32_t n = b->n;
     b->nodes8 = dalloc(c, sqk::bvh8_node_bytes(n));
     b->tris8 = dalloc(c, sqk::bvh8_tri_bytes(n));
-    uint32_t* ws = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * (4ull * (n + 2) + 8)));
-    if (!b->nodes8 || !b->tris8 || !ws) {
-        dfree(c, ws);
-        return fail(c, SQ_ERR_OOM, "8-wide BVH allocation failed (n=%u)", n);
-    }
-    const uint32_t cnt = sqk::build_bvh8(b->nodes, b->root, b->leaf0, b->tris, n, b->nodes8, b->tris8, ws, c->host_ctl,
-                                         c->ctrl, c->stream);
-    dfree(c, ws);
-    if (cnt == 0xFFFFFFFFu) return fail(c, SQ_ERR_CUDA, "8-wide collapse: %s", cudaGetErrorString(cudaGetLastError()));
-    b->n8 = cnt;
+    b->ws8 = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * sqk::bvh8_ws_words(n)));
+    if (!b->nodes8 || !b->tris8 || !b->ws8) return fail(c, SQ_ERR_OOM, "8-wide BVH allocation failed (n=%u)", n);
+    const int rc = sqk::build_bvh8(b->nodes, b->root, b->leaf0, b->tris, n, b->nodes8, b->tris8, b->ws8, c->host_ctl,
+                                   c->ctrl, c->stream);
+    if (rc != 0) return fail(c, SQ_ERR_CUDA, "8-wide collapse: %s", cudaGetErrorString((cudaError_t)rc));
+    b->n8 = c->host_ctl[0];
+    b->levels8 = c->host_ctl[3];
+    dfree(c, b->ws8);
+    b->ws8 = nullptr;
     return SQ_OK;
 }
 
@@ -412,19 +413,22 @@ sq_status sq_bvh_free(sq_bvh* b)
     dfree(c, b->perm);
     dfree(c, b->nodes8);
     dfree(c, b->tris8);
+    dfree(c, b->ws8);
     delete b;
     return SQ_OK;
 }
 
-sq_status sq_bvh_get_info(const sq_bvh* b, sq_bvh_info* info)
+sq_status sq_bvh_get_info(const sq_bvh* b_const, sq_bvh_info* info)
 {
-    if (!b || !info) return SQ_ERR_INVALID;
+    if (!b_const || !info) return SQ_ERR_INVALID;
+    const sq_bvh* b = b_const;
     info->node_capacity = b->cap;
     info->root = b->root;
     info->tri_count = b->n;
     info->kind = b->kind;
     for (int k = 0; k < 3; ++k) { info->scene_min[k] = b->scene[k]; info->scene_max[k] = b->scene[3 + k]; }
     info->wide_nodes = b->n8;
+    info->wide_levels = b->levels8;
     return SQ_OK;
 }
 
@@ -642,7 +646,7 @@ sq_status sq_trace(sq_ctx* c, const sq_bvh* b, const sq_ray_source* rays, uint32
     a.err = c->ctrl;
     a.stats = reinterpret_cast<unsigned long long*>(c->ctrl + 4);
     cudaStream_t s = c->stream;
-    SQ_CUDA(c, cudaMemsetAsync(c->ctrl + 1, 0, 7 * sizeof(uint32_t), s));
+    SQ_CUDA(c, cudaMemsetAsync(c->ctrl + 1, 0, 11 * sizeof(uint32_t), s));
     SQ_CUDA(c, cudaEventRecord(c->ev[4], s));
     if (count > 0) {
         if (b->nodes8 && mode != SQ_TRACE_REF && !force_binary) {
@@ -678,6 +682,17 @@ sq_status sq_trace(sq_ctx* c, const sq_bvh* b, const sq_ray_source* rays, uint32
     dfree(c, hits_tmp);
     dfree(c, heat_tmp);
     return st;
+}
+
+sq_status sq_last_trace_stats(sq_ctx* c, uint64_t stats[4])
+{
+    if (!c || !stats) return SQ_ERR_INVALID;
+    Guard g(c->device);
+    SQ_CUDA(c, cudaStreamSynchronize(c->stream));
+    unsigned long long st[4] = {0, 0, 0, 0};
+    SQ_CUDA(c, cudaMemcpy(st, c->ctrl + 4, sizeof st, cudaMemcpyDeviceToHost));
+    for (int k = 0; k < 4; ++k) stats[k] = st[k];
+    return SQ_OK;
 }
 
 sq_status sq_last_timings(sq_ctx* c, float stage_ms[8])

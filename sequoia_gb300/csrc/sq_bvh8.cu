@@ -115,20 +115,19 @@ __device__ __forceinline__ Entry make_entry(const Node* __restrict__ rec, uint32
     return e;
 }
 
-// One thread per 8-wide node: `tasks[i]` = binary record whose children the
-// node holds; `task_node[i]` = index of the node to write.
-__global__ void k_collapse(const Node* __restrict__ rec, uint32_t leaf0, const float* __restrict__ tris,
-                           const uint32_t* __restrict__ tasks, const uint32_t* __restrict__ task_node, uint32_t ntasks,
-                           Node8* __restrict__ nodes8, float4* __restrict__ tris8, uint32_t* __restrict__ counters,
-                           uint32_t* __restrict__ next_tasks, uint32_t* __restrict__ next_node, uint32_t* err)
+// Build the 8-wide node `node_i` from binary record `rec_i`; its inner
+// children become nodes [child_base, child_base + n) where child_base is
+// returned by reserve(n).  Returns false on an error.
+template <class Reserve, class Publish>
+__device__ bool collapse_node(const Node* __restrict__ rec, uint32_t leaf0, const float* __restrict__ tris,
+                              uint32_t rec_i, uint32_t node_i, Node8* __restrict__ nodes8, float4* __restrict__ tris8,
+                              uint32_t* __restrict__ tri_counter, uint32_t* err, Reserve reserve, Publish publish)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ntasks) return;
-    const Node self = rec[tasks[i]];
+    const Node self = rec[rec_i];
     Entry ch[8];
     int nc = 0;
     const uint32_t c0 = self.child, cn = node_count(self.count_flags);
-    if (cn > 8) { raise_error(err, SQ_DEVERR_NODE_COUNT); return; }
+    if (cn > 8) { raise_error(err, SQ_DEVERR_NODE_COUNT); return false; }
     // the start set: a binary record's two children, or a cluster's leaves
     for (uint32_t k = 0; k < cn; ++k) ch[nc++] = make_entry(rec, c0 + k, leaf0);
     // Open the child of largest area until no child can be opened within 8
@@ -152,7 +151,7 @@ __global__ void k_collapse(const Node* __restrict__ rec, uint32_t leaf0, const f
     // own box; larger clusters stay leaf children of up to 15 triangles.
     for (int k = 0; k < nc; ++k)
         if (ch[k].kind == 1 && ch[k].cnt >= 2 && ch[k].cnt <= 8) ch[k].kind = 0;
-    // allocate inner children and leaf triangles (children with an empty box,
+    // count inner children and leaf triangles (children with an empty box,
     // i.e. empty grid cells and subtrees of them, take no slot)
     uint32_t n_inner = 0, n_tris = 0;
     uint32_t cnt[8];
@@ -165,14 +164,12 @@ __global__ void k_collapse(const Node* __restrict__ rec, uint32_t leaf0, const f
         if (ch[k].kind == 0) n_inner++;
         else {
             cnt[k] = node_count(r.count_flags);
-            if (cnt[k] > 15u) { raise_error(err, SQ_DEVERR_NODE_COUNT); return; }
+            if (cnt[k] > 15u) { raise_error(err, SQ_DEVERR_NODE_COUNT); return false; }
             n_tris += cnt[k];
         }
     }
-    const uint32_t child_base = n_inner ? atomicAdd(counters + 0, n_inner) : 0u;
-    const uint32_t tri_base = n_tris ? atomicAdd(counters + 1, n_tris) : 0u;
-    const uint32_t task_base = n_inner ? atomicAdd(counters + 2, n_inner) : 0u;
-    // node box = union of the children (the record's own box)
+    const uint32_t child_base = n_inner ? reserve(n_inner) : 0u;
+    const uint32_t tri_base = n_tris ? atomicAdd(tri_counter, n_tris) : 0u;
     const float lo[3] = {self.mnx, self.mny, self.mnz}, hi[3] = {self.mxx, self.mxy, self.mxz};
     Node8 nd;
     nd.ox = lo[0]; nd.oy = lo[1]; nd.oz = lo[2];
@@ -180,13 +177,12 @@ __global__ void k_collapse(const Node* __restrict__ rec, uint32_t leaf0, const f
     for (int a = 0; a < 3; ++a) e[a] = quant_exp(lo[a], hi[a]);
     uint32_t imask = 0, counts = 0, valid = 0;
     uint32_t inner_rank = 0, tri_off = 0;
-    for (int k = 0; k < 8; ++k) {
+    for (int k = 0; k < 8; ++k)
         for (int a = 0; a < 3; ++a) { nd.qlo[a][k] = 255; nd.qhi[a][k] = 0; }
-    }
     for (int k = 0; k < nc; ++k) {
+        if (!ok[k]) continue;
         const Node r = rec[ch[k].rec];
         const float cl[3] = {r.mnx, r.mny, r.mnz}, chh[3] = {r.mxx, r.mxy, r.mxz};
-        if (!ok[k]) continue;  // empty box: slot unused
         valid |= 1u << k;
         for (int a = 0; a < 3; ++a) {
             nd.qlo[a][k] = quant_lo(cl[a], lo[a], e[a]);
@@ -194,33 +190,19 @@ __global__ void k_collapse(const Node* __restrict__ rec, uint32_t leaf0, const f
         }
         if (ch[k].kind == 0) {
             imask |= 1u << k;
-            next_tasks[task_base + inner_rank] = ch[k].rec;
-            next_node[task_base + inner_rank] = child_base + inner_rank;
+            publish(child_base + inner_rank, ch[k].rec);
             inner_rank++;
         } else {
             counts |= cnt[k] << (4 * k);
-            // copy the leaf's triangles (a cluster's leaf records, or the leaf itself)
-            if (node_is_leaf(r.count_flags)) {
-                for (uint32_t j = 0; j < cnt[k]; ++j) {
-                    const uint32_t id = r.child + j;
-                    float t[9];
-                    load_tri(tris, id, t);
-                    float4* d = tris8 + 3ull * (tri_base + tri_off + j);
-                    d[0] = make_float4(t[0], t[1], t[2], __uint_as_float(id));
-                    d[1] = make_float4(t[3], t[4], t[5], 0.0f);
-                    d[2] = make_float4(t[6], t[7], t[8], 0.0f);
-                }
-            } else {
-                for (uint32_t j = 0; j < cnt[k]; ++j) {
-                    const Node lf = rec[r.child + j];
-                    const uint32_t id = lf.child;
-                    float t[9];
-                    load_tri(tris, id, t);
-                    float4* d = tris8 + 3ull * (tri_base + tri_off + j);
-                    d[0] = make_float4(t[0], t[1], t[2], __uint_as_float(id));
-                    d[1] = make_float4(t[3], t[4], t[5], 0.0f);
-                    d[2] = make_float4(t[6], t[7], t[8], 0.0f);
-                }
+            for (uint32_t j = 0; j < cnt[k]; ++j) {
+                // a leaf record is its own triangle; a cluster's are its leaves
+                const uint32_t id = node_is_leaf(r.count_flags) ? r.child + j : rec[r.child + j].child;
+                float t[9];
+                load_tri(tris, id, t);
+                float4* d = tris8 + 3ull * (tri_base + tri_off + j);
+                d[0] = make_float4(t[0], t[1], t[2], __uint_as_float(id));
+                d[1] = make_float4(t[3], t[4], t[5], 0.0f);
+                d[2] = make_float4(t[6], t[7], t[8], 0.0f);
             }
             tri_off += cnt[k];
         }
@@ -230,7 +212,34 @@ __global__ void k_collapse(const Node* __restrict__ rec, uint32_t leaf0, const f
     nd.tri_base = tri_base;
     nd.counts = counts;
     nd.valid = valid;
-    nodes8[task_node[i]] = nd;
+    nodes8[node_i] = nd;
+    return true;
+}
+
+// One level of the collapse: thread i builds node task_node[i] from binary
+// record tasks[i]; inner children are allocated contiguously from the node
+// counter and appended to the next level's task list.
+__global__ void __launch_bounds__(128) k_collapse_level(const Node* __restrict__ rec, uint32_t leaf0,
+                                                        const float* __restrict__ tris, const uint32_t* __restrict__ tasks,
+                                                        const uint32_t* __restrict__ task_node, uint32_t ntasks,
+                                                        Node8* __restrict__ nodes8, float4* __restrict__ tris8,
+                                                        uint32_t* __restrict__ counters, uint32_t* __restrict__ next_tasks,
+                                                        uint32_t* __restrict__ next_node, uint32_t capacity, uint32_t* err)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ntasks) return;
+    auto reserve = [&](uint32_t k) -> uint32_t {
+        const uint32_t b0 = atomicAdd(counters + 0, k);
+        if ((unsigned long long)b0 + k > capacity) { raise_error(err, SQ_DEVERR_SAH_QUEUE); return 0u; }
+        return b0;
+    };
+    auto publish = [&](uint32_t node, uint32_t record) {
+        if (node >= capacity) return;
+        const uint32_t j = atomicAdd(counters + 2, 1u);
+        next_tasks[j] = record;
+        next_node[j] = node;
+    };
+    collapse_node(rec, leaf0, tris, tasks[i], task_node[i], nodes8, tris8, counters + 1, err, reserve, publish);
 }
 
 // ---------------------------------------------------------------------------
@@ -307,7 +316,7 @@ __device__ __forceinline__ bool tri8(const float4* __restrict__ t8, uint32_t k, 
 struct Res8 {
     uint32_t id;
     float t;
-    uint32_t tests, tri_tests;
+    uint32_t tests, tri_tests, nodes;
     bool overflow;
 };
 
@@ -318,7 +327,7 @@ __device__ Res8 trace8(const Node8* __restrict__ nodes, const float4* __restrict
     prep8(ray, rp);
     float best_t = rp.tmax;
     uint32_t best = kNoHit;
-    uint32_t tests = 0, ttests = 0;
+    uint32_t tests = 0, ttests = 0, nvis = 0;
     bool overflow = false;
     uint32_t st_e[kStack8];
     float st_t[kStack8];
@@ -328,6 +337,7 @@ __device__ Res8 trace8(const Node8* __restrict__ nodes, const float4* __restrict
     while (have) {
         const float4* p = reinterpret_cast<const float4*>(nodes + cur);
         const float4 w0 = __ldg(p), w1 = __ldg(p + 1), w2 = __ldg(p + 2), w3 = __ldg(p + 3), w4 = __ldg(p + 4);
+        nvis++;
         const float org[3] = {w0.x, w0.y, w0.z};
         const uint32_t ei = __float_as_uint(w0.w);
         const float sc[3] = {pow2f((int)(ei & 0xFFu) - 127), pow2f((int)((ei >> 8) & 0xFFu) - 127),
@@ -413,6 +423,7 @@ __device__ Res8 trace8(const Node8* __restrict__ nodes, const float4* __restrict
     r.t = best == kNoHit ? 0.0f : best_t;
     r.tests = tests;
     r.tri_tests = ttests;
+    r.nodes = nvis;
     r.overflow = overflow;
     return r;
 }
@@ -492,18 +503,26 @@ __global__ void __launch_bounds__(128) k_trace8(const sqk::Trace8Args a, uint32_
         Res8 res;
         res.tests = 0;
         res.tri_tests = 0;
+        res.nodes = 0;
         if (active) {
             res = trace8<MODE == SQ_TRACE_ANYHIT>(static_cast<const Node8*>(a.nodes), a.tris8, r);
             if (res.overflow) raise_error(a.err, SQ_DEVERR_STACK_OVERFLOW);
         }
         if (a.stats) {
-            unsigned long long bt = res.tests, tt = res.tri_tests;
+            // requested bytes: ray in (explicit rays), hit record + heatmap out,
+            // 80 B per wide node visited, 48 B per triangle tested
+            unsigned long long bt = res.tests, tt = res.tri_tests, nv = res.nodes;
+            unsigned long long by = active ? (unsigned long long)(camera ? 0u : 32u) + (a.hits ? 12u : 0u) +
+                                                 (a.heat ? 3u : 0u) + 80ull * res.nodes + 48ull * res.tri_tests
+                                           : 0ull;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 bt += __shfl_xor_sync(0xFFFFFFFFu, bt, o);
                 tt += __shfl_xor_sync(0xFFFFFFFFu, tt, o);
+                by += __shfl_xor_sync(0xFFFFFFFFu, by, o);
+                nv += __shfl_xor_sync(0xFFFFFFFFu, nv, o);
             }
-            if (lane == 0) { atomicAdd(a.stats, bt); atomicAdd(a.stats + 1, tt); }
+            if (lane == 0) { atomicAdd(a.stats, bt); atomicAdd(a.stats + 1, tt); atomicAdd(a.stats + 2, by); atomicAdd(a.stats + 3, nv); }
         }
         if (!active) continue;
         if (a.hits) {
@@ -548,38 +567,48 @@ void launch8(const sqk::Trace8Args& a, cudaStream_t s)
 
 namespace sqk {
 
-size_t bvh8_node_bytes(uint32_t n) { return sizeof(Node8) * ((size_t)n + 2); }
+// A wide node has at least two children except the root and nodes next to
+// empty grid cells (at most 64 of those), so n + 130 nodes always suffice.
+uint32_t bvh8_capacity(uint32_t n) { return n + 130u; }
+size_t bvh8_node_bytes(uint32_t n) { return sizeof(Node8) * (size_t)bvh8_capacity(n); }
+size_t bvh8_ws_words(uint32_t n) { return 4ull * bvh8_capacity(n) + 16; }
 size_t bvh8_tri_bytes(uint32_t n) { return sizeof(float4) * 3ull * ((size_t)n + 1); }
 
 // Collapse the binary tree rooted at record `root` (an inner record) into
-// nodes8 / tris8.  ws: 4 * (n + 2) words.  host_ctl: pinned 16 words.
-// Returns the 8-wide node count, or 0xFFFFFFFF on a CUDA error.
-uint32_t build_bvh8(const Node* rec, uint32_t root, uint32_t leaf0, const float* tris, uint32_t n, void* nodes8,
-                    void* tris8, uint32_t* ws, uint32_t* host_ctl, uint32_t* err, cudaStream_t s)
+// nodes8 / tris8, one kernel launch per level of the 8-wide tree (the host
+// reads each level's task count from pinned memory).  ws: bvh8_ws_words(n)
+// words; host_ctl: pinned, 4 words.  Returns 0 or a cudaError_t; the node
+// count is host_ctl[0] and the number of levels host_ctl[3].
+int build_bvh8(const Node* rec, uint32_t root, uint32_t leaf0, const float* tris, uint32_t n, void* nodes8, void* tris8,
+               uint32_t* ws, uint32_t* host_ctl, uint32_t* err, cudaStream_t s)
 {
-    uint32_t* counters = ws;                 // [0] nodes used, [1] tris used, [2] next task count
-    uint32_t* ta = ws + 8;                   // task lists (record index, node index), ping-pong
-    uint32_t* na = ta + (n + 2);
-    uint32_t* tb = na + (n + 2);
-    uint32_t* nb = tb + (n + 2);
-    // level 0: the root record -> node 0
+    const uint32_t capacity = bvh8_capacity(n);
+    uint32_t* counters = ws;  // [0] nodes allocated, [1] triangles placed, [2] next-level tasks
+    uint32_t* ta = ws + 8;    // task lists (record, node), two levels
+    uint32_t* na = ta + capacity;
+    uint32_t* tb = na + capacity;
+    uint32_t* nb = tb + capacity;
+    cudaError_t e;
     const uint32_t init[4] = {1u, 0u, 0u, 0u};
-    if (cudaMemcpyAsync(counters, init, sizeof init, cudaMemcpyHostToDevice, s) != cudaSuccess) return 0xFFFFFFFFu;
+    if ((e = cudaMemcpyAsync(counters, init, sizeof init, cudaMemcpyHostToDevice, s)) != cudaSuccess) return (int)e;
     const uint32_t first[2] = {root, 0u};
-    if (cudaMemcpyAsync(ta, &first[0], 4, cudaMemcpyHostToDevice, s) != cudaSuccess) return 0xFFFFFFFFu;
-    if (cudaMemcpyAsync(na, &first[1], 4, cudaMemcpyHostToDevice, s) != cudaSuccess) return 0xFFFFFFFFu;
-    uint32_t ntasks = 1;
+    if ((e = cudaMemcpyAsync(ta, &first[0], 4, cudaMemcpyHostToDevice, s)) != cudaSuccess) return (int)e;
+    if ((e = cudaMemcpyAsync(na, &first[1], 4, cudaMemcpyHostToDevice, s)) != cudaSuccess) return (int)e;
+    uint32_t ntasks = 1, levels = 0;
     while (ntasks) {
-        if (cudaMemsetAsync(counters + 2, 0, 4, s) != cudaSuccess) return 0xFFFFFFFFu;
-        k_collapse<<<(ntasks + 127) / 128, 128, 0, s>>>(rec, leaf0, tris, ta, na, ntasks, static_cast<Node8*>(nodes8),
-                                                        static_cast<float4*>(tris8), counters, tb, nb, err);
-        if (cudaMemcpyAsync(host_ctl, counters, 12, cudaMemcpyDeviceToHost, s) != cudaSuccess) return 0xFFFFFFFFu;
-        if (cudaStreamSynchronize(s) != cudaSuccess) return 0xFFFFFFFFu;
+        ++levels;
+        if ((e = cudaMemsetAsync(counters + 2, 0, 4, s)) != cudaSuccess) return (int)e;
+        k_collapse_level<<<(ntasks + 127) / 128, 128, 0, s>>>(rec, leaf0, tris, ta, na, ntasks,
+                                                               static_cast<Node8*>(nodes8), static_cast<float4*>(tris8),
+                                                               counters, tb, nb, capacity, err);
+        if ((e = cudaMemcpyAsync(host_ctl, counters, 12, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return (int)e;
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return (int)e;
         ntasks = host_ctl[2];
         std::swap(ta, tb);
         std::swap(na, nb);
     }
-    return host_ctl[0];
+    host_ctl[3] = levels;
+    return (int)cudaGetLastError();
 }
 
 void trace8(const Trace8Args& a, cudaStream_t s)

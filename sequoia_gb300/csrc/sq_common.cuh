@@ -171,7 +171,7 @@ struct TraceArgs {
     uint8_t* heat;        // may be null
     uint32_t* work;       // persistent work counter (zeroed)
     uint32_t* err;
-    unsigned long long* stats;  // {box tests, triangle tests}, accumulated
+    unsigned long long* stats;  // {box tests, triangle tests, bytes requested, node visits}
 };
 void trace(const TraceArgs& a, cudaStream_t s);
 
@@ -189,10 +189,12 @@ struct Trace8Args {
     uint32_t* err;
     unsigned long long* stats;
 };
+uint32_t bvh8_capacity(uint32_t n);
 size_t bvh8_node_bytes(uint32_t n);
+size_t bvh8_ws_words(uint32_t n);
 size_t bvh8_tri_bytes(uint32_t n);
-uint32_t build_bvh8(const sq::Node* rec, uint32_t root, uint32_t leaf0, const float* tris, uint32_t n, void* nodes8,
-                    void* tris8, uint32_t* ws, uint32_t* host_ctl, uint32_t* err, cudaStream_t s);
+int build_bvh8(const sq::Node* rec, uint32_t root, uint32_t leaf0, const float* tris, uint32_t n, void* nodes8,
+               void* tris8, uint32_t* ws, uint32_t* host_ctl, uint32_t* err, cudaStream_t s);
 void trace8(const Trace8Args& a, cudaStream_t s);
 
 }  // namespace sqk

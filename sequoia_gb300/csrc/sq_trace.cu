@@ -447,13 +447,19 @@ __global__ void __launch_bounds__(128) k_trace(const sqk::TraceArgs a, uint32_t 
             if (res.bad) raise_error(a.err, SQ_DEVERR_TOPOLOGY);
         }
         if (a.stats) {
+            // requested bytes: ray in (explicit rays), hit record + heatmap out,
+            // 32 B per node record tested, 36 B per triangle tested
             unsigned long long bt = res.tests, tt = res.tri_tests;
+            unsigned long long by = active ? (unsigned long long)(camera ? 0u : 32u) + (a.hits ? 12u : 0u) +
+                                                 (a.heat ? 3u : 0u) + 32ull * res.tests + 36ull * res.tri_tests
+                                           : 0ull;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 bt += __shfl_xor_sync(0xFFFFFFFFu, bt, o);
                 tt += __shfl_xor_sync(0xFFFFFFFFu, tt, o);
+                by += __shfl_xor_sync(0xFFFFFFFFu, by, o);
             }
-            if (lane == 0) { atomicAdd(a.stats, bt); atomicAdd(a.stats + 1, tt); }
+            if (lane == 0) { atomicAdd(a.stats, bt); atomicAdd(a.stats + 1, tt); atomicAdd(a.stats + 2, by); atomicAdd(a.stats + 3, bt); }
         }
         if (!active) continue;
         if (a.hits) {
