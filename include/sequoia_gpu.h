@@ -258,6 +258,55 @@ sq_status sq_radix_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* v
 sq_status sq_trace(sq_ctx* ctx, const sq_bvh* bvh, const sq_ray_source* rays,
                    uint32_t mode, sq_hit* hits, uint8_t* heatmap_rgb);
 
+/* ---- batches: many meshes and ray tiles, one launch sequence ------------ */
+
+/* Build-and-trace of many independent meshes at once: the reference's
+ * build_hierarchy_morton + trace (src/builder.cpp:2474, src/tracer.cpp:195)
+ * run for every mesh, as one sequence of launches over all meshes, captured
+ * once in a CUDA graph (SQ_BATCH_GRAPH) and replayed by sq_batch_run.  The
+ * reference has no batched form; each mesh's result equals a separate
+ * sq_build + sq_trace of that mesh (same trees, same hits).                */
+typedef struct sq_batch sq_batch;
+
+typedef struct sq_batch_mesh {
+    const sq_triangle* tris;   /* host or device; copied into the batch     */
+    uint32_t tri_count;
+    sq_ray_source rays;        /* camera or explicit rays for this mesh     */
+} sq_batch_mesh;
+
+#define SQ_BATCH_GRAPH 0x1u    /* capture the run in a CUDA graph           */
+
+typedef struct sq_batch_params {
+    uint32_t builder;          /* SQ_BUILDER_MORTON                         */
+    uint32_t sort_digit_bits;  /* 6, 8 or 10 (0 = 8)                        */
+    uint32_t wide;             /* 1: trace the 8-wide quantised BVH         */
+    uint32_t block_threads;    /* trace block: 64, 128 or 256 (0 = 128)     */
+    uint32_t mode;             /* sq_trace_mode                             */
+    uint32_t flags;            /* SQ_BATCH_*                                */
+} sq_batch_params;
+
+typedef struct sq_batch_info {
+    uint32_t meshes, tris, rays;
+    uint32_t graph;            /* 1 if the run is a captured CUDA graph     */
+    sq_batch_params params;
+} sq_batch_info;
+
+sq_status sq_batch_create(sq_ctx* ctx, const sq_batch_mesh* meshes, uint32_t mesh_count,
+                          const sq_batch_params* params, sq_batch** out);
+/* One run: build every mesh and trace every tile.  hits / heatmap_rgb (host
+ * or device, optional) receive all rays' records, mesh after mesh; triangle
+ * ids are per mesh.                                                          */
+sq_status sq_batch_run(sq_batch* batch, sq_hit* hits, uint8_t* heatmap_rgb);
+sq_status sq_batch_info_get(const sq_batch* batch, sq_batch_info* info);
+sq_status sq_batch_free(sq_batch* batch);
+/* Time every sort digit width (6/8/10), BVH width (binary / 8-wide) and
+ * trace block shape (64/128/256) on this batch, keep the fastest (the batch
+ * is re-prepared with it) and return it.  cache_path (optional): JSON-lines
+ * file; a cached choice for the batch's size class is used without timing,
+ * a new choice is appended.                                                 */
+sq_status sq_batch_autotune(sq_batch* batch, const char* cache_path, sq_batch_params* best,
+                            float* best_ms);
+
 /* Device time of the stages of the last sq_build / sq_trace on this context,
  * in milliseconds, measured with CUDA events on the context stream
  * (synchronises).  stage_ms[0] = build total, [1] = bounds+codes, [2] = sort,

@@ -61,6 +61,20 @@ class _RaySource(C.Structure):
                 ("vfov_deg", C.c_float), ("rays", C.c_void_p), ("ray_count", C.c_uint32)]
 
 
+class _BatchMesh(C.Structure):
+    _fields_ = [("tris", C.c_void_p), ("tri_count", C.c_uint32), ("rays", _RaySource)]
+
+
+class _BatchParams(C.Structure):
+    _fields_ = [("builder", C.c_uint32), ("sort_digit_bits", C.c_uint32), ("wide", C.c_uint32),
+                ("block_threads", C.c_uint32), ("mode", C.c_uint32), ("flags", C.c_uint32)]
+
+
+class _BatchInfo(C.Structure):
+    _fields_ = [("meshes", C.c_uint32), ("tris", C.c_uint32), ("rays", C.c_uint32), ("graph", C.c_uint32),
+                ("params", _BatchParams)]
+
+
 _lib = None
 
 
@@ -94,6 +108,11 @@ def load_library():
         "sq_trace": (i32, [vp, vp, C.POINTER(_RaySource), u32, vp, vp]),
         "sq_last_timings": (i32, [vp, C.POINTER(C.c_float * 8)]),
         "sq_last_trace_stats": (i32, [vp, C.POINTER(C.c_uint64 * 4)]),
+        "sq_batch_create": (i32, [vp, C.POINTER(_BatchMesh), u32, C.POINTER(_BatchParams), C.POINTER(vp)]),
+        "sq_batch_run": (i32, [vp, vp, vp]),
+        "sq_batch_info_get": (i32, [vp, C.POINTER(_BatchInfo)]),
+        "sq_batch_free": (i32, [vp]),
+        "sq_batch_autotune": (i32, [vp, C.c_char_p, C.POINTER(_BatchParams), C.POINTER(C.c_float)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -172,6 +191,49 @@ class Bvh:
     def free(self):
         if self.handle:
             load_library().sq_bvh_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many meshes and ray tiles built and traced by one launch sequence
+    (sq_batch), replayed as a CUDA graph."""
+
+    def __init__(self, ctx, handle, keep):
+        self.ctx = ctx
+        self.handle = handle
+        self._keep = keep
+
+    def info(self):
+        i = _BatchInfo()
+        self.ctx._check(load_library().sq_batch_info_get(self.handle, C.byref(i)))
+        p = i.params
+        return {"meshes": i.meshes, "tris": i.tris, "rays": i.rays, "graph": bool(i.graph),
+                "sort_digit_bits": p.sort_digit_bits, "wide": p.wide, "block_threads": p.block_threads,
+                "mode": p.mode}
+
+    def run(self, hits=True, heatmap=False):
+        n = self.info()["rays"]
+        h_arr = np.empty(n, HIT) if hits is True else (hits if hits is not False else None)
+        m_arr = np.empty(n * 3, np.uint8) if heatmap is True else (heatmap if heatmap is not False else None)
+        self.ctx._check(load_library().sq_batch_run(self.handle, _addr(h_arr), _addr(m_arr)))
+        return h_arr, m_arr
+
+    def autotune(self, cache_path=None):
+        best = _BatchParams()
+        ms = C.c_float()
+        path = cache_path.encode() if cache_path else None
+        self.ctx._check(load_library().sq_batch_autotune(self.handle, path, C.byref(best), C.byref(ms)))
+        return {"sort_digit_bits": best.sort_digit_bits, "wide": best.wide, "block_threads": best.block_threads}, ms.value
+
+    def free(self):
+        if self.handle:
+            load_library().sq_batch_free(self.handle)
             self.handle = None
 
     def __del__(self):
@@ -283,6 +345,28 @@ class Context:
         arr = (C.c_uint64 * 4)()
         self._check(load_library().sq_last_trace_stats(self.handle, C.byref(arr)))
         return {"box_tests": arr[0], "tri_tests": arr[1], "bytes": arr[2], "nodes": arr[3]}
+
+    def batch(self, meshes, mode="closest", wide=True, digit_bits=8, block=128, graph=True):
+        """meshes: list of dicts with `tris` and either `rays` (explicit) or a
+        camera (`camera`, `width`, `height`, `origin`, `target`, `up`, `vfov`)."""
+        arr = (_BatchMesh * len(meshes))()
+        keep = []
+        for k, m in enumerate(meshes):
+            t = m["tris"]
+            if isinstance(t, np.ndarray):
+                t = np.ascontiguousarray(t, np.float32)
+            keep.append(t)
+            arr[k].tris = _addr(t)
+            arr[k].tri_count = _len(t, 9)
+            cam = {kk: m[kk] for kk in ("camera", "width", "height", "origin", "target", "up", "vfov") if kk in m}
+            src, _ = self._ray_source(rays=m.get("rays"), **cam)
+            if m.get("rays") is not None:
+                keep.append(m["rays"])
+            arr[k].rays = src
+        p = _BatchParams(0, digit_bits, 1 if wide else 0, block, MODES[mode], 1 if graph else 0)
+        h = C.c_void_p()
+        self._check(load_library().sq_batch_create(self.handle, arr, len(meshes), C.byref(p), C.byref(h)))
+        return Batch(self, h, keep)
 
     def timings(self):
         arr = (C.c_float * 8)()

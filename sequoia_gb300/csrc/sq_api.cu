@@ -3,7 +3,7 @@
 // Host side of the library: contexts (one CUDA stream each), a caching device
 // allocator so repeated builds and traces do not call cudaMalloc, host/device
 // pointer detection, and the build / trace dispatch.
-#include "sq_common.cuh"
+#include "sq_internal.cuh"
 
 #include <cstdarg>
 #include <cstdio>
@@ -13,42 +13,7 @@
 #include <string>
 #include <vector>
 
-using sq::Node;
-
-struct sq_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    std::string err;
-    uint32_t* ctrl = nullptr;  // [0] device error word, [1] work counter, [4..11] trace stats (4 x u64)
-    std::multimap<size_t, void*> free_blocks;
-    std::map<void*, size_t> live_blocks;
-    cudaEvent_t ev[8] = {};
-    bool build_timed = false, trace_timed = false;
-    uint32_t* host_ctl = nullptr;  // pinned, 64 bytes: per-level task counts of the SAH build
-};
-
-struct sq_bvh {
-    sq_ctx* ctx = nullptr;
-    Node* nodes = nullptr;
-    uint32_t cap = 0;
-    uint32_t root = 0;
-    uint32_t n = 0;
-    const float* tris = nullptr;  // device
-    float* tris_own = nullptr;
-    uint32_t kind = 0;
-    float scene[6] = {0, 0, 0, 0, 0, 0};
-    uint32_t* codes = nullptr;  // sorted codes (Morton builds)
-    uint32_t* perm = nullptr;   // sorted permutation
-    void* nodes8 = nullptr;     // 8-wide quantised nodes (SQ_BUILD_WIDE8)
-    void* tris8 = nullptr;      // their 48-byte triangles
-    uint32_t n8 = 0;
-    uint32_t levels8 = 0;       // collapse kernel launches
-    uint32_t* ws8 = nullptr;    // collapse queue state (its first word = nodes reserved)
-    uint32_t leaf0 = 0;         // first leaf-region slot of the binary tree
-};
-
-namespace {
+namespace sqi {
 
 sq_status fail(sq_ctx* c, sq_status st, const char* fmt, ...)
 {
@@ -63,15 +28,7 @@ sq_status fail(sq_ctx* c, sq_status st, const char* fmt, ...)
     return st;
 }
 
-#define SQ_CUDA(c, call)                                                                              \
-    do {                                                                                              \
-        cudaError_t e_ = (call);                                                                      \
-        if (e_ != cudaSuccess)                                                                        \
-            return fail((c), e_ == cudaErrorMemoryAllocation ? SQ_ERR_OOM : SQ_ERR_CUDA, "%s: %s (%s:%d)", \
-                        #call, cudaGetErrorString(e_), __FILE__, __LINE__);                           \
-    } while (0)
-
-size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+static size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 // Caching allocator: freed blocks are kept by size and reused.
 void* dalloc(sq_ctx* c, size_t bytes)
@@ -121,21 +78,6 @@ bool is_device_ptr(const void* p)
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-struct Guard {
-    int prev = -1;
-    explicit Guard(int dev)
-    {
-        cudaGetDevice(&prev);
-        if (prev != dev) cudaSetDevice(dev);
-    }
-    ~Guard()
-    {
-        int cur = -1;
-        cudaGetDevice(&cur);
-        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
-    }
-};
-
 sq_status check_device_error(sq_ctx* c, uint32_t* bits_out)
 {
     uint32_t bits = 0;
@@ -149,6 +91,12 @@ sq_status check_device_error(sq_ctx* c, uint32_t* bits_out)
     }
     return SQ_OK;
 }
+
+}  // namespace sqi
+
+namespace {
+
+using namespace sqi;
 
 uint32_t sort_passes_for(uint32_t key_bits, uint32_t digit_bits) { return (key_bits + digit_bits - 1) / digit_bits; }
 
@@ -293,6 +241,8 @@ sq_status build_wide(sq_ctx* c, sq_bvh* b)
 
 }  // namespace
 
+using namespace sqi;
+
 extern "C" {
 
 uint32_t sq_abi_version(void) { return SQ_ABI_VERSION; }
@@ -386,6 +336,11 @@ sq_status sq_build(sq_ctx* c, const sq_triangle* tris, uint32_t n, const sq_buil
         root.child = 2;
         SQ_CUDA(c, cudaMemcpyAsync(b->nodes, &root, sizeof root, cudaMemcpyHostToDevice, c->stream));
         SQ_CUDA(c, cudaStreamSynchronize(c->stream));
+        b->leaf0 = 2u;
+        if (p.flags & SQ_BUILD_WIDE8) {
+            st = build_wide(c, b);  // one wide root without children
+            if (st != SQ_OK) { sq_bvh_free(b); return st; }
+        }
         *out = b;
         return SQ_OK;
     }

@@ -242,6 +242,77 @@ __global__ void __launch_bounds__(128) k_collapse_level(const Node* __restrict__
     collapse_node(rec, leaf0, tris, tasks[i], task_node[i], nodes8, tris8, counters + 1, err, reserve, publish);
 }
 
+// Persistent collapse over a device work queue (no host synchronisation, so
+// it can be captured in a CUDA graph).  Queue slot i holds the binary record
+// of 8-wide node i (0xFFFFFFFF until written).  `state` packs
+// (nodes processed << 32 | slots reserved): a node reserves its inner
+// children's slots before it counts itself processed, so processed ==
+// reserved, read in one 64-bit load, means no node can appear any more.
+// Every wait is bounded (SQ_DEVERR_SAH_QUEUE when it runs out); all blocks are
+// resident, so the producer a thread waits for is always running.
+constexpr uint32_t kQueueSpin = 1u << 22;
+constexpr uint32_t kEmpty = 0xFFFFFFFFu;
+
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p)
+{
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__global__ void __launch_bounds__(128) k_collapse_queue(const Node* __restrict__ rec, uint32_t leaf0,
+                                                        const float* __restrict__ tris, uint32_t* queue,
+                                                        unsigned long long* state, uint32_t* head, uint32_t capacity,
+                                                        Node8* __restrict__ nodes8, float4* __restrict__ tris8,
+                                                        uint32_t* __restrict__ tri_counter, uint32_t* err)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(head, 32u);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= capacity) return;
+        const uint32_t i = base + lane;
+        bool stop = i >= capacity;
+        uint32_t r = kEmpty;
+        uint32_t spins = 0, nap = 32;
+        while (!stop) {
+            r = ld_volatile_u32(queue + i);
+            if (r != kEmpty) break;
+            const unsigned long long st = ld_acquire_u64(state);
+            const uint32_t reserved = (uint32_t)st, processed = (uint32_t)(st >> 32);
+            if (processed == reserved && i >= reserved) { stop = true; break; }
+            if (++spins > kQueueSpin) { raise_error(err, SQ_DEVERR_SAH_QUEUE); stop = true; break; }
+            __nanosleep(nap);
+            if (nap < 1024) nap <<= 1;
+        }
+        if (!stop) {
+            __threadfence();
+            auto reserve = [&](uint32_t k) -> uint32_t {
+                const unsigned long long old = atomicAdd(state, (unsigned long long)k);
+                const uint32_t b0 = (uint32_t)old;
+                if ((unsigned long long)b0 + k > capacity) { raise_error(err, SQ_DEVERR_SAH_QUEUE); return 0u; }
+                return b0;
+            };
+            auto publish = [&](uint32_t slot, uint32_t record) {
+                if (slot < capacity) st_release_u32(queue + slot, record);
+            };
+            collapse_node(rec, leaf0, tris, r, i, nodes8, tris8, tri_counter, err, reserve, publish);
+            __threadfence();
+            atomicAdd(state, 1ull << 32);
+        }
+        if (__all_sync(0xFFFFFFFFu, stop)) return;
+    }
+}
+
+__global__ void k_queue_seed(const uint32_t* __restrict__ roots, uint32_t nroots, uint32_t* queue,
+                             unsigned long long* state)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nroots; i += gridDim.x * blockDim.x)
+        queue[i] = roots[i];
+    if (blockIdx.x == 0 && threadIdx.x == 0) *state = (unsigned long long)nroots;
+}
+
 // ---------------------------------------------------------------------------
 // traversal
 
@@ -277,6 +348,51 @@ __device__ __forceinline__ void prep8(const Ray8& r, Pre8& p)
 }
 
 __device__ __forceinline__ float sel3(const float* v, int k) { return k == 0 ? v[0] : (k == 1 ? v[1] : v[2]); }
+
+// Camera rays, same arithmetic as the FP32 traversal: the reference camera
+// (src/tracer.cpp:207-216) or the pinhole basis.
+__device__ __forceinline__ void camera_ray8(uint32_t kind, uint32_t x, uint32_t y, uint32_t w, uint32_t h,
+                                            const float* cam, Ray8& r)
+{
+    if (kind == SQ_RAYS_REFERENCE_CAMERA) {
+        const float aspect = (float)w / (float)h;
+        float nx = ((float)x + 0.5f) / (float)w;
+        nx = nx * 2.0f;
+        nx = nx - 1.0f;
+        float ny = ((float)y + 0.5f) / (float)h;
+        ny = ny * 2.0f;
+        ny = ny - 1.0f;
+        nx = nx * aspect;
+        float l2 = nx * nx + ny * ny;
+        l2 = l2 + 1.0f * 1.0f;
+        const float len = sqrtf(l2);
+        r.o[0] = cam[0]; r.o[1] = cam[1]; r.o[2] = cam[2];
+        r.d[0] = nx / len; r.d[1] = ny / len; r.d[2] = 1.0f / len;
+        r.tmin = 0.0f;
+        r.tmax = 10000.0f;
+        return;
+    }
+    float px = ((float)x + 0.5f) / (float)w;
+    px = px * 2.0f;
+    px = px - 1.0f;
+    float py = ((float)y + 0.5f) / (float)h;
+    py = py * 2.0f;
+    py = py - 1.0f;
+    px = px * cam[12];
+    py = py * cam[13];
+    float d[3];
+    for (int k = 0; k < 3; ++k) {
+        const float s = cam[3 + k] + px * cam[6 + k];
+        d[k] = s + py * cam[9 + k];
+    }
+    float l2 = d[0] * d[0] + d[1] * d[1];
+    l2 = l2 + d[2] * d[2];
+    const float len = sqrtf(l2);
+    r.o[0] = cam[0]; r.o[1] = cam[1]; r.o[2] = cam[2];
+    r.d[0] = d[0] / len; r.d[1] = d[1] / len; r.d[2] = d[2] / len;
+    r.tmin = 0.0f;
+    r.tmax = FLT_MAX;
+}
 
 // watertight test (same operations as the FP32 traversal)
 __device__ __forceinline__ bool tri8(const float4* __restrict__ t8, uint32_t k, const Pre8& r, float tmax, float& tout,
@@ -321,7 +437,7 @@ struct Res8 {
 };
 
 template <bool ANY>
-__device__ Res8 trace8(const Node8* __restrict__ nodes, const float4* __restrict__ t8, const Ray8& ray)
+__device__ Res8 trace8(const Node8* __restrict__ nodes, uint32_t root, const float4* __restrict__ t8, const Ray8& ray)
 {
     Pre8 rp;
     prep8(ray, rp);
@@ -332,7 +448,7 @@ __device__ Res8 trace8(const Node8* __restrict__ nodes, const float4* __restrict
     uint32_t st_e[kStack8];
     float st_t[kStack8];
     int sp = 0;
-    uint32_t cur = 0;  // root node
+    uint32_t cur = root;
     bool have = true;
     while (have) {
         const float4* p = reinterpret_cast<const float4*>(nodes + cur);
@@ -505,7 +621,7 @@ __global__ void __launch_bounds__(128) k_trace8(const sqk::Trace8Args a, uint32_
         res.tri_tests = 0;
         res.nodes = 0;
         if (active) {
-            res = trace8<MODE == SQ_TRACE_ANYHIT>(static_cast<const Node8*>(a.nodes), a.tris8, r);
+            res = trace8<MODE == SQ_TRACE_ANYHIT>(static_cast<const Node8*>(a.nodes), 0u, a.tris8, r);
             if (res.overflow) raise_error(a.err, SQ_DEVERR_STACK_OVERFLOW);
         }
         if (a.stats) {
@@ -563,9 +679,141 @@ void launch8(const sqk::Trace8Args& a, cudaStream_t s)
     k_trace8<MODE><<<grid, 128, 0, s>>>(a, batches);
 }
 
+template <int MODE>
+__global__ void __launch_bounds__(256) k_trace8_batch(const sqk::BatchTraceArgs a)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const Node8* nodes = static_cast<const Node8*>(a.nodes8);
+    for (;;) {
+        uint32_t b = 0;
+        if (lane == 0) b = atomicAdd(a.work, 1u);
+        b = __shfl_sync(0xFFFFFFFFu, b, 0);
+        if (b >= a.total_batches) return;
+        const uint32_t j = find_job(a.jobs, a.njobs, b);
+        const sqk::BatchJob& job = a.jobs[j];
+        const uint32_t lb = b - job.batch_begin;
+        Ray8 r;
+        uint32_t rid = 0;
+        bool active;
+        if (job.ray_kind != SQ_RAYS_EXPLICIT) {
+            const uint32_t tiles_x = (job.width + 7u) >> 3;
+            const uint32_t x = (lb % tiles_x) * 8u + (lane & 7u);
+            const uint32_t y = (lb / tiles_x) * 4u + (lane >> 3);
+            active = x < job.width && y < job.height;
+            rid = y * job.width + x;
+            if (active) camera_ray8(job.ray_kind, x, y, job.width, job.height, job.cam, r);
+        } else {
+            rid = lb * 32u + lane;
+            active = rid < job.ray_count;
+            if (active) {
+                const float4* p = reinterpret_cast<const float4*>(a.rays) + 2ull * (job.ray_offset + rid);
+                const float4 x0 = __ldg(p), x1 = __ldg(p + 1);
+                r.o[0] = x0.x; r.o[1] = x0.y; r.o[2] = x0.z; r.tmin = x0.w;
+                r.d[0] = x1.x; r.d[1] = x1.y; r.d[2] = x1.z; r.tmax = x1.w;
+            }
+        }
+        Res8 res;
+        res.tests = 0;
+        res.tri_tests = 0;
+        res.nodes = 0;
+        if (active) {
+            res = trace8<MODE == SQ_TRACE_ANYHIT>(nodes, job.root, a.tris8, r);
+            if (res.overflow) raise_error(a.err, SQ_DEVERR_STACK_OVERFLOW);
+            if (res.id != kNoHit) res.id -= job.tri_offset;
+        }
+        if (a.stats) {
+            unsigned long long bt = res.tests, tt = res.tri_tests, nv = res.nodes;
+            unsigned long long by = active ? (unsigned long long)(job.ray_kind == SQ_RAYS_EXPLICIT ? 32u : 0u) +
+                                                 (a.hits ? 12u : 0u) + (a.heat ? 3u : 0u) + 80ull * res.nodes +
+                                                 48ull * res.tri_tests
+                                           : 0ull;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                bt += __shfl_xor_sync(0xFFFFFFFFu, bt, o);
+                tt += __shfl_xor_sync(0xFFFFFFFFu, tt, o);
+                by += __shfl_xor_sync(0xFFFFFFFFu, by, o);
+                nv += __shfl_xor_sync(0xFFFFFFFFu, nv, o);
+            }
+            if (lane == 0) { atomicAdd(a.stats, bt); atomicAdd(a.stats + 1, tt); atomicAdd(a.stats + 2, by); atomicAdd(a.stats + 3, nv); }
+        }
+        if (!active) continue;
+        const uint64_t out = (uint64_t)job.out_offset + rid;
+        if (a.hits) {
+            uint32_t* h = reinterpret_cast<uint32_t*>(a.hits) + 3ull * out;
+            h[0] = res.id;
+            h[1] = __float_as_uint(res.t);
+            h[2] = res.tests;
+        }
+        if (a.heat) {
+            float x = (float)res.tests / 200.0f;
+            x = (x < 1.0f) ? x : 1.0f;
+            const uint8_t v = (uint8_t)f2u(x * 255.0f);
+            uint8_t* hp = a.heat + 3ull * out;
+            hp[0] = v; hp[1] = v; hp[2] = v;
+        }
+    }
+}
+
+template <int MODE>
+void launch8_batch(const sqk::BatchTraceArgs& a, int block, cudaStream_t s)
+{
+    if (a.total_batches == 0) return;
+    static int per_sm[3] = {0, 0, 0}, sms = 0;
+    const int bi = block <= 64 ? 0 : (block <= 128 ? 1 : 2);
+    if (!per_sm[bi]) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[bi], k_trace8_batch<MODE>, block, 0);
+        if (per_sm[bi] <= 0) per_sm[bi] = 1;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = kNumSMs;
+    }
+    uint32_t grid = (uint32_t)(per_sm[bi] * sms);
+    const uint32_t need = (a.total_batches + (uint32_t)(block / 32) - 1) / (uint32_t)(block / 32);
+    if (grid > need) grid = need;
+    k_trace8_batch<MODE><<<grid, block, 0, s>>>(a);
+}
+
 }  // namespace
 
 namespace sqk {
+
+void trace8_batch(const BatchTraceArgs& a, int block, cudaStream_t s)
+{
+    if (block != 64 && block != 128 && block != 256) block = 128;
+    if (a.mode == SQ_TRACE_ANYHIT) launch8_batch<SQ_TRACE_ANYHIT>(a, block, s);
+    else launch8_batch<SQ_TRACE_CLOSEST>(a, block, s);
+}
+
+int build_bvh8_queue(const Node* rec, const uint32_t* roots_dev, uint32_t nroots, uint32_t leaf0, const float* tris,
+                     uint32_t n, void* nodes8, void* tris8, uint32_t* ws, uint32_t* err, cudaStream_t s)
+{
+    unsigned long long* state = reinterpret_cast<unsigned long long*>(ws);  // ws[0..1]
+    uint32_t* head = ws + 2;
+    uint32_t* tri_counter = ws + 3;
+    uint32_t* queue = ws + 8;
+    const uint32_t capacity = bvh8_capacity(n) + nroots;
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(ws, 0, sizeof(uint32_t) * 8, s)) != cudaSuccess) return (int)e;
+    if ((e = cudaMemsetAsync(queue, 0xFF, sizeof(uint32_t) * (size_t)capacity, s)) != cudaSuccess) return (int)e;
+    k_queue_seed<<<(nroots + 255) / 256, 256, 0, s>>>(roots_dev, nroots, queue, state);
+    static int per_sm = 0, sms = 0;
+    if (!per_sm) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collapse_queue, 128, 0);
+        if (per_sm <= 0) per_sm = 1;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = kNumSMs;
+    }
+    // grid <= one wave, so every block is resident
+    k_collapse_queue<<<(uint32_t)(per_sm * sms), 128, 0, s>>>(rec, leaf0, tris, queue, state, head, capacity,
+                                                             static_cast<Node8*>(nodes8), static_cast<float4*>(tris8),
+                                                             tri_counter, err);
+    return (int)cudaGetLastError();
+}
+
+
 
 // A wide node has at least two children except the root and nodes next to
 // empty grid cells (at most 64 of those), so n + 130 nodes always suffice.

@@ -197,4 +197,56 @@ int build_bvh8(const sq::Node* rec, uint32_t root, uint32_t leaf0, const float* 
                void* tris8, uint32_t* ws, uint32_t* host_ctl, uint32_t* err, cudaStream_t s);
 void trace8(const Trace8Args& a, cudaStream_t s);
 
+// batched trace over many BVHs and ray tiles (sq_trace.cu, sq_bvh8.cu)
+struct BatchJob {
+    uint32_t ray_kind;     // sq_ray_kind
+    uint32_t width, height;
+    uint32_t ray_count;    // rays of this job
+    uint32_t ray_offset;   // explicit rays: first ray in the concatenated ray array
+    uint32_t out_offset;   // first hit record / heatmap pixel of this job
+    uint32_t root;         // binary root record, or 8-wide root node
+    uint32_t batch_begin;  // first 32-ray batch of this job
+    uint32_t tri_offset;   // subtracted from reported triangle ids
+    uint32_t pad[3];
+    float cam[16];         // reference camera origin, or pinhole basis (14 floats)
+};
+static_assert(sizeof(BatchJob) == 112, "BatchJob is 112 bytes");
+
+struct BatchTraceArgs {
+    const sq::Node* nodes;
+    uint32_t node_count, tri_count;
+    const void* nodes8;
+    const float4* tris8;
+    const float* tris;
+    const float* rays;
+    const BatchJob* jobs;
+    uint32_t njobs, total_batches, mode;
+    sq_hit* hits;
+    uint8_t* heat;
+    uint32_t* work;
+    uint32_t* err;
+    unsigned long long* stats;
+};
+void trace_batch(const BatchTraceArgs& a, int block_threads, cudaStream_t s);
+void trace8_batch(const BatchTraceArgs& a, int block_threads, cudaStream_t s);
+
+// 8-wide collapse seeded with several roots, over a device work queue: no
+// host synchronisation, so it can be captured in a CUDA graph.  ws:
+// bvh8_ws_words(n) words.  Wide node k (k < nroots) is the tree of roots[k].
+int build_bvh8_queue(const sq::Node* rec, const uint32_t* roots_dev, uint32_t nroots, uint32_t leaf0, const float* tris,
+                     uint32_t n, void* nodes8, void* tris8, uint32_t* ws, uint32_t* err, cudaStream_t s);
+
 }  // namespace sqk
+
+// Shared helpers for locating a 32-ray batch in a job table.
+namespace sq {
+__device__ __forceinline__ uint32_t find_job(const sqk::BatchJob* __restrict__ jobs, uint32_t njobs, uint32_t b)
+{
+    uint32_t lo = 0, hi = njobs;  // largest j with jobs[j].batch_begin <= b
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&jobs[mid].batch_begin) <= b) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+}  // namespace sq

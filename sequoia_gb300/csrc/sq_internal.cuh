@@ -1,0 +1,77 @@
+// sq_internal.cuh -- host-side internals shared by the C-ABI translation
+// units (sq_api.cu, sq_batch.cu): context and BVH objects, the caching device
+// allocator, pointer-kind detection and error helpers.
+#pragma once
+
+#include "sq_common.cuh"
+
+#include <map>
+#include <string>
+
+using sq::Node;
+
+struct sq_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+    uint32_t* ctrl = nullptr;  // [0] device error word, [1] work counter, [4..11] trace stats (4 x u64)
+    std::multimap<size_t, void*> free_blocks;
+    std::map<void*, size_t> live_blocks;
+    cudaEvent_t ev[8] = {};
+    bool build_timed = false, trace_timed = false;
+    uint32_t* host_ctl = nullptr;  // pinned, 64 bytes: per-level task counts of the SAH build
+};
+
+struct sq_bvh {
+    sq_ctx* ctx = nullptr;
+    Node* nodes = nullptr;
+    uint32_t cap = 0;
+    uint32_t root = 0;
+    uint32_t n = 0;
+    const float* tris = nullptr;  // device
+    float* tris_own = nullptr;
+    uint32_t kind = 0;
+    float scene[6] = {0, 0, 0, 0, 0, 0};
+    uint32_t* codes = nullptr;  // sorted codes (Morton builds)
+    uint32_t* perm = nullptr;   // sorted permutation
+    void* nodes8 = nullptr;     // 8-wide quantised nodes (SQ_BUILD_WIDE8)
+    void* tris8 = nullptr;      // their 48-byte triangles
+    uint32_t n8 = 0;
+    uint32_t levels8 = 0;       // collapse kernel launches
+    uint32_t* ws8 = nullptr;    // collapse queue state (its first word = nodes reserved)
+    uint32_t leaf0 = 0;         // first leaf-region slot of the binary tree
+};
+
+namespace sqi {
+
+sq_status fail(sq_ctx* c, sq_status st, const char* fmt, ...);
+void* dalloc(sq_ctx* c, size_t bytes);
+void dfree(sq_ctx* c, void* p);
+bool is_device_ptr(const void* p);
+sq_status check_device_error(sq_ctx* c, uint32_t* bits_out);
+
+struct Guard {
+    int prev = -1;
+    explicit Guard(int dev)
+    {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~Guard()
+    {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+}  // namespace sqi
+
+#define SQ_CUDA(c, call)                                                                                     \
+    do {                                                                                                     \
+        cudaError_t e_ = (call);                                                                             \
+        if (e_ != cudaSuccess)                                                                               \
+            return sqi::fail((c), e_ == cudaErrorMemoryAllocation ? SQ_ERR_OOM : SQ_ERR_CUDA, "%s: %s (%s:%d)", \
+                             #call, cudaGetErrorString(e_), __FILE__, __LINE__);                             \
+    } while (0)

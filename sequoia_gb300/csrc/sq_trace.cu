@@ -500,9 +500,116 @@ void launch(const sqk::TraceArgs& a, cudaStream_t s)
     k_trace<MODE><<<grid, 128, 0, s>>>(a, batches);
 }
 
+// Batched trace: warps take 32-ray batches of any job (a mesh's BVH and its
+// ray tile) from one counter; each job names its root and ray source.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_trace_batch(const sqk::BatchTraceArgs a)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    for (;;) {
+        uint32_t b = 0;
+        if (lane == 0) b = atomicAdd(a.work, 1u);
+        b = __shfl_sync(0xFFFFFFFFu, b, 0);
+        if (b >= a.total_batches) return;
+        const uint32_t j = find_job(a.jobs, a.njobs, b);
+        const sqk::BatchJob& job = a.jobs[j];
+        const uint32_t lb = b - job.batch_begin;
+        Ray r;
+        uint32_t rid = 0;
+        bool active;
+        if (job.ray_kind != SQ_RAYS_EXPLICIT) {
+            const uint32_t tiles_x = (job.width + 7u) >> 3;
+            const uint32_t x = (lb % tiles_x) * 8u + (lane & 7u);
+            const uint32_t y = (lb / tiles_x) * 4u + (lane >> 3);
+            active = x < job.width && y < job.height;
+            rid = y * job.width + x;
+            if (active) {
+                if (job.ray_kind == SQ_RAYS_REFERENCE_CAMERA) gen_reference_camera(x, y, job.width, job.height, job.cam, r);
+                else gen_pinhole(x, y, job.width, job.height, job.cam, r);
+            }
+        } else {
+            rid = lb * 32u + lane;
+            active = rid < job.ray_count;
+            if (active) {
+                const float4* p = reinterpret_cast<const float4*>(a.rays) + 2ull * (job.ray_offset + rid);
+                const float4 x0 = __ldg(p), x1 = __ldg(p + 1);
+                r.o[0] = x0.x; r.o[1] = x0.y; r.o[2] = x0.z; r.tmin = x0.w;
+                r.d[0] = x1.x; r.d[1] = x1.y; r.d[2] = x1.z; r.tmax = x1.w;
+            }
+        }
+        Result res;
+        res.tests = 0;
+        res.tri_tests = 0;
+        if (active) {
+            if (MODE == SQ_TRACE_REF) res = trace_ref(a.nodes, a.node_count, a.tri_count, job.root, a.tris, r);
+            else res = trace_closest<MODE == SQ_TRACE_ANYHIT>(a.nodes, a.node_count, a.tri_count, job.root, a.tris, r);
+            if (res.overflow) raise_error(a.err, SQ_DEVERR_STACK_OVERFLOW);
+            if (res.bad) raise_error(a.err, SQ_DEVERR_TOPOLOGY);
+            if (MODE != SQ_TRACE_REF && res.id != kNoHit) res.id -= job.tri_offset;
+        }
+        if (a.stats) {
+            unsigned long long bt = res.tests, tt = res.tri_tests;
+            unsigned long long by = active ? (unsigned long long)(job.ray_kind == SQ_RAYS_EXPLICIT ? 32u : 0u) +
+                                                 (a.hits ? 12u : 0u) + (a.heat ? 3u : 0u) + 32ull * res.tests +
+                                                 36ull * res.tri_tests
+                                           : 0ull;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                bt += __shfl_xor_sync(0xFFFFFFFFu, bt, o);
+                tt += __shfl_xor_sync(0xFFFFFFFFu, tt, o);
+                by += __shfl_xor_sync(0xFFFFFFFFu, by, o);
+            }
+            if (lane == 0) { atomicAdd(a.stats, bt); atomicAdd(a.stats + 1, tt); atomicAdd(a.stats + 2, by); atomicAdd(a.stats + 3, bt); }
+        }
+        if (!active) continue;
+        const uint64_t out = (uint64_t)job.out_offset + rid;
+        if (a.hits) {
+            uint32_t* h = reinterpret_cast<uint32_t*>(a.hits) + 3ull * out;
+            h[0] = res.id;
+            h[1] = __float_as_uint(res.t);
+            h[2] = res.tests;
+        }
+        if (a.heat) {
+            float x = (float)res.tests / 200.0f;
+            x = (x < 1.0f) ? x : 1.0f;
+            const uint8_t v = (uint8_t)f2u(x * 255.0f);
+            uint8_t* hp = a.heat + 3ull * out;
+            hp[0] = v; hp[1] = v; hp[2] = v;
+        }
+    }
+}
+
+template <int MODE>
+void launch_batch(const sqk::BatchTraceArgs& a, int block, cudaStream_t s)
+{
+    if (a.total_batches == 0) return;
+    static int per_sm[3] = {0, 0, 0}, sms = 0;
+    const int bi = block <= 64 ? 0 : (block <= 128 ? 1 : 2);
+    if (!per_sm[bi]) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[bi], k_trace_batch<MODE>, block, 0);
+        if (per_sm[bi] <= 0) per_sm[bi] = 1;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = kNumSMs;
+    }
+    uint32_t grid = (uint32_t)(per_sm[bi] * sms);
+    const uint32_t need = (a.total_batches + (uint32_t)(block / 32) - 1) / (uint32_t)(block / 32);
+    if (grid > need) grid = need;
+    k_trace_batch<MODE><<<grid, block, 0, s>>>(a);
+}
+
 }  // namespace
 
 namespace sqk {
+
+void trace_batch(const BatchTraceArgs& a, int block, cudaStream_t s)
+{
+    if (block != 64 && block != 128 && block != 256) block = 128;
+    if (a.mode == SQ_TRACE_REF) launch_batch<SQ_TRACE_REF>(a, block, s);
+    else if (a.mode == SQ_TRACE_CLOSEST) launch_batch<SQ_TRACE_CLOSEST>(a, block, s);
+    else launch_batch<SQ_TRACE_ANYHIT>(a, block, s);
+}
 
 void trace(const TraceArgs& a, cudaStream_t s)
 {
