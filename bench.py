@@ -17,6 +17,11 @@ L2 is flushed between steps (512 MB write).
              origins uniform in the scene box and directions uniform on the
              sphere, in 64 batches of log-uniform size [16K, 1M] traced by
              one launch: 8-wide quantised vs plain FP32, closest and any-hit
+  batch      256 meshes (displaced icospheres and soups, 1K-200K triangles
+             each, log-uniform, seeds 4000+i) with one square primary-ray
+             tile each (side log-uniform in [64, 512]): built and traced by
+             one CUDA-graph launch with the autotuned sort digit width, BVH
+             width and block shape, against 256 separate build+trace calls
   roofline   the dominant kernel (the 8-wide trace): bytes it requested
              (counted by the kernel: node loads, triangle loads, ray records
              and outputs) / kernel time, against the measured HBM bandwidth
@@ -217,6 +222,70 @@ def stress_leg(ctx, flush, torch):
     return out
 
 
+def batch_leg(ctx, flush, torch, sq):
+    """256 meshes with one ray tile each: one graph launch (autotuned) vs 256
+    separate plain build + trace calls, same hits."""
+    from sequoia_gb300 import scenes
+    meshes, tiles = scenes.mesh_batch(256, seed=4000)
+    d_meshes = [torch.from_numpy(m).cuda() for m in meshes]
+    descs = []
+    for m, dm, side in zip(meshes, d_meshes, tiles):
+        lo, hi = scenes.scene_box(m)
+        c = (lo + hi) * 0.5
+        ext = float(max(hi - lo))
+        eye = (float(c[0]), float(c[1]) + 0.5 * ext, float(c[2]) - 2.5 * ext)
+        descs.append(dict(tris=dm, camera="pinhole", width=int(side), height=int(side), origin=eye,
+                          target=tuple(float(x) for x in c), up=(0.0, 1.0, 0.0), vfov=50.0))
+    n_tris = sum(len(m) for m in meshes)
+    n_rays = sum(int(t) * int(t) for t in tiles)
+    b = ctx.batch(descs, mode="closest", wide=True, graph=True)
+    best, tune_ms = b.autotune()
+    for _ in range(3):
+        b.run(hits=False)
+    times = []
+    stream = torch.cuda.current_stream()
+    for _ in range(5):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.run(hits=False)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    got, _ = b.run()
+    b.free()
+    # 256 separate plain (binary FP32, default digits) build + trace calls
+    d_hits = torch.empty(n_rays * 3, dtype=torch.int32, device="cuda")
+    def separate():
+        off = 0
+        for d in descs:
+            bvh = ctx.build(d["tris"], "morton")
+            cnt = d["width"] * d["height"]
+            ctx.trace(bvh, "closest", hits=d_hits[3 * off:3 * (off + cnt)], camera="pinhole", width=d["width"],
+                      height=d["height"], origin=d["origin"], target=d["target"], up=d["up"], vfov=d["vfov"])
+            bvh.free()
+            off += cnt
+    separate()
+    sep = []
+    for _ in range(3):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        separate()
+        e1.record(stream)
+        e1.synchronize()
+        sep.append(e0.elapsed_time(e1))
+    ref = d_hits.view(-1, 3).cpu().numpy()
+    same = bool(np.array_equal(got["id"], ref[:, 0].view(np.uint32)) and np.array_equal(got["t"], ref[:, 1].view(np.float32)))
+    ms, sms = min(times), min(sep)
+    return {"meshes": len(meshes), "tris": n_tris, "rays": n_rays, "autotuned": best,
+            "graph_ms": ms, "graph_mrays_s": n_rays / ms / 1e3, "graph_mtris_s": n_tris / ms / 1e3,
+            "separate_launches_ms": sms, "separate_mrays_s": n_rays / sms / 1e3, "speedup": sms / ms,
+            "same_hits": same}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -323,7 +392,7 @@ def main():
         e2e_total = float(t.item())
     e2e_value = world * rays_total * args.steps / (e2e_total / 1e3) / 1e6
 
-    plain = stress = None
+    plain = stress = batch = None
     if not args.no_extra:
         # plain FP32 binary traversal of the same tree, same rays; same hits?
         bvh = ctx.build(d_tris, "morton", wide=True)
@@ -341,6 +410,7 @@ def main():
                  "same_hits": same}
         del d_hits2
         stress = stress_leg(ctx, flush, torch)
+        batch = batch_leg(ctx, flush, torch, sq)
 
     if rank != 0:
         if dist:
@@ -389,6 +459,7 @@ def main():
                            "frac": build_gbs / peak, "bytes_model": "264 B/tri (200 + 16 x 4 sort passes)"},
         "plain_fp32": plain,
         "stress": stress,
+        "batch": batch,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": n * 36,
                 "d2h_bytes_per_step": rays_total * 15, "ms_per_step": e2e_total / args.steps},

@@ -12,6 +12,7 @@ Triangles are float32 arrays of shape (n, 9): v0, v1, v2.
 """
 from __future__ import annotations
 
+import functools
 import math
 
 import numpy as np
@@ -23,8 +24,21 @@ __all__ = [
 ]
 
 
+@functools.lru_cache(maxsize=8)
+def _icosphere_cached(level: int):
+    v, f = _icosphere(level)
+    v.setflags(write=False)
+    f.setflags(write=False)
+    return v, f
+
+
 def icosphere(level: int):
     """Unit icosphere: returns (vertices float64 (v,3), faces int64 (f,3))."""
+    v, f = _icosphere_cached(level)
+    return v.copy(), f.copy()
+
+
+def _icosphere(level: int):
     t = (1.0 + 5.0 ** 0.5) / 2.0
     v = np.array([(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0),
                   (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
@@ -253,15 +267,20 @@ def batch_sizes(total: int = 1 << 24, count: int = 64, lo: int = 16 << 10,
 def mesh_batch(count: int = 256, seed: int = 4000, lo: int = 1000, hi: int = 200_000):
     """`count` independent meshes (displaced icosphere or Gaussian soup, chosen
     by the per-mesh seed) with triangle counts log-uniform in [lo, hi], and a
-    square primary-ray tile side log-uniform in [64, 512] per mesh."""
+    square primary-ray tile side log-uniform in [64, 512] per mesh.  An
+    icosphere mesh is the first n triangles of the smallest subdivision level
+    that has at least n."""
     meshes, tiles = [], []
     for i in range(count):
         rng = np.random.default_rng(seed + i)
         n = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
         side = int(round(math.exp(rng.uniform(math.log(64), math.log(512)))))
         if rng.uniform() < 0.5:
-            level = max(1, min(7, int(round(math.log(max(n, 20) / 20.0, 4)))))
-            tris = displaced_icosphere(level, seed=seed + i)
+            # the first n triangles of the smallest icosphere level with at least n
+            level = 0
+            while 20 * 4 ** level < n:
+                level += 1
+            tris = np.ascontiguousarray(displaced_icosphere(level, seed=seed + i)[:n])
         else:
             tris = gaussian_soup(n, clusters=8, seed=seed + i)
         meshes.append(tris)
