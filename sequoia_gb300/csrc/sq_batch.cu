@@ -10,8 +10,9 @@
 //                    result is (mesh, code) order, each mesh contiguous
 //   k_seg_climb      the LBVH climb of sq_lbvh.cu that never merges across a
 //                    mesh boundary; mesh m's root record is slot 3N + 2 + m
-//   8-wide collapse  (optional) the work-queue collapse seeded with all mesh
-//                    roots: 8-wide node m is mesh m's root
+//   8-wide collapse  (optional) seeded with all mesh roots, a fixed number
+//                    of level kernels with device-side task counts: 8-wide
+//                    node m is mesh m's root
 // Trace: one persistent kernel over a job table (mesh, camera or rays,
 // output offset); warps take 32-ray batches of any job.
 //
@@ -487,7 +488,7 @@ sq_status sq_batch_create(sq_ctx* c, const sq_batch_mesh* meshes, uint32_t mesh_
     b->d_nodes = static_cast<Node*>(dalloc(c, sizeof(Node) * (3ull * N + 2 + M)));
     b->d_nodes8 = dalloc(c, 80ull * (sqk::bvh8_capacity(N) + M));
     b->d_tris8 = dalloc(c, sqk::bvh8_tri_bytes(N));
-    b->d_ws8 = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * (sqk::bvh8_ws_words(N) + M)));
+    b->d_ws8 = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * (sqk::bvh8_ws_words(N) + 4ull * M)));
     b->d_zero = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * zero));
     b->d_keys = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * 6ull * (N ? N : 1)));
     b->d_info = static_cast<float4*>(dalloc(c, sizeof(float4) * 4ull * (N ? N : 1)));

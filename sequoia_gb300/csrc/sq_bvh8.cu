@@ -242,75 +242,57 @@ __global__ void __launch_bounds__(128) k_collapse_level(const Node* __restrict__
     collapse_node(rec, leaf0, tris, tasks[i], task_node[i], nodes8, tris8, counters + 1, err, reserve, publish);
 }
 
-// Persistent collapse over a device work queue (no host synchronisation, so
-// it can be captured in a CUDA graph).  Queue slot i holds the binary record
-// of 8-wide node i (0xFFFFFFFF until written).  `state` packs
-// (nodes processed << 32 | slots reserved): a node reserves its inner
-// children's slots before it counts itself processed, so processed ==
-// reserved, read in one 64-bit load, means no node can appear any more.
-// Every wait is bounded (SQ_DEVERR_SAH_QUEUE when it runs out); all blocks are
-// resident, so the producer a thread waits for is always running.
-constexpr uint32_t kQueueSpin = 1u << 22;
-constexpr uint32_t kEmpty = 0xFFFFFFFFu;
+// Collapse without host synchronisation (so it can be captured in a CUDA
+// graph): a fixed number of level kernels, each a grid-stride loop over the
+// task count its predecessor left in device memory (counts[level]); a level
+// with no tasks returns at once.  Nothing waits on anything.  If the tree is
+// deeper than the launched levels, the last level raises SQ_DEVERR_SAH_QUEUE.
+constexpr uint32_t kFixedLevels = 64;
 
-__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p)
+__global__ void __launch_bounds__(128) k_collapse_fixed(const Node* __restrict__ rec, uint32_t leaf0,
+                                                        const float* __restrict__ tris, uint32_t level,
+                                                        uint32_t* __restrict__ counts, const uint32_t* __restrict__ tasks,
+                                                        const uint32_t* __restrict__ task_node,
+                                                        uint32_t* __restrict__ next_tasks, uint32_t* __restrict__ next_node,
+                                                        uint32_t* __restrict__ node_counter,
+                                                        uint32_t* __restrict__ tri_counter, Node8* __restrict__ nodes8,
+                                                        float4* __restrict__ tris8, uint32_t capacity, uint32_t* err)
 {
-    unsigned long long v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-
-__global__ void __launch_bounds__(128) k_collapse_queue(const Node* __restrict__ rec, uint32_t leaf0,
-                                                        const float* __restrict__ tris, uint32_t* queue,
-                                                        unsigned long long* state, uint32_t* head, uint32_t capacity,
-                                                        Node8* __restrict__ nodes8, float4* __restrict__ tris8,
-                                                        uint32_t* __restrict__ tri_counter, uint32_t* err)
-{
-    const uint32_t lane = threadIdx.x & 31u;
-    for (;;) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(head, 32u);
-        base = __shfl_sync(0xFFFFFFFFu, base, 0);
-        if (base >= capacity) return;
-        const uint32_t i = base + lane;
-        bool stop = i >= capacity;
-        uint32_t r = kEmpty;
-        uint32_t spins = 0, nap = 32;
-        while (!stop) {
-            r = ld_volatile_u32(queue + i);
-            if (r != kEmpty) break;
-            const unsigned long long st = ld_acquire_u64(state);
-            const uint32_t reserved = (uint32_t)st, processed = (uint32_t)(st >> 32);
-            if (processed == reserved && i >= reserved) { stop = true; break; }
-            if (++spins > kQueueSpin) { raise_error(err, SQ_DEVERR_SAH_QUEUE); stop = true; break; }
-            __nanosleep(nap);
-            if (nap < 1024) nap <<= 1;
-        }
-        if (!stop) {
-            __threadfence();
-            auto reserve = [&](uint32_t k) -> uint32_t {
-                const unsigned long long old = atomicAdd(state, (unsigned long long)k);
-                const uint32_t b0 = (uint32_t)old;
-                if ((unsigned long long)b0 + k > capacity) { raise_error(err, SQ_DEVERR_SAH_QUEUE); return 0u; }
-                return b0;
-            };
-            auto publish = [&](uint32_t slot, uint32_t record) {
-                if (slot < capacity) st_release_u32(queue + slot, record);
-            };
-            collapse_node(rec, leaf0, tris, r, i, nodes8, tris8, tri_counter, err, reserve, publish);
-            __threadfence();
-            atomicAdd(state, 1ull << 32);
-        }
-        if (__all_sync(0xFFFFFFFFu, stop)) return;
+    const uint32_t ntasks = counts[level];
+    if (ntasks == 0) return;
+    if (level + 1 >= kFixedLevels) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) raise_error(err, SQ_DEVERR_SAH_QUEUE);
+        return;
+    }
+    uint32_t* next_count = counts + level + 1;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < ntasks; i += gridDim.x * blockDim.x) {
+        auto reserve = [&](uint32_t k) -> uint32_t {
+            const uint32_t b0 = atomicAdd(node_counter, k);
+            if ((unsigned long long)b0 + k > capacity) { raise_error(err, SQ_DEVERR_SAH_QUEUE); return 0u; }
+            return b0;
+        };
+        auto publish = [&](uint32_t node, uint32_t record) {
+            if (node >= capacity) return;
+            const uint32_t j = atomicAdd(next_count, 1u);
+            next_tasks[j] = record;
+            next_node[j] = node;
+        };
+        collapse_node(rec, leaf0, tris, tasks[i], task_node[i], nodes8, tris8, tri_counter, err, reserve, publish);
     }
 }
 
-__global__ void k_queue_seed(const uint32_t* __restrict__ roots, uint32_t nroots, uint32_t* queue,
-                             unsigned long long* state)
+__global__ void k_fixed_seed(const uint32_t* __restrict__ roots, uint32_t nroots, uint32_t* __restrict__ tasks,
+                             uint32_t* __restrict__ task_node, uint32_t* __restrict__ counts,
+                             uint32_t* __restrict__ node_counter)
 {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nroots; i += gridDim.x * blockDim.x)
-        queue[i] = roots[i];
-    if (blockIdx.x == 0 && threadIdx.x == 0) *state = (unsigned long long)nroots;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nroots; i += gridDim.x * blockDim.x) {
+        tasks[i] = roots[i];
+        task_node[i] = i;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        counts[0] = nroots;
+        *node_counter = nroots;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -788,28 +770,36 @@ void trace8_batch(const BatchTraceArgs& a, int block, cudaStream_t s)
 int build_bvh8_queue(const Node* rec, const uint32_t* roots_dev, uint32_t nroots, uint32_t leaf0, const float* tris,
                      uint32_t n, void* nodes8, void* tris8, uint32_t* ws, uint32_t* err, cudaStream_t s)
 {
-    unsigned long long* state = reinterpret_cast<unsigned long long*>(ws);  // ws[0..1]
-    uint32_t* head = ws + 2;
-    uint32_t* tri_counter = ws + 3;
-    uint32_t* queue = ws + 8;
+    // ws: [0] node counter, [1] triangle counter, [8 .. 8+kFixedLevels] level
+    // counts, then two (record, node) task lists of `capacity` entries
     const uint32_t capacity = bvh8_capacity(n) + nroots;
+    uint32_t* node_counter = ws;
+    uint32_t* tri_counter = ws + 1;
+    uint32_t* counts = ws + 8;
+    uint32_t* ta = counts + kFixedLevels + 8;
+    uint32_t* na = ta + capacity;
+    uint32_t* tb = na + capacity;
+    uint32_t* nb = tb + capacity;
     cudaError_t e;
-    if ((e = cudaMemsetAsync(ws, 0, sizeof(uint32_t) * 8, s)) != cudaSuccess) return (int)e;
-    if ((e = cudaMemsetAsync(queue, 0xFF, sizeof(uint32_t) * (size_t)capacity, s)) != cudaSuccess) return (int)e;
-    k_queue_seed<<<(nroots + 255) / 256, 256, 0, s>>>(roots_dev, nroots, queue, state);
-    static int per_sm = 0, sms = 0;
-    if (!per_sm) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collapse_queue, 128, 0);
-        if (per_sm <= 0) per_sm = 1;
-        int dev = 0;
+    if ((e = cudaMemsetAsync(ws, 0, sizeof(uint32_t) * (16 + kFixedLevels), s)) != cudaSuccess) return (int)e;
+    k_fixed_seed<<<(nroots + 255) / 256, 256, 0, s>>>(roots_dev, nroots, ta, na, counts, node_counter);
+    static int grid = 0;
+    if (!grid) {
+        int per_sm = 0, sms = 0, dev = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collapse_fixed, 128, 0);
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = kNumSMs;
+        grid = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : kNumSMs);
     }
-    // grid <= one wave, so every block is resident
-    k_collapse_queue<<<(uint32_t)(per_sm * sms), 128, 0, s>>>(rec, leaf0, tris, queue, state, head, capacity,
-                                                             static_cast<Node8*>(nodes8), static_cast<float4*>(tris8),
-                                                             tri_counter, err);
+    for (uint32_t level = 0; level < kFixedLevels; ++level) {
+        uint32_t* in_t = (level & 1) ? tb : ta;
+        uint32_t* in_n = (level & 1) ? nb : na;
+        uint32_t* out_t = (level & 1) ? ta : tb;
+        uint32_t* out_n = (level & 1) ? na : nb;
+        k_collapse_fixed<<<grid, 128, 0, s>>>(rec, leaf0, tris, level, counts, in_t, in_n, out_t, out_n, node_counter,
+                                              tri_counter, static_cast<Node8*>(nodes8), static_cast<float4*>(tris8),
+                                              capacity, err);
+    }
     return (int)cudaGetLastError();
 }
 
@@ -819,7 +809,7 @@ int build_bvh8_queue(const Node* rec, const uint32_t* roots_dev, uint32_t nroots
 // empty grid cells (at most 64 of those), so n + 130 nodes always suffice.
 uint32_t bvh8_capacity(uint32_t n) { return n + 130u; }
 size_t bvh8_node_bytes(uint32_t n) { return sizeof(Node8) * (size_t)bvh8_capacity(n); }
-size_t bvh8_ws_words(uint32_t n) { return 4ull * bvh8_capacity(n) + 16; }
+size_t bvh8_ws_words(uint32_t n) { return 4ull * bvh8_capacity(n) + 16 + 2 * kFixedLevels; }
 size_t bvh8_tri_bytes(uint32_t n) { return sizeof(float4) * 3ull * ((size_t)n + 1); }
 
 // Collapse the binary tree rooted at record `root` (an inner record) into

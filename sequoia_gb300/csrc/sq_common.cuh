@@ -230,9 +230,10 @@ struct BatchTraceArgs {
 void trace_batch(const BatchTraceArgs& a, int block_threads, cudaStream_t s);
 void trace8_batch(const BatchTraceArgs& a, int block_threads, cudaStream_t s);
 
-// 8-wide collapse seeded with several roots, over a device work queue: no
-// host synchronisation, so it can be captured in a CUDA graph.  ws:
-// bvh8_ws_words(n) words.  Wide node k (k < nroots) is the tree of roots[k].
+// 8-wide collapse seeded with several roots, with no host synchronisation
+// (a fixed number of level kernels with device-side task counts), so it can
+// be captured in a CUDA graph.  ws: bvh8_ws_words(n) + 4 * nroots words.
+// Wide node k (k < nroots) is the tree of roots[k].
 int build_bvh8_queue(const sq::Node* rec, const uint32_t* roots_dev, uint32_t nroots, uint32_t leaf0, const float* tris,
                      uint32_t n, void* nodes8, void* tris8, uint32_t* ws, uint32_t* err, cudaStream_t s);
 
