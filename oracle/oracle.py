@@ -246,6 +246,8 @@ def ref(variant="b8"):
         L.ref_traverse.argtypes = [vp, u32, u32, vp, u32, vp, u32, vp, vp]
         L.ref_load_obj.argtypes = [C.c_char_p, vp, u32]
         L.ref_load_obj.restype = u32
+        L.ref_write_bmp.argtypes = [C.c_char_p, u32, u32, vp]
+        L.ref_write_bmp.restype = i32
         _refs[variant] = L
     return _refs[variant]
 
@@ -299,6 +301,11 @@ def ref_traverse(nodes, root, tris, rays, variant="b8"):
     ref(variant).ref_traverse(_p(nodes), len(nodes), root, _p(tris), len(tris), _p(rays), len(rays),
                               _p(hit), _p(tests))
     return hit, tests
+
+
+def ref_write_bmp(path, w, h, rgb, variant="b8"):
+    rgb = np.ascontiguousarray(rgb, np.uint8)
+    return int(ref(variant).ref_write_bmp(path.encode(), w, h, _p(rgb)))
 
 
 def ref_load_obj(path, cap=1 << 26, variant="b8"):

@@ -31,6 +31,9 @@ typedef struct alignas(8) RadixInput32 {
 void setup_morton(std::vector<Triangle>& primitives, std::vector<RadixInput32>& morton_codes, AABB1& scene_aabb);
 unsigned find_split_morton(std::vector<RadixInput32>::iterator begin, std::vector<RadixInput32>::iterator end);
 std::vector<Triangle> loadOBJFromFile(std::string filename);
+// stb_image_write v1.14 as compiled into the reference's main.cpp
+extern "C" int stbi_write_bmp(char const* filename, int w, int h, int comp, const void* data);
+extern "C" void stbi_flip_vertically_on_write(int flag);
 
 static std::vector<Triangle> to_tris(const float* t, uint32_t n)
 {
@@ -189,6 +192,13 @@ uint32_t ref_load_obj(const char* path, float* out, uint32_t cap)
         p[6] = v[i].v2.x; p[7] = v[i].v2.y; p[8] = v[i].v2.z;
     }
     return (uint32_t)v.size();
+}
+
+// The reference's image output (src/main.cpp:335-336): flip on, 24-bit BMP
+int ref_write_bmp(const char* path, uint32_t w, uint32_t h, const uint8_t* rgb)
+{
+    stbi_flip_vertically_on_write(1);
+    return stbi_write_bmp(path, (int)w, (int)h, 3, rgb);
 }
 
 }  // extern "C"

@@ -20,7 +20,8 @@ import os
 import numpy as np
 
 __all__ = ["Context", "Bvh", "Hierarchy", "Builder", "trace", "traverse", "SequoiaError",
-           "NODE1", "HIT", "NO_HIT", "library_path", "load_library"]
+           "NODE1", "HIT", "NO_HIT", "library_path", "load_library", "load_obj", "parse_obj",
+           "encode_bmp", "write_bmp"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(HERE, "libsequoia_gpu.so")
@@ -70,6 +71,10 @@ class _BatchParams(C.Structure):
                 ("block_threads", C.c_uint32), ("mode", C.c_uint32), ("flags", C.c_uint32)]
 
 
+class _ObjInfo(C.Structure):
+    _fields_ = [("faces", C.c_uint32), ("vertices", C.c_uint32), ("lines", C.c_uint32), ("threads", C.c_uint32)]
+
+
 class _BatchInfo(C.Structure):
     _fields_ = [("meshes", C.c_uint32), ("tris", C.c_uint32), ("rays", C.c_uint32), ("graph", C.c_uint32),
                 ("params", _BatchParams)]
@@ -113,6 +118,13 @@ def load_library():
         "sq_batch_info_get": (i32, [vp, C.POINTER(_BatchInfo)]),
         "sq_batch_free": (i32, [vp]),
         "sq_batch_autotune": (i32, [vp, C.c_char_p, C.POINTER(_BatchParams), C.POINTER(C.c_float)]),
+        "sq_obj_load": (i32, [C.c_char_p, u32, C.POINTER(vp), C.POINTER(u32), C.POINTER(_ObjInfo)]),
+        "sq_obj_parse": (i32, [vp, C.c_uint64, u32, C.POINTER(vp), C.POINTER(u32), C.POINTER(_ObjInfo)]),
+        "sq_obj_free": (None, [vp]),
+        "sq_bmp_write": (i32, [C.c_char_p, u32, u32, vp]),
+        "sq_bmp_size": (C.c_uint64, [u32, u32]),
+        "sq_bmp_encode": (i32, [u32, u32, vp, vp]),
+        "sq_host_last_error": (C.c_char_p, []),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -449,3 +461,57 @@ def traverse(hierarchy, rays):
     ctx, bvh = _bvh_of(hierarchy)
     hits, _ = ctx.trace(bvh, mode="ref", rays=np.ascontiguousarray(rays, np.float32))
     return (hits["id"] != NO_HIT).astype(np.uint32), hits["tests"].copy()
+
+
+# ---------------------------------------------------------------- host I/O
+
+def _host_check(status):
+    if status != 0:
+        raise SequoiaError(status, load_library().sq_host_last_error().decode(errors="replace"))
+
+
+def _obj_result(L, tp, n, info):
+    try:
+        tris = np.empty((n.value, 9), np.float32)
+        if n.value:
+            C.memmove(tris.ctypes.data, tp.value, tris.nbytes)
+    finally:
+        L.sq_obj_free(tp)
+    return tris, {"faces": info.faces, "vertices": info.vertices, "lines": info.lines, "threads": info.threads}
+
+
+def load_obj(path, threads=0):
+    """loadOBJFromFile (src/main.cpp:108-179) with the reference's parse:
+    returns (float32 (n, 9) triangles, {faces, vertices, lines, threads})."""
+    L = load_library()
+    tp, n, info = C.c_void_p(), C.c_uint32(), _ObjInfo()
+    _host_check(L.sq_obj_load(os.fsencode(path), threads, C.byref(tp), C.byref(n), C.byref(info)))
+    return _obj_result(L, tp, n, info)
+
+
+def parse_obj(data, threads=0):
+    """The same parse over OBJ text in memory (bytes)."""
+    L = load_library()
+    buf = np.frombuffer(bytes(data), np.uint8) if len(data) else np.zeros(1, np.uint8)
+    tp, n, info = C.c_void_p(), C.c_uint32(), _ObjInfo()
+    _host_check(L.sq_obj_parse(buf.ctypes.data, len(data), threads, C.byref(tp), C.byref(n), C.byref(info)))
+    return _obj_result(L, tp, n, info)
+
+
+def encode_bmp(rgb, w, h):
+    """The reference's render.bmp (src/main.cpp:335-336) as bytes."""
+    L = load_library()
+    rgb = np.ascontiguousarray(rgb, np.uint8).reshape(-1)
+    if rgb.size != 3 * w * h:
+        raise ValueError("rgb must hold w*h*3 bytes")
+    out = np.empty(int(L.sq_bmp_size(w, h)), np.uint8)
+    _host_check(L.sq_bmp_encode(w, h, rgb.ctypes.data if rgb.size else None, out.ctypes.data))
+    return out.tobytes()
+
+
+def write_bmp(path, rgb, w, h):
+    L = load_library()
+    rgb = np.ascontiguousarray(rgb, np.uint8).reshape(-1)
+    if rgb.size != 3 * w * h:
+        raise ValueError("rgb must hold w*h*3 bytes")
+    _host_check(L.sq_bmp_write(os.fsencode(path), w, h, rgb.ctypes.data if rgb.size else None))

@@ -1,0 +1,130 @@
+// sequoia.hpp -- C++ drop-in for Sequoia's build/trace entry points.
+//
+// The same names, argument meanings and ownership as the reference
+// (src/aabb.h:17-24, 180-205, src/builder.h:78-104, src/tracer.h:129-135,
+// src/main.cpp:108): Builder::build_hierarchy* return a Hierarchy whose
+// node_base was allocated with new[] (the caller delete[]s it) and whose
+// tri_base points into the caller's vector; trace() returns a new[]'d
+// w*h*3 heatmap.  Every call runs on the GPU through the C ABI of
+// sequoia_gpu.h; nothing here computes on the host except the OBJ parse.
+//
+// Errors: the reference has no error path (it asserts or exits); these
+// functions throw sequoia::Error when the library reports one -- no GPU, a
+// failed CUDA call, a device error word -- and never fall back to the CPU.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "sequoia_gpu.h"
+#include "sequoia_host.h"
+
+namespace sequoia {
+
+struct vec3f1 {
+    float x, y, z;
+    vec3f1() : x(0), y(0), z(0) {}
+    vec3f1(float x_, float y_, float z_) : x(x_), y(y_), z(z_) {}
+};
+
+// src/aabb.h:17-24 (36 bytes)
+struct Triangle {
+    vec3f1 v0, v1, v2;
+    Triangle() = default;
+    Triangle(const vec3f1& a, const vec3f1& b, const vec3f1& c) : v0(a), v1(b), v2(c) {}
+};
+
+enum AABB_FLAGS { AABB_FLAGS_NONE = 0x00, AABB_FLAGS_LEAF = 0x01 };
+
+// src/aabb.h:180-195 (32 bytes).  Inner node: children child .. child+count-1.
+// Leaf: triangles child .. child+count-1 of tri_base.
+struct Node1 {
+    vec3f1 min;
+    uint16_t count;
+    uint16_t flags;
+    vec3f1 max;
+    uint32_t child;
+};
+
+struct PluckerTriangle;  // never produced (the reference leaves it null too)
+
+// src/aabb.h:197-205
+struct Hierarchy {
+    Node1* node_base;
+    unsigned node_count;
+    Triangle* tri_base;
+    PluckerTriangle* plucker_tri_base;
+    unsigned tri_count;
+    unsigned root_index;
+};
+
+static_assert(sizeof(Triangle) == sizeof(sq_triangle), "Triangle layout");
+static_assert(sizeof(Node1) == sizeof(sq_node1), "Node1 layout");
+
+struct Error : std::runtime_error {
+    sq_status status;
+    Error(sq_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+// src/builder.h:78-104.  Builders with no GPU counterpart of their own build
+// the tree of the nearest one: horizontal -> the SAH tree of build_hierarchy
+// (the reference's horizontal top levels are a different split policy);
+// grid_sse and grid_m128 -> build_hierarchy_grid with each cell node bounded
+// by its own triangles (build_hierarchy_grid gives cell nodes the scene box,
+// src/builder.cpp:2173-2174, and the SIMD variants do not).
+class Builder {
+public:
+    static Hierarchy build_hierarchy(std::vector<Triangle>& primitives);
+    static Hierarchy build_hierarchy_morton(std::vector<Triangle>& primitives);
+    static Hierarchy build_hierarchy_morton2(std::vector<Triangle>& primitives);  // throws: 64-bit codes unsupported
+    static Hierarchy build_hierarchy_grid(std::vector<Triangle>& primitives);
+    static Hierarchy build_hierarchy_grid_sse(std::vector<Triangle>& primitives);
+    static Hierarchy build_hierarchy_grid_m128(std::vector<Triangle>& primitives);
+    static Hierarchy build_hierarchy_horizontal(std::vector<Triangle>& primitives);
+};
+
+// src/tracer.cpp:195-230: w*h rays from the reference camera at `origin`, the
+// per-ray box-test count as a grey heatmap (new[]'d, w*h*3 bytes).
+uint8_t* trace(Hierarchy& hierarchy, uint32_t w, uint32_t h, vec3f1 origin);
+
+// src/tracer.h:131-135.  The reference's packet and bundle tracers count box
+// tests per packet, so their heatmaps differ from trace()'s; on the GPU every
+// warp is already a 32-ray packet, and these return trace()'s image.
+template <size_t K>
+uint8_t* trace_packet(Hierarchy& hierarchy, uint32_t w, uint32_t h, vec3f1 origin)
+{
+    return trace(hierarchy, w, h, origin);
+}
+template <size_t K>
+uint8_t* trace_bundle(Hierarchy& hierarchy, uint32_t w, uint32_t h, vec3f1 origin)
+{
+    return trace(hierarchy, w, h, origin);
+}
+
+// src/main.cpp:108-179, with the same parse (sq_obj_load); prints the same
+// "Geometry" summary.  A file that cannot be opened is reported on stderr and
+// exits with status 1, as the reference does; a malformed file throws.
+std::vector<Triangle> loadOBJFromFile(std::string filename);
+
+// ---- GB300 additions -------------------------------------------------------
+
+// Parameters of the next builds (bins, leaf size, sort digit width, Morton
+// bounds, SQ_BUILD_WIDE8).  kind and the grid scene-bounds flag are set by
+// the Builder function called.
+void set_build_params(const sq_build_params& params);
+sq_build_params build_params();
+// Threads of the OBJ parse (0 = all hardware threads; the CLI's -threads).
+void set_host_threads(uint32_t threads);
+// The process-wide context (device from SEQUOIA_DEVICE, default 0).
+sq_ctx* context();
+// The device tree behind a Hierarchy returned by Builder (null if none).
+sq_bvh* device_tree(const Hierarchy& hierarchy);
+// delete[] node_base and free the device tree.
+void release(Hierarchy& hierarchy);
+// Timings of the last build or trace (sq_last_timings).
+void last_timings(float stage_ms[8]);
+
+}  // namespace sequoia
