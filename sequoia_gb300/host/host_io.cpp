@@ -28,6 +28,11 @@
 #include <thread>
 #include <vector>
 
+#include <fcntl.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
 namespace {
 
 thread_local std::string g_error;
@@ -74,7 +79,7 @@ inline Token next_token(const char*& s, const char* e, bool first)
 
 // atof / atoi on a NUL-terminated copy of the token, as the reference calls
 // them on gstrtok's static buffer
-inline float token_float(const Token& t)
+inline float token_float_libc(const Token& t)
 {
     char buf[kLineMax + 1];
     memcpy(buf, t.p, t.len);
@@ -82,12 +87,93 @@ inline float token_float(const Token& t)
     return (float)strtod(buf, nullptr);
 }
 
-inline int token_int(const Token& t)
+inline int token_int_libc(const Token& t)
 {
     char buf[kLineMax + 1];
     memcpy(buf, t.p, t.len);
     buf[t.len] = '\0';
     return (int)strtol(buf, nullptr, 10);
+}
+
+// Exact powers of ten in double (10^0 .. 10^22 are all representable).
+constexpr double kPow10[23] = {1e0,  1e1,  1e2,  1e3,  1e4,  1e5,  1e6,  1e7,  1e8,  1e9,  1e10, 1e11,
+                               1e12, 1e13, 1e14, 1e15, 1e16, 1e17, 1e18, 1e19, 1e20, 1e21, 1e22};
+
+// (float)atof(token) without the library call for plain decimals, by
+// Clinger's fast path (W. D. Clinger, "How to read floating point numbers
+// accurately", PLDI 1990): when the decimal significand m < 2^53 and the
+// decimal exponent |e| <= 22, both m and 10^|e| are exact doubles, so the one
+// IEEE multiply or divide m * 10^e is the correctly rounded double -- the
+// value strtod returns.  The float is then that double rounded to float, as
+// the reference's (float)atof does.  Only a token that is exactly
+// [+-]digits[.digits][(e|E)[+-]digits] (optionally followed by '\r', where
+// strtod stops too) takes the fast path; everything else (leading
+// whitespace, hex, inf/nan, trailing text, long significands, large
+// exponents) goes to strtod itself.
+inline float token_float(const Token& t)
+{
+    const char* p = t.p;
+    const char* e = t.p + t.len;
+    if (e > p && e[-1] == '\r') --e;
+    if (p == e) return token_float_libc(t);
+    bool neg = false;
+    if (*p == '+' || *p == '-') neg = *p++ == '-';
+    uint64_t m = 0;
+    int digits = 0, frac = 0;
+    bool any = false;
+    while (p < e && *p >= '0' && *p <= '9') {
+        if (m || *p != '0') ++digits;
+        m = m * 10 + (uint64_t)(*p++ - '0');
+        any = true;
+        if (digits > 18) return token_float_libc(t);
+    }
+    if (p < e && *p == '.') {
+        ++p;
+        while (p < e && *p >= '0' && *p <= '9') {
+            if (m || *p != '0') ++digits;
+            m = m * 10 + (uint64_t)(*p++ - '0');
+            ++frac;
+            any = true;
+            if (digits > 18) return token_float_libc(t);
+        }
+    }
+    if (!any) return token_float_libc(t);
+    int ex = 0;
+    if (p < e && (*p == 'e' || *p == 'E')) {
+        ++p;
+        bool eneg = false;
+        if (p < e && (*p == '+' || *p == '-')) eneg = *p++ == '-';
+        if (p == e) return token_float_libc(t);
+        while (p < e && *p >= '0' && *p <= '9') {
+            ex = ex * 10 + (*p++ - '0');
+            if (ex > 1000) return token_float_libc(t);
+        }
+        if (eneg) ex = -ex;
+    }
+    if (p != e) return token_float_libc(t);
+    ex -= frac;
+    if (m > (1ull << 53) || ex < -22 || ex > 22) return token_float_libc(t);
+    double v = (double)m;
+    v = ex < 0 ? v / kPow10[-ex] : v * kPow10[ex];
+    return (float)(neg ? -v : v);
+}
+
+// atoi(token) = (int)strtol(token, NULL, 10); the fast path takes
+// [+-]digits with at most 9 digits (no overflow), stopping at the first
+// non-digit as strtol does ("7/2/9" reads 7).
+inline int token_int(const Token& t)
+{
+    const char* p = t.p;
+    const char* e = t.p + t.len;
+    bool neg = false;
+    if (p < e && (*p == '+' || *p == '-')) neg = *p++ == '-';
+    int v = 0, n = 0;
+    while (p < e && *p >= '0' && *p <= '9') {
+        if (++n > 9) return token_int_libc(t);
+        v = v * 10 + (*p++ - '0');
+    }
+    if (n == 0) return token_int_libc(t);
+    return neg ? -v : v;
 }
 
 struct Chunk {
@@ -298,18 +384,34 @@ sq_status sq_obj_parse(const char* text, uint64_t len, uint32_t threads, sq_tria
 sq_status sq_obj_load(const char* path, uint32_t threads, sq_triangle** tris, uint32_t* tri_count, sq_obj_info* info)
 {
     if (!path) return host_fail(SQ_ERR_INVALID, "null path");
-    FILE* fp = fopen(path, "rb");
-    if (!fp) return host_fail(SQ_ERR_INVALID, "Can't open OBJ file %s: %s", path, strerror(errno));
-    std::vector<char> buf;
-    if (fseek(fp, 0, SEEK_END) == 0) {
-        const long size = ftell(fp);
-        if (size > 0) buf.resize((size_t)size);
-        fseek(fp, 0, SEEK_SET);
+    const int fd = open(path, O_RDONLY);
+    if (fd < 0) return host_fail(SQ_ERR_INVALID, "Can't open OBJ file %s: %s", path, strerror(errno));
+    struct stat st;
+    if (fstat(fd, &st) == 0 && S_ISREG(st.st_mode) && st.st_size > 0) {
+        // a regular file is mapped, so the parse threads fault its pages in
+        // parallel instead of waiting for one sequential read
+        void* m = mmap(nullptr, (size_t)st.st_size, PROT_READ, MAP_PRIVATE, fd, 0);
+        if (m != MAP_FAILED) {
+            close(fd);
+            const sq_status s = sq_obj_parse(static_cast<const char*>(m), (uint64_t)st.st_size, threads, tris,
+                                             tri_count, info);
+            munmap(m, (size_t)st.st_size);
+            return s;
+        }
     }
-    size_t got = buf.empty() ? 0 : fread(buf.data(), 1, buf.size(), fp);
-    const bool err = ferror(fp) != 0;
-    fclose(fp);
-    if (err || got != buf.size()) return host_fail(SQ_ERR_INVALID, "read error on OBJ file %s", path);
+    std::vector<char> buf;
+    char tmp[1 << 16];
+    for (;;) {
+        const ssize_t got = read(fd, tmp, sizeof(tmp));
+        if (got < 0 && errno == EINTR) continue;
+        if (got < 0) {
+            close(fd);
+            return host_fail(SQ_ERR_INVALID, "read error on OBJ file %s: %s", path, strerror(errno));
+        }
+        if (got == 0) break;
+        buf.insert(buf.end(), tmp, tmp + got);
+    }
+    close(fd);
     return sq_obj_parse(buf.data(), buf.size(), threads, tris, tri_count, info);
 }
 
