@@ -121,6 +121,22 @@ def dist_info():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+def reduce_max(x, dist, device="cuda"):
+    """Max of a per-rank float over all ranks (the slowest rank's time)."""
+    if not dist:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_value(rays_per_step, steps, world, total_ms):
+    """Mrays/s of the whole job: every rank traces rays_per_step rays per step
+    (independent replicas), timed by the slowest rank."""
+    return world * rays_per_step * steps / (total_ms / 1e3) / 1e6
+
+
 def make_scene():
     from sequoia_gb300 import scenes
     w = WORKLOAD
@@ -362,13 +378,9 @@ def main():
     if dist:
         dist.barrier()
     clk = clocks.stop()
-    total_ms = float(sum(step_ms))
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = reduce_max(sum(step_ms), dist)
     ms_per_step = total_ms / args.steps
-    value = world * rays_total * args.steps / (total_ms / 1e3) / 1e6
+    value = whole_job_value(rays_total, args.steps, world, total_ms)
 
     # end to end through the public API with pinned host buffers
     e2e_ms = []
@@ -385,12 +397,8 @@ def main():
             torch.cuda.synchronize()
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
             bvh.free()
-    e2e_total = float(sum(e2e_ms)) if e2e_ms else float("nan")
-    if dist:
-        t = torch.tensor([e2e_total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_total = float(t.item())
-    e2e_value = world * rays_total * args.steps / (e2e_total / 1e3) / 1e6
+    e2e_total = reduce_max(sum(e2e_ms) if e2e_ms else float("nan"), dist)
+    e2e_value = whole_job_value(rays_total, args.steps, world, e2e_total)
 
     plain = stress = batch = None
     if not args.no_extra:

@@ -418,11 +418,33 @@ struct Res8 {
     bool overflow;
 };
 
-template <bool ANY>
-__device__ Res8 trace8(const Node8* __restrict__ nodes, uint32_t root, const float4* __restrict__ t8, const Ray8& ray)
+// Quantised coordinate j (0..3) of a packed word as an exact float: the byte
+// is placed in the mantissa of 2^23 (one byte permute) and 2^23 subtracted.
+__device__ __forceinline__ float qbyte(uint32_t word, uint32_t j)
 {
-    Pre8 rp;
-    prep8(ray, rp);
+    return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u | j)) - 8388608.0f;
+}
+
+// A ray for which no slab distance can be NaN: finite origin and finite,
+// non-zero reciprocal direction (so bound - origin is finite or +-inf and its
+// product with the reciprocal is never 0 * inf).  For such a ray the near
+// plane of each axis is known from the sign of the direction, and the
+// near/far distances are exactly what the min/max form of the slab test
+// computes (min(t0, t1) is t0 when the reciprocal is positive, because the
+// rounded product is monotone in the bound); so the test can pick the near
+// and far byte once per node instead of taking min and max per child.
+__device__ __forceinline__ bool no_nan_slabs(const Pre8& r)
+{
+    bool ok = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) ok = ok && isfinite(r.o[a]) && isfinite(r.inv[a]) && r.inv[a] != 0.0f;
+    return ok;
+}
+
+template <bool ANY, bool SIGNED>
+__device__ Res8 trace8_impl(const Node8* __restrict__ nodes, uint32_t root, const float4* __restrict__ t8,
+                            const Pre8& rp)
+{
     float best_t = rp.tmax;
     uint32_t best = kNoHit;
     uint32_t tests = 0, ttests = 0, nvis = 0;
@@ -432,6 +454,8 @@ __device__ Res8 trace8(const Node8* __restrict__ nodes, uint32_t root, const flo
     int sp = 0;
     uint32_t cur = root;
     bool have = true;
+    // SIGNED: which of the (lo, hi) word pairs holds the near plane, per axis
+    const bool neg[3] = {rp.inv[0] < 0.0f, rp.inv[1] < 0.0f, rp.inv[2] < 0.0f};
     while (have) {
         const float4* p = reinterpret_cast<const float4*>(nodes + cur);
         const float4 w0 = __ldg(p), w1 = __ldg(p + 1), w2 = __ldg(p + 2), w3 = __ldg(p + 3), w4 = __ldg(p + 4);
@@ -443,10 +467,20 @@ __device__ Res8 trace8(const Node8* __restrict__ nodes, uint32_t root, const flo
         const uint32_t imask = ei >> 24;
         const uint32_t child_base = __float_as_uint(w1.x), tri_base = __float_as_uint(w1.y);
         const uint32_t counts = __float_as_uint(w1.z), valid = __float_as_uint(w1.w);
+        // q words: qlo x (2 words: slots 0-3, 4-7), qlo y, qlo z, qhi x, qhi y, qhi z
         const uint32_t q[12] = {__float_as_uint(w2.x), __float_as_uint(w2.y), __float_as_uint(w2.z), __float_as_uint(w2.w),
                                 __float_as_uint(w3.x), __float_as_uint(w3.y), __float_as_uint(w3.z), __float_as_uint(w3.w),
                                 __float_as_uint(w4.x), __float_as_uint(w4.y), __float_as_uint(w4.z), __float_as_uint(w4.w)};
-        // q words: qlo x (2 words: slots 0-3, 4-7), qlo y, qlo z, qhi x, qhi y, qhi z
+        uint32_t qa[6], qb[6];  // SIGNED: near and far words; otherwise lo and hi
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+#pragma unroll
+            for (int w = 0; w < 2; ++w) {
+                const uint32_t lo = q[a * 2 + w], hi = q[6 + a * 2 + w];
+                qa[a * 2 + w] = (SIGNED && neg[a]) ? hi : lo;
+                qb[a * 2 + w] = (SIGNED && neg[a]) ? lo : hi;
+            }
+        }
         uint32_t hn[8];
         float ht[8];
         int nh = 0;
@@ -456,24 +490,25 @@ __device__ Res8 trace8(const Node8* __restrict__ nodes, uint32_t root, const flo
             const uint32_t cnt = (counts >> (4 * k)) & 0xFu;
             const bool is_inner = (imask >> k) & 1u;
             if ((valid >> k) & 1u) {
-                const int w = k >> 2, sh = (k & 3) * 8;
-                float lo[3], hi[3];
+                const int w = k >> 2;
+                const uint32_t j = (uint32_t)(k & 3);
+                float ta[3], tb[3];
 #pragma unroll
                 for (int a = 0; a < 3; ++a) {
-                    const float ql = (float)((q[a * 2 + w] >> sh) & 0xFFu);
-                    const float qh = (float)((q[6 + a * 2 + w] >> sh) & 0xFFu);
-                    lo[a] = fmaf(ql, sc[a], org[a]);
-                    hi[a] = fmaf(qh, sc[a], org[a]);
+                    const float ba = fmaf(qbyte(qa[a * 2 + w], j), sc[a], org[a]);
+                    const float bb = fmaf(qbyte(qb[a * 2 + w], j), sc[a], org[a]);
+                    ta[a] = (ba - rp.o[a]) * rp.inv[a];
+                    tb[a] = (bb - rp.o[a]) * rp.inv[a];
                 }
                 tests++;
-                const float t0x = (lo[0] - rp.o[0]) * rp.inv[0];
-                const float t1x = (hi[0] - rp.o[0]) * rp.inv[0];
-                const float t0y = (lo[1] - rp.o[1]) * rp.inv[1];
-                const float t1y = (hi[1] - rp.o[1]) * rp.inv[1];
-                const float t0z = (lo[2] - rp.o[2]) * rp.inv[2];
-                const float t1z = (hi[2] - rp.o[2]) * rp.inv[2];
-                const float n = fmaxf(fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z)), rp.tmin);
-                float f = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+                float n, f;
+                if (SIGNED) {
+                    n = fmaxf(fmaxf(fmaxf(ta[0], ta[1]), ta[2]), rp.tmin);
+                    f = fminf(fminf(tb[0], tb[1]), tb[2]);
+                } else {
+                    n = fmaxf(fmaxf(fmaxf(fminf(ta[0], tb[0]), fminf(ta[1], tb[1])), fminf(ta[2], tb[2])), rp.tmin);
+                    f = fminf(fminf(fmaxf(ta[0], tb[0]), fmaxf(ta[1], tb[1])), fmaxf(ta[2], tb[2]));
+                }
                 f = f * kRobust;
                 if (n <= f && n <= best_t * kRobust) {
                     const uint32_t ent = is_inner ? (child_base + inner_rank)
@@ -524,6 +559,15 @@ __device__ Res8 trace8(const Node8* __restrict__ nodes, uint32_t root, const flo
     r.nodes = nvis;
     r.overflow = overflow;
     return r;
+}
+
+template <bool ANY>
+__device__ Res8 trace8(const Node8* __restrict__ nodes, uint32_t root, const float4* __restrict__ t8, const Ray8& ray)
+{
+    Pre8 rp;
+    prep8(ray, rp);
+    if (no_nan_slabs(rp)) return trace8_impl<ANY, true>(nodes, root, t8, rp);
+    return trace8_impl<ANY, false>(nodes, root, t8, rp);
 }
 
 __device__ __forceinline__ uint32_t f2u(float x) { return (x >= 0.0f) ? (uint32_t)x : 0u; }
