@@ -621,6 +621,7 @@ sq_status sq_trace(sq_ctx* c, const sq_bvh* b, const sq_ray_source* rays, uint32
             w.work = a.work;
             w.err = a.err;
             w.stats = a.stats;
+            w.refill = a.ray_kind == SQ_RAYS_EXPLICIT ? 1u : 0u;  // camera rays: coherent 8x4 tiles per warp
             sqk::trace8(w, s);
         } else {
             sqk::trace(a, s);

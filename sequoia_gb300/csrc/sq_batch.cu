@@ -345,6 +345,9 @@ sq_status enqueue_run(sq_batch* b)
     a.work = c->ctrl + 1;
     a.err = c->ctrl;
     a.stats = reinterpret_cast<unsigned long long*>(c->ctrl + 4);
+    // per-lane ray refill when most rays are explicit (incoherent); camera
+    // tiles keep whole 32-ray batches per warp
+    a.refill = 2ull * b->explicit_rays > (uint64_t)b->rays ? 1u : 0u;
     const int block = b->params.block_threads ? (int)b->params.block_threads : 128;
     if (wide && a.mode != SQ_TRACE_REF) sqk::trace8_batch(a, block, s);
     else sqk::trace_batch(a, block, s);

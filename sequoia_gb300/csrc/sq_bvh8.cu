@@ -411,12 +411,6 @@ __device__ __forceinline__ bool tri8(const float4* __restrict__ t8, uint32_t k, 
     return true;
 }
 
-struct Res8 {
-    uint32_t id;
-    float t;
-    uint32_t tests, tri_tests, nodes;
-    bool overflow;
-};
 
 // Quantised coordinate j (0..3) of a packed word as an exact float: the byte
 // is placed in the mantissa of 2^23 (one byte permute) and 2^23 subtracted.
@@ -441,6 +435,16 @@ __device__ __forceinline__ bool no_nan_slabs(const Pre8& r)
     return ok;
 }
 
+struct Res8 {
+    uint32_t id;
+    float t;
+    uint32_t tests, tri_tests, nodes;
+    bool overflow;
+};
+
+// One ray from the root to the end: the nearest hit child is taken next,
+// the other hits are pushed far to near (popped entries are culled against
+// the current closest distance).
 template <bool ANY, bool SIGNED>
 __device__ Res8 trace8_impl(const Node8* __restrict__ nodes, uint32_t root, const float4* __restrict__ t8,
                             const Pre8& rp)
@@ -572,8 +576,182 @@ __device__ Res8 trace8(const Node8* __restrict__ nodes, uint32_t root, const flo
 
 __device__ __forceinline__ uint32_t f2u(float x) { return (x >= 0.0f) ? (uint32_t)x : 0u; }
 
+// ---------------------------------------------------------------------------
+// Persistent traversal kernels hand out rays in one of two ways (persistent
+// threads, Aila and Laine, HPG 2009):
+//   tiles    a warp takes a whole 32-ray batch (an 8x4 pixel tile of a
+//            camera) and each lane runs its ray to the end (trace8); the
+//            warp takes the next batch when all its lanes are done.  This
+//            keeps neighbouring primary rays in one warp and their node
+//            fetches shared -- the choice for camera rays;
+//   refill   one ray per lane as a state machine that visits one wide node
+//            per loop iteration (visit8); a lane whose ray has finished takes
+//            the next unprocessed ray at once (one atomic per warp for all
+//            lanes that need one), so a warp never idles behind its slowest
+//            ray -- the choice for explicit (typically incoherent) rays.
+// Both visit children in the same order (ascending entry distance, then
+// slot), so they count the same box tests for the same ray.
+
+struct Lane8 {
+    Pre8 rp;
+    float best_t;
+    uint32_t best, tests, ttests, nvis;
+    uint32_t cur;  // next wide node to visit, or kNoHit when the ray is finished
+    int sp;
+    bool overflow;
+};
+
+__device__ __forceinline__ void lane_start(Lane8& L, const Ray8& ray, uint32_t root)
+{
+    prep8(ray, L.rp);
+    L.best_t = L.rp.tmax;
+    L.best = kNoHit;
+    L.tests = L.ttests = L.nvis = 0;
+    L.cur = root;
+    L.sp = 0;
+    L.overflow = false;
+}
+
+// Test a leaf entry's triangles; returns true when an any-hit ray is done.
+template <bool ANY>
+__device__ __forceinline__ bool leaf8(Lane8& L, const float4* __restrict__ t8, uint32_t e)
+{
+    const uint32_t cnt = (e >> 27) & 0xFu, first = e & 0x07FFFFFFu;
+    for (uint32_t j = 0; j < cnt; ++j) {
+        float t;
+        uint32_t id;
+        L.ttests++;
+        if (tri8(t8, first + j, L.rp, L.best_t, t, id)) {
+            if (t < L.best_t || (t == L.best_t && id < L.best)) { L.best_t = t; L.best = id; }
+            if (ANY) return true;
+        }
+    }
+    return false;
+}
+
+// Visit node L.cur; afterwards L.cur is the next node, or kNoHit when the
+// ray has finished (stack empty, any-hit found, or stack overflow).
+template <bool ANY, bool SIGNED>
+__device__ __forceinline__ void visit8(Lane8& L, const Node8* __restrict__ nodes, const float4* __restrict__ t8,
+                                       uint32_t* st_e, float* st_t)
+{
+    const Pre8& rp = L.rp;
+    const float4* p = reinterpret_cast<const float4*>(nodes + L.cur);
+    const float4 w0 = __ldg(p), w1 = __ldg(p + 1), w2 = __ldg(p + 2), w3 = __ldg(p + 3), w4 = __ldg(p + 4);
+    L.nvis++;
+    const float org[3] = {w0.x, w0.y, w0.z};
+    const uint32_t ei = __float_as_uint(w0.w);
+    const float sc[3] = {pow2f((int)(ei & 0xFFu) - 127), pow2f((int)((ei >> 8) & 0xFFu) - 127),
+                         pow2f((int)((ei >> 16) & 0xFFu) - 127)};
+    const uint32_t imask = ei >> 24;
+    const uint32_t child_base = __float_as_uint(w1.x), tri_base = __float_as_uint(w1.y);
+    const uint32_t counts = __float_as_uint(w1.z), valid = __float_as_uint(w1.w);
+    const uint32_t q[12] = {__float_as_uint(w2.x), __float_as_uint(w2.y), __float_as_uint(w2.z), __float_as_uint(w2.w),
+                            __float_as_uint(w3.x), __float_as_uint(w3.y), __float_as_uint(w3.z), __float_as_uint(w3.w),
+                            __float_as_uint(w4.x), __float_as_uint(w4.y), __float_as_uint(w4.z), __float_as_uint(w4.w)};
+    uint32_t qa[6], qb[6];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const bool ng = SIGNED && rp.inv[a] < 0.0f;
+#pragma unroll
+        for (int w = 0; w < 2; ++w) {
+            const uint32_t lo = q[a * 2 + w], hi = q[6 + a * 2 + w];
+            qa[a * 2 + w] = ng ? hi : lo;
+            qb[a * 2 + w] = ng ? lo : hi;
+        }
+    }
+    const float lim = L.best_t * kRobust;
+    // nearest hit child (kept in registers) and the others pushed onto the
+    // stack, sorted far (bottom) to near (top) within this node's pushes
+    uint32_t near_e = kNoHit;
+    float near_t = 0.0f;
+    const int seg = L.sp;
+    uint32_t inner_rank = 0, tri_off = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const uint32_t cnt = (counts >> (4 * k)) & 0xFu;
+        const bool is_inner = (imask >> k) & 1u;
+        if ((valid >> k) & 1u) {
+            const int w = k >> 2;
+            const uint32_t j = (uint32_t)(k & 3);
+            float ta[3], tb[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const float ba = fmaf(qbyte(qa[a * 2 + w], j), sc[a], org[a]);
+                const float bb = fmaf(qbyte(qb[a * 2 + w], j), sc[a], org[a]);
+                ta[a] = (ba - rp.o[a]) * rp.inv[a];
+                tb[a] = (bb - rp.o[a]) * rp.inv[a];
+            }
+            L.tests++;
+            float n, f;
+            if (SIGNED) {
+                n = fmaxf(fmaxf(fmaxf(ta[0], ta[1]), ta[2]), rp.tmin);
+                f = fminf(fminf(tb[0], tb[1]), tb[2]);
+            } else {
+                n = fmaxf(fmaxf(fmaxf(fminf(ta[0], tb[0]), fminf(ta[1], tb[1])), fminf(ta[2], tb[2])), rp.tmin);
+                f = fminf(fminf(fmaxf(ta[0], tb[0]), fmaxf(ta[1], tb[1])), fmaxf(ta[2], tb[2]));
+            }
+            f = f * kRobust;
+            if (n <= f && n <= lim) {
+                uint32_t ent = is_inner ? (child_base + inner_rank) : (0x80000000u | (cnt << 27) | (tri_base + tri_off));
+                float et = n;
+                if (near_e == kNoHit) {
+                    near_e = ent;
+                    near_t = n;
+                } else {
+                    // Children are visited in ascending (entry distance, slot)
+                    // order.  The pushed entries keep that order from the top;
+                    // a new child has the largest slot so far and goes below
+                    // entries of equal distance, a displaced nearest has the
+                    // smallest and goes above them.
+                    bool displaced = false;
+                    if (n < near_t) {
+                        const uint32_t te = near_e; const float tt = near_t;
+                        near_e = ent; near_t = n;
+                        ent = te; et = tt;
+                        displaced = true;
+                    }
+                    if (L.sp >= kStack8) {
+                        L.overflow = true;
+                    } else {
+                        int b = L.sp - 1;
+                        while (b >= seg && (st_t[b] < et || (!displaced && st_t[b] == et))) {
+                            st_e[b + 1] = st_e[b]; st_t[b + 1] = st_t[b]; --b;
+                        }
+                        st_e[b + 1] = ent;
+                        st_t[b + 1] = et;
+                        L.sp++;
+                    }
+                }
+            }
+        }
+        inner_rank += is_inner;
+        tri_off += cnt;
+    }
+    if (L.overflow) { L.cur = kNoHit; return; }
+    // the next node: the nearest child, else the stack (leaves tested on the way)
+    uint32_t e = near_e;
+    for (;;) {
+        if (e == kNoHit) {
+            if (L.sp == 0) { L.cur = kNoHit; return; }
+            --L.sp;
+            if (st_t[L.sp] > L.best_t * kRobust) continue;
+            e = st_e[L.sp];
+        }
+        if (e & 0x80000000u) {
+            if (leaf8<ANY>(L, t8, e)) { L.cur = kNoHit; return; }
+            e = kNoHit;
+            continue;
+        }
+        L.cur = e;
+        return;
+    }
+}
+
+// Camera rays, tiles: a warp takes one 8x4 pixel tile, each lane runs its
+// ray to the end (trace8), then the warp takes the next tile.
 template <int MODE>
-__global__ void __launch_bounds__(128) k_trace8(const sqk::Trace8Args a, uint32_t batches)
+__global__ void __launch_bounds__(128) k_trace8_tiles(const sqk::Trace8Args a, uint32_t batches)
 {
     const uint32_t lane = threadIdx.x & 31u;
     const bool camera = a.ray_kind != SQ_RAYS_EXPLICIT;
@@ -684,29 +862,135 @@ __global__ void __launch_bounds__(128) k_trace8(const sqk::Trace8Args a, uint32_
 }
 
 template <int MODE>
+__global__ void __launch_bounds__(128) k_trace8_refill(const sqk::Trace8Args a, uint32_t total)
+{
+    constexpr bool ANY = MODE == SQ_TRACE_ANYHIT;
+    const uint32_t lane = threadIdx.x & 31u;
+    const bool camera = a.ray_kind != SQ_RAYS_EXPLICIT;
+    const uint32_t tiles_x = (a.width + 7u) >> 3;
+    const Node8* nodes = static_cast<const Node8*>(a.nodes);
+    uint32_t st_e[kStack8];
+    float st_t[kStack8];
+    Lane8 L;
+    L.cur = kNoHit;
+    bool has = false, exhausted = false;
+    uint32_t rid = 0;
+    unsigned long long s_bt = 0, s_tt = 0, s_by = 0, s_nv = 0;
+    for (;;) {
+        // refill: every lane without a ray takes the next one
+        const uint32_t need = __ballot_sync(0xFFFFFFFFu, !has && !exhausted);
+        if (need) {
+            const uint32_t leader = __ffs(need) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(a.work, __popc(need));
+            base = __shfl_sync(0xFFFFFFFFu, base, leader);
+            if (!has && !exhausted) {
+                const uint32_t g = base + __popc(need & ((1u << lane) - 1u));
+                if (g >= total) {
+                    exhausted = true;
+                } else {
+                    Ray8 r;
+                    bool ok;
+                    if (camera) {
+                        // ray g: pixel (g mod 32) of 8x4 tile g / 32, tiles in row order
+                        const uint32_t b = g >> 5, l = g & 31u;
+                        const uint32_t x = (b % tiles_x) * 8u + (l & 7u);
+                        const uint32_t y = (b / tiles_x) * 4u + (l >> 3);
+                        ok = x < a.width && y < a.height;
+                        rid = y * a.width + x;
+                        if (ok) camera_ray8(a.ray_kind, x, y, a.width, a.height, a.cam, r);
+                    } else {
+                        rid = g;
+                        ok = true;
+                        const float4* p = reinterpret_cast<const float4*>(a.rays) + 2ull * rid;
+                        const float4 x0 = __ldg(p), x1 = __ldg(p + 1);
+                        r.o[0] = x0.x; r.o[1] = x0.y; r.o[2] = x0.z; r.tmin = x0.w;
+                        r.d[0] = x1.x; r.d[1] = x1.y; r.d[2] = x1.z; r.tmax = x1.w;
+                    }
+                    if (ok) {
+                        lane_start(L, r, 0u);
+                        has = true;
+                    }
+                }
+            }
+        }
+        const uint32_t busy = __ballot_sync(0xFFFFFFFFu, has);
+        if (!busy) {
+            if (__all_sync(0xFFFFFFFFu, exhausted)) break;
+            continue;
+        }
+        if (has) {
+            // slab form: sign-selected planes when no lane's ray can produce NaN
+            if (__all_sync(busy, no_nan_slabs(L.rp))) visit8<ANY, true>(L, nodes, a.tris8, st_e, st_t);
+            else visit8<ANY, false>(L, nodes, a.tris8, st_e, st_t);
+            if (L.cur == kNoHit) {
+                has = false;
+                if (L.overflow) raise_error(a.err, SQ_DEVERR_STACK_OVERFLOW);
+                if (a.stats) {
+                    s_bt += L.tests;
+                    s_tt += L.ttests;
+                    s_nv += L.nvis;
+                    s_by += (camera ? 0u : 32u) + (a.hits ? 12u : 0u) + (a.heat ? 3u : 0u) + 80ull * L.nvis +
+                            48ull * L.ttests;
+                }
+                if (a.hits) {
+                    uint32_t* h = reinterpret_cast<uint32_t*>(a.hits) + 3ull * rid;
+                    h[0] = L.best;
+                    h[1] = __float_as_uint(L.best == kNoHit ? 0.0f : L.best_t);
+                    h[2] = L.tests;
+                }
+                if (a.heat) {
+                    float x = (float)L.tests / 200.0f;
+                    x = (x < 1.0f) ? x : 1.0f;
+                    const uint8_t v = (uint8_t)f2u(x * 255.0f);
+                    uint8_t* hp = a.heat + 3ull * rid;
+                    hp[0] = v; hp[1] = v; hp[2] = v;
+                }
+            }
+        }
+    }
+    if (a.stats) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            s_bt += __shfl_xor_sync(0xFFFFFFFFu, s_bt, o);
+            s_tt += __shfl_xor_sync(0xFFFFFFFFu, s_tt, o);
+            s_by += __shfl_xor_sync(0xFFFFFFFFu, s_by, o);
+            s_nv += __shfl_xor_sync(0xFFFFFFFFu, s_nv, o);
+        }
+        if (lane == 0) {
+            atomicAdd(a.stats, s_bt); atomicAdd(a.stats + 1, s_tt); atomicAdd(a.stats + 2, s_by); atomicAdd(a.stats + 3, s_nv);
+        }
+    }
+}
+
+template <int MODE>
 void launch8(const sqk::Trace8Args& a, cudaStream_t s)
 {
     uint32_t batches;
     if (a.ray_kind == SQ_RAYS_EXPLICIT) batches = (a.ray_count + 31u) / 32u;
     else batches = ((a.width + 7u) / 8u) * ((a.height + 3u) / 4u);
     if (batches == 0) return;
-    static int per_sm = 0, sms = 0;
-    if (!per_sm) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace8<MODE>, 128, 0);
-        if (per_sm <= 0) per_sm = 1;
+    static int per_sm[2] = {0, 0}, sms = 0;
+    const int v = a.refill ? 1 : 0;
+    if (!per_sm[v]) {
+        if (v) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[v], k_trace8_refill<MODE>, 128, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[v], k_trace8_tiles<MODE>, 128, 0);
+        if (per_sm[v] <= 0) per_sm[v] = 1;
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = kNumSMs;
     }
-    uint32_t grid = (uint32_t)(per_sm * sms);
+    uint32_t grid = (uint32_t)(per_sm[v] * sms);
     const uint32_t need = (batches + 3u) / 4u;
     if (grid > need) grid = need;
-    k_trace8<MODE><<<grid, 128, 0, s>>>(a, batches);
+    if (v) k_trace8_refill<MODE><<<grid, 128, 0, s>>>(a, a.ray_kind == SQ_RAYS_EXPLICIT ? a.ray_count : batches * 32u);
+    else k_trace8_tiles<MODE><<<grid, 128, 0, s>>>(a, batches);
 }
 
+// Batch, tiles: as k_trace8_tiles over the job table's 32-ray batches.
 template <int MODE>
-__global__ void __launch_bounds__(256) k_trace8_batch(const sqk::BatchTraceArgs a)
+__global__ void __launch_bounds__(256) k_trace8_batch_tiles(const sqk::BatchTraceArgs a)
 {
     const uint32_t lane = threadIdx.x & 31u;
     const Node8* nodes = static_cast<const Node8*>(a.nodes8);
@@ -781,23 +1065,136 @@ __global__ void __launch_bounds__(256) k_trace8_batch(const sqk::BatchTraceArgs 
 }
 
 template <int MODE>
+__global__ void __launch_bounds__(256) k_trace8_batch_refill(const sqk::BatchTraceArgs a)
+{
+    constexpr bool ANY = MODE == SQ_TRACE_ANYHIT;
+    const uint32_t lane = threadIdx.x & 31u;
+    const Node8* nodes = static_cast<const Node8*>(a.nodes8);
+    const uint32_t total = a.total_batches * 32u;
+    uint32_t st_e[kStack8];
+    float st_t[kStack8];
+    Lane8 L;
+    L.cur = kNoHit;
+    bool has = false, exhausted = false, explicit_rays = false;
+    uint32_t out = 0, tri_offset = 0;
+    unsigned long long s_bt = 0, s_tt = 0, s_by = 0, s_nv = 0;
+    for (;;) {
+        const uint32_t need = __ballot_sync(0xFFFFFFFFu, !has && !exhausted);
+        if (need) {
+            const uint32_t leader = __ffs(need) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(a.work, __popc(need));
+            base = __shfl_sync(0xFFFFFFFFu, base, leader);
+            if (!has && !exhausted) {
+                const uint32_t g = base + __popc(need & ((1u << lane) - 1u));
+                if (g >= total) {
+                    exhausted = true;
+                } else {
+                    // ray slot g: lane g mod 32 of the job's 32-ray batch g / 32
+                    const uint32_t b = g >> 5, l = g & 31u;
+                    const uint32_t j = find_job(a.jobs, a.njobs, b);
+                    const sqk::BatchJob& job = a.jobs[j];
+                    const uint32_t lb = b - job.batch_begin;
+                    Ray8 r;
+                    bool ok;
+                    uint32_t rid;
+                    explicit_rays = job.ray_kind == SQ_RAYS_EXPLICIT;
+                    if (!explicit_rays) {
+                        const uint32_t tiles_x = (job.width + 7u) >> 3;
+                        const uint32_t x = (lb % tiles_x) * 8u + (l & 7u);
+                        const uint32_t y = (lb / tiles_x) * 4u + (l >> 3);
+                        ok = x < job.width && y < job.height;
+                        rid = y * job.width + x;
+                        if (ok) camera_ray8(job.ray_kind, x, y, job.width, job.height, job.cam, r);
+                    } else {
+                        rid = lb * 32u + l;
+                        ok = rid < job.ray_count;
+                        if (ok) {
+                            const float4* p = reinterpret_cast<const float4*>(a.rays) + 2ull * (job.ray_offset + rid);
+                            const float4 x0 = __ldg(p), x1 = __ldg(p + 1);
+                            r.o[0] = x0.x; r.o[1] = x0.y; r.o[2] = x0.z; r.tmin = x0.w;
+                            r.d[0] = x1.x; r.d[1] = x1.y; r.d[2] = x1.z; r.tmax = x1.w;
+                        }
+                    }
+                    if (ok) {
+                        out = job.out_offset + rid;
+                        tri_offset = job.tri_offset;
+                        lane_start(L, r, job.root);
+                        has = true;
+                    }
+                }
+            }
+        }
+        const uint32_t busy = __ballot_sync(0xFFFFFFFFu, has);
+        if (!busy) {
+            if (__all_sync(0xFFFFFFFFu, exhausted)) break;
+            continue;
+        }
+        if (has) {
+            if (__all_sync(busy, no_nan_slabs(L.rp))) visit8<ANY, true>(L, nodes, a.tris8, st_e, st_t);
+            else visit8<ANY, false>(L, nodes, a.tris8, st_e, st_t);
+            if (L.cur == kNoHit) {
+                has = false;
+                if (L.overflow) raise_error(a.err, SQ_DEVERR_STACK_OVERFLOW);
+                if (a.stats) {
+                    s_bt += L.tests;
+                    s_tt += L.ttests;
+                    s_nv += L.nvis;
+                    s_by += (explicit_rays ? 32u : 0u) + (a.hits ? 12u : 0u) + (a.heat ? 3u : 0u) + 80ull * L.nvis +
+                            48ull * L.ttests;
+                }
+                const uint32_t id = L.best == kNoHit ? kNoHit : L.best - tri_offset;
+                if (a.hits) {
+                    uint32_t* h = reinterpret_cast<uint32_t*>(a.hits) + 3ull * out;
+                    h[0] = id;
+                    h[1] = __float_as_uint(L.best == kNoHit ? 0.0f : L.best_t);
+                    h[2] = L.tests;
+                }
+                if (a.heat) {
+                    float x = (float)L.tests / 200.0f;
+                    x = (x < 1.0f) ? x : 1.0f;
+                    const uint8_t v = (uint8_t)f2u(x * 255.0f);
+                    uint8_t* hp = a.heat + 3ull * out;
+                    hp[0] = v; hp[1] = v; hp[2] = v;
+                }
+            }
+        }
+    }
+    if (a.stats) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            s_bt += __shfl_xor_sync(0xFFFFFFFFu, s_bt, o);
+            s_tt += __shfl_xor_sync(0xFFFFFFFFu, s_tt, o);
+            s_by += __shfl_xor_sync(0xFFFFFFFFu, s_by, o);
+            s_nv += __shfl_xor_sync(0xFFFFFFFFu, s_nv, o);
+        }
+        if (lane == 0) {
+            atomicAdd(a.stats, s_bt); atomicAdd(a.stats + 1, s_tt); atomicAdd(a.stats + 2, s_by); atomicAdd(a.stats + 3, s_nv);
+        }
+    }
+}
+
+template <int MODE>
 void launch8_batch(const sqk::BatchTraceArgs& a, int block, cudaStream_t s)
 {
     if (a.total_batches == 0) return;
-    static int per_sm[3] = {0, 0, 0}, sms = 0;
+    static int per_sm[2][3] = {{0, 0, 0}, {0, 0, 0}}, sms = 0;
     const int bi = block <= 64 ? 0 : (block <= 128 ? 1 : 2);
-    if (!per_sm[bi]) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[bi], k_trace8_batch<MODE>, block, 0);
-        if (per_sm[bi] <= 0) per_sm[bi] = 1;
+    const int v = a.refill ? 1 : 0;
+    if (!per_sm[v][bi]) {
+        if (v) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[v][bi], k_trace8_batch_refill<MODE>, block, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[v][bi], k_trace8_batch_tiles<MODE>, block, 0);
+        if (per_sm[v][bi] <= 0) per_sm[v][bi] = 1;
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = kNumSMs;
     }
-    uint32_t grid = (uint32_t)(per_sm[bi] * sms);
+    uint32_t grid = (uint32_t)(per_sm[v][bi] * sms);
     const uint32_t need = (a.total_batches + (uint32_t)(block / 32) - 1) / (uint32_t)(block / 32);
     if (grid > need) grid = need;
-    k_trace8_batch<MODE><<<grid, block, 0, s>>>(a);
+    if (v) k_trace8_batch_refill<MODE><<<grid, block, 0, s>>>(a);
+    else k_trace8_batch_tiles<MODE><<<grid, block, 0, s>>>(a);
 }
 
 }  // namespace

@@ -188,6 +188,7 @@ struct Trace8Args {
     uint32_t* work;
     uint32_t* err;
     unsigned long long* stats;
+    uint32_t refill;       // 1: per-lane ray refill; 0: whole 32-ray batches per warp
 };
 uint32_t bvh8_capacity(uint32_t n);
 size_t bvh8_node_bytes(uint32_t n);
@@ -226,6 +227,7 @@ struct BatchTraceArgs {
     uint32_t* work;
     uint32_t* err;
     unsigned long long* stats;
+    uint32_t refill;       // 8-wide kernel: 1 = per-lane ray refill (see sq_bvh8.cu)
 };
 void trace_batch(const BatchTraceArgs& a, int block_threads, cudaStream_t s);
 void trace8_batch(const BatchTraceArgs& a, int block_threads, cudaStream_t s);
