@@ -358,6 +358,7 @@ def main():
     if dist:
         dist.barrier()
     step_ms, build_ms, wide_ms, trace_ms, stats, launches = [], [], [], [], [], 0
+    lbvh_stage = {"codes": [], "sort": [], "topology": []}
     for _ in range(args.steps):
         flush.zero_()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -370,6 +371,8 @@ def main():
         step_ms.append(e0.elapsed_time(e1))
         build_ms.append(tm["build"])
         wide_ms.append(tm["wide"])
+        for k in lbvh_stage:
+            lbvh_stage[k].append(tm[k])
         trace_ms.append(tm["trace"])
         stats.append(st)
         launches += LBVH_KERNELS + bvh.info().wide_levels + 1
@@ -453,7 +456,8 @@ def main():
         "lbvh_mtris_s": n / (lbvh_ms / 1e3) / 1e6,
         "trace_mrays_s": rays_total / (tr_ms / 1e3) / 1e6,
         "stage_ms": {"build_total": b_ms, "lbvh": lbvh_ms, "wide_collapse": statistics.mean(wide_ms),
-                     "trace": tr_ms, "step": ms_per_step},
+                     "trace": tr_ms, "step": ms_per_step,
+                     "lbvh_stages": {k: statistics.mean(v) for k, v in lbvh_stage.items()}},
         "per_ray": {"box_tests": statistics.mean(s["box_tests"] for s in stats) / rays_total,
                     "tri_tests": statistics.mean(s["tri_tests"] for s in stats) / rays_total,
                     "wide_nodes": statistics.mean(s["nodes"] for s in stats) / rays_total,

@@ -217,11 +217,10 @@ __global__ void __launch_bounds__(256) k_seg_climb(const uint32_t* __restrict__ 
         float4* mine = info + 2ull * (2ull * p + (left ? 0u : 1u));
         mine[0] = make_float4(box.mn[0], box.mn[1], box.mn[2], __uint_as_float(left ? l : r));
         mine[1] = make_float4(box.mx[0], box.mx[1], box.mx[2], __uint_as_float(split));
-        __threadfence();
-        const uint32_t old = atomicAdd(flags + p, 1u);
+        // release my record, acquire the sibling's (the first arrival stops)
+        const uint32_t old = atomic_add_acq_rel_u32(flags + p, 1u);
         if (old == 0) return;
         if (old != 1) { raise_error(err, SQ_DEVERR_TOPOLOGY); return; }
-        __threadfence();
         const float4* sib = info + 2ull * (2ull * p + (left ? 1u : 0u));
         const float4 s0 = __ldcg(sib), s1 = __ldcg(sib + 1);
         Box sbx;

@@ -109,6 +109,29 @@ __device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v)
 {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+// Relaxed (but coherent, untorn) GPU-scope load and store of a word that
+// carries all its information itself, e.g. a look-back flag and count packed
+// together: nothing else is published with it, so no ordering is needed and
+// independent loads may be in flight together.
+__device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p)
+{
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed_u32(uint32_t* p, uint32_t v)
+{
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+// fetch-and-add with acquire-release semantics at GPU scope: the caller's
+// earlier writes are visible to whoever later acquires this word, and the
+// caller sees the writes released before earlier additions to it.
+__device__ __forceinline__ uint32_t atomic_add_acq_rel_u32(uint32_t* p, uint32_t v)
+{
+    uint32_t old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
 __device__ __forceinline__ uint32_t ld_volatile_u32(const uint32_t* p)
 {
     uint32_t v;

@@ -30,6 +30,7 @@ constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagInc = 2u << 30;
 constexpr uint32_t kCountMask = (1u << 30) - 1u;
 constexpr uint32_t kSpinLimit = 1u << 22;
+constexpr int kWindow = 8;  // look-back words loaded per round
 
 template <int RADIX>
 __device__ __forceinline__ void block_exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t* s_tmp)
@@ -107,13 +108,14 @@ __global__ void __launch_bounds__(kBlock) k_onesweep(const uint32_t* __restrict_
     const uint32_t tile = s_tile;
     const uint32_t base = tile * (uint32_t)kTile;
 
-    uint32_t k[kItems], v[kItems], rk[kItems];
+    // keys stay in registers through the ranking; values are read only in
+    // the scatter (fewer registers: four blocks fit on an SM)
+    uint32_t k[kItems], rk[kItems];
     const uint32_t wbase = base + (uint32_t)warp * (kItems * 32);
 #pragma unroll
     for (int it = 0; it < kItems; ++it) {
         const uint32_t idx = wbase + it * 32 + lane;
-        if (idx < n) { k[it] = kin[idx]; v[it] = vin[idx]; }
-        else { k[it] = 0xFFFFFFFFu; v[it] = 0; }
+        k[it] = idx < n ? kin[idx] : 0xFFFFFFFFu;
     }
     const uint32_t lt = (1u << lane) - 1u;
     uint32_t* wh = s_whist + warp * RADIX;
@@ -125,13 +127,11 @@ __global__ void __launch_bounds__(kBlock) k_onesweep(const uint32_t* __restrict_
         const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
         const int leader = __ffs(peers) - 1;
         uint32_t old = 0;
-        if (lane == leader && valid) {
-            old = wh[d];
-            wh[d] = old + __popc(peers);
-        }
+        // a shared-memory atomic (not a load and a store) so that the
+        // iterations do not wait on one another through wh[]
+        if (lane == leader && valid) old = atomicAdd(wh + d, __popc(peers));
         old = __shfl_sync(0xFFFFFFFFu, old, leader);
         rk[it] = old + __popc(peers & lt);
-        __syncwarp();
     }
     __syncthreads();
     // exclusive offsets across warps per digit; block counts
@@ -144,29 +144,45 @@ __global__ void __launch_bounds__(kBlock) k_onesweep(const uint32_t* __restrict_
             run += c;
         }
         s_bcount[d] = run;
-        st_release_u32(lookback + (size_t)tile * RADIX + d, (tile == 0 ? kFlagInc : kFlagAgg) | run);
+        st_relaxed_u32(lookback + (size_t)tile * RADIX + d, (tile == 0 ? kFlagInc : kFlagAgg) | run);
     }
     __syncthreads();
     block_exclusive_scan<RADIX>(hist, s_gbase, s_tmp);
     block_exclusive_scan<RADIX>(s_bcount, s_lexcl, s_tmp);
-    // decoupled look-back, one digit per thread (or several)
+    // decoupled look-back, one digit per thread (or several).  The words of
+    // kWindow predecessors are loaded at once (independent relaxed loads, one
+    // memory latency: each word carries its flag and count together, so no
+    // ordering with other data is needed) and consumed in order until an
+    // inclusive prefix is found; an unpublished word ends the window and is
+    // read again.
     for (int d = tid; d < RADIX; d += kBlock) {
         uint32_t excl = 0;
         if (tile > 0) {
             int32_t j = (int32_t)tile - 1;
             uint32_t spins = 0;
-            for (;;) {
-                const uint32_t w = ld_acquire_u32(lookback + (size_t)j * RADIX + d);
-                const uint32_t f = w & ~kCountMask;
-                if (f == 0) {
-                    if (++spins > kSpinLimit) { raise_error(err, SQ_DEVERR_LOOKBACK_TIMEOUT); break; }
-                    continue;
+            bool done = false;
+            while (!done) {
+                uint32_t w[kWindow];
+#pragma unroll
+                for (int q = 0; q < kWindow; ++q)
+                    w[q] = (j - q >= 0) ? ld_relaxed_u32(lookback + (size_t)(j - q) * RADIX + d) : kFlagInc;
+                int used = 0;
+#pragma unroll
+                for (int q = 0; q < kWindow; ++q) {
+                    if (done || used != q) continue;
+                    const uint32_t f = w[q] & ~kCountMask;
+                    if (f == 0) continue;  // not yet published: stop this window here
+                    excl += w[q] & kCountMask;
+                    used = q + 1;
+                    if (f == kFlagInc || j - q == 0) done = true;
                 }
-                excl += w & kCountMask;
-                if (f == kFlagInc || j == 0) break;
-                --j;
+                j -= used;
+                if (!done && used == 0 && ++spins > kSpinLimit) {
+                    raise_error(err, SQ_DEVERR_LOOKBACK_TIMEOUT);
+                    break;
+                }
             }
-            st_release_u32(lookback + (size_t)tile * RADIX + d, kFlagInc | ((excl + s_bcount[d]) & kCountMask));
+            st_relaxed_u32(lookback + (size_t)tile * RADIX + d, kFlagInc | ((excl + s_bcount[d]) & kCountMask));
         }
         s_gbase[d] += excl;
     }
@@ -179,7 +195,7 @@ __global__ void __launch_bounds__(kBlock) k_onesweep(const uint32_t* __restrict_
             const uint32_t d = (k[it] >> shift) & MASK;
             const uint32_t pos = s_lexcl[d] + wh[d] + rk[it];
             s_keys[pos] = k[it];
-            s_vals[pos] = v[it];
+            s_vals[pos] = vin[idx];
         }
     }
     __syncthreads();
