@@ -59,12 +59,6 @@ __device__ __forceinline__ float node_sa(const Node& r)
     return lx * ly + lx * lz + ly * lz;
 }
 
-struct Entry {
-    uint32_t rec;  // binary record index
-    float sa;
-    uint32_t kind; // 0: binary inner record, 1: leaf cluster, 2: single-triangle leaf
-    uint32_t cnt;  // children of the record (2, cluster size, or 1)
-};
 
 // Exponent of the quantisation step so that origin + 255 * 2^e >= hi.
 __device__ int quant_exp(float lo, float hi)
@@ -82,10 +76,13 @@ __device__ int quant_exp(float lo, float hi)
     return e;
 }
 
+// (v - origin) / 2^e is computed as (v - origin) * 2^-e: both are the
+// correctly rounded value of the same real number (2^-e is exact for every
+// exponent quant_exp returns), and the multiply is far cheaper.
 __device__ __forceinline__ uint8_t quant_lo(float v, float origin, int e)
 {
     const float s = pow2f(e);
-    float q = floorf((v - origin) / s);
+    float q = floorf((v - origin) * ldexpf(1.0f, -e));
     int qi = q < 0.0f ? 0 : (q > 255.0f ? 255 : (int)q);
     while (qi > 0 && fmaf((float)qi, s, origin) > v) --qi;
     return (uint8_t)qi;
@@ -94,129 +91,194 @@ __device__ __forceinline__ uint8_t quant_lo(float v, float origin, int e)
 __device__ __forceinline__ uint8_t quant_hi(float v, float origin, int e)
 {
     const float s = pow2f(e);
-    float q = ceilf((v - origin) / s);
+    float q = ceilf((v - origin) * ldexpf(1.0f, -e));
     int qi = q < 0.0f ? 0 : (q > 255.0f ? 255 : (int)q);
     while (qi < 255 && fmaf((float)qi, s, origin) < v) ++qi;
     return (uint8_t)qi;
 }
 
-// Kind of a record in the range-tree layout: a binary inner record (children
-// outside the leaf region), a leaf cluster (children in the leaf region) or a
-// single-triangle leaf record.
-__device__ __forceinline__ Entry make_entry(const Node* __restrict__ rec, uint32_t i, uint32_t leaf0)
-{
-    const Node r = rec[i];
-    Entry e;
-    e.rec = i;
-    e.sa = node_sa(r);
-    e.cnt = node_count(r.count_flags);
-    if (node_is_leaf(r.count_flags)) e.kind = 2;
-    else e.kind = (r.child < leaf0 && e.cnt > 0) ? 0u : 1u;
-    return e;
-}
 
-// Build the 8-wide node `node_i` from binary record `rec_i`; its inner
-// children become nodes [child_base, child_base + n) where child_base is
-// returned by reserve(n).  Returns false on an error.
+// Build the 8-wide node `node_i` from binary record `rec_i` with one warp:
+// lane k < 8 holds candidate child slot k (its binary record in registers),
+// so the records a step opens are loaded in parallel and the six dequantised
+// planes of each slot are computed by the slot's own lane.  The decisions are
+// those of a sequential scan over the slots: open the first child of largest
+// surface area that still fits, until none does.  Inner children become
+// nodes [child_base, child_base + n) where child_base comes from reserve(n)
+// (called by lane 0); publish(node, record) is called by the child's lane.
 template <class Reserve, class Publish>
-__device__ bool collapse_node(const Node* __restrict__ rec, uint32_t leaf0, const float* __restrict__ tris,
-                              uint32_t rec_i, uint32_t node_i, Node8* __restrict__ nodes8, float4* __restrict__ tris8,
-                              uint32_t* __restrict__ tri_counter, uint32_t* err, Reserve reserve, Publish publish)
+__device__ void collapse_node_warp(const Node* __restrict__ rec, uint32_t leaf0, const float* __restrict__ tris,
+                                   uint32_t rec_i, uint32_t node_i, Node8* __restrict__ nodes8,
+                                   float4* __restrict__ tris8, uint32_t* __restrict__ tri_counter, uint32_t* err,
+                                   Reserve reserve, Publish publish)
 {
+    constexpr uint32_t FULL = 0xFFFFFFFFu;
+    const int lane = (int)(threadIdx.x & 31u);
     const Node self = rec[rec_i];
-    Entry ch[8];
-    int nc = 0;
     const uint32_t c0 = self.child, cn = node_count(self.count_flags);
-    if (cn > 8) { raise_error(err, SQ_DEVERR_NODE_COUNT); return false; }
-    // the start set: a binary record's two children, or a cluster's leaves
-    for (uint32_t k = 0; k < cn; ++k) ch[nc++] = make_entry(rec, c0 + k, leaf0);
-    // Open the child of largest area until no child can be opened within 8
-    // slots: a binary record opens into its two children, a leaf cluster into
-    // its single-triangle leaves (so each triangle keeps its own box).
+    if (cn > 8) {
+        if (lane == 0) raise_error(err, SQ_DEVERR_NODE_COUNT);
+        return;
+    }
+    // slot state of this lane
+    Node e_node;
+    uint32_t e_rec = 0, e_kind = 0, e_cnt = 0;
+    float e_sa = 0.0f;
+    auto load_entry = [&](uint32_t i) {
+        e_node = rec[i];
+        e_rec = i;
+        e_sa = node_sa(e_node);
+        e_cnt = node_count(e_node.count_flags);
+        if (node_is_leaf(e_node.count_flags)) e_kind = 2;
+        else e_kind = (e_node.child < leaf0 && e_cnt > 0) ? 0u : 1u;
+    };
+    if (lane < (int)cn) load_entry(c0 + (uint32_t)lane);
+    // the start set is a binary record's two children or a cluster's leaves;
+    // open the child of largest area (a binary record into its two children,
+    // a leaf cluster into its single-triangle leaves) while it fits in 8 slots
+    int nc = (int)cn;
     for (;;) {
+        const bool can = lane < nc && (e_kind == 0 ? (nc + 1 <= 8) : (e_kind == 1 && nc + (int)e_cnt - 1 <= 8));
+        const uint32_t canm = __ballot_sync(FULL, can);
+        if (!canm) break;
         int best = -1;
-        for (int k = 0; k < nc; ++k) {
-            const bool can = ch[k].kind == 0 ? (nc + 1 <= 8) : (ch[k].kind == 1 && nc + (int)ch[k].cnt - 1 <= 8);
-            if (can && (best < 0 || ch[k].sa > ch[best].sa)) best = k;
+        float bsa = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const float sk = __shfl_sync(FULL, e_sa, k);
+            if (((canm >> k) & 1u) && (best < 0 || sk > bsa)) { best = k; bsa = sk; }
         }
-        if (best < 0) break;
-        const Node r = rec[ch[best].rec];
-        const uint32_t m = ch[best].kind == 0 ? 2u : ch[best].cnt;
-        if (m == 0) { ch[best] = ch[--nc]; continue; }
-        ch[best] = make_entry(rec, r.child, leaf0);
-        for (uint32_t j = 1; j < m; ++j) ch[nc++] = make_entry(rec, r.child + j, leaf0);
-    }
-    // A cluster of 2..8 triangles that did not fit becomes a wide child node
-    // of its own (its triangles one per slot), so every triangle keeps its
-    // own box; larger clusters stay leaf children of up to 15 triangles.
-    for (int k = 0; k < nc; ++k)
-        if (ch[k].kind == 1 && ch[k].cnt >= 2 && ch[k].cnt <= 8) ch[k].kind = 0;
-    // count inner children and leaf triangles (children with an empty box,
-    // i.e. empty grid cells and subtrees of them, take no slot)
-    uint32_t n_inner = 0, n_tris = 0;
-    uint32_t cnt[8];
-    bool ok[8];
-    for (int k = 0; k < nc; ++k) {
-        const Node r = rec[ch[k].rec];
-        ok[k] = r.mnx <= r.mxx && r.mny <= r.mxy && r.mnz <= r.mxz;
-        cnt[k] = 0;
-        if (!ok[k]) continue;
-        if (ch[k].kind == 0) n_inner++;
-        else {
-            cnt[k] = node_count(r.count_flags);
-            if (cnt[k] > 15u) { raise_error(err, SQ_DEVERR_NODE_COUNT); return false; }
-            n_tris += cnt[k];
+        const uint32_t bkind = __shfl_sync(FULL, e_kind, best), bcnt = __shfl_sync(FULL, e_cnt, best);
+        const uint32_t bchild = __shfl_sync(FULL, e_node.child, best);
+        const uint32_t m = bkind == 0 ? 2u : bcnt;
+        if (m == 0) {
+            // drop the empty cluster: the last slot moves into its place
+            --nc;
+            Node t;
+            t.mnx = __shfl_sync(FULL, e_node.mnx, nc); t.mny = __shfl_sync(FULL, e_node.mny, nc);
+            t.mnz = __shfl_sync(FULL, e_node.mnz, nc); t.count_flags = __shfl_sync(FULL, e_node.count_flags, nc);
+            t.mxx = __shfl_sync(FULL, e_node.mxx, nc); t.mxy = __shfl_sync(FULL, e_node.mxy, nc);
+            t.mxz = __shfl_sync(FULL, e_node.mxz, nc); t.child = __shfl_sync(FULL, e_node.child, nc);
+            const uint32_t trec = __shfl_sync(FULL, e_rec, nc), tkind = __shfl_sync(FULL, e_kind, nc);
+            const uint32_t tcnt = __shfl_sync(FULL, e_cnt, nc);
+            const float tsa = __shfl_sync(FULL, e_sa, nc);
+            if (lane == best) { e_node = t; e_rec = trec; e_kind = tkind; e_cnt = tcnt; e_sa = tsa; }
+            continue;
         }
+        if (lane == best) load_entry(bchild);
+        else if (lane >= nc && lane < nc + (int)m - 1) load_entry(bchild + 1u + (uint32_t)(lane - nc));
+        nc += (int)m - 1;
     }
-    const uint32_t child_base = n_inner ? reserve(n_inner) : 0u;
-    const uint32_t tri_base = n_tris ? atomicAdd(tri_counter, n_tris) : 0u;
+    // a cluster of 2..8 triangles that did not fit becomes a wide child node
+    // of its own (its triangles one per slot), so every triangle keeps its own
+    // box; larger clusters stay leaf children of up to 15 triangles
+    if (lane < nc && e_kind == 1 && e_cnt >= 2 && e_cnt <= 8) e_kind = 0;
+    // children with an empty box (empty grid cells and subtrees of them) take
+    // no slot
+    const bool ok = lane < nc && e_node.mnx <= e_node.mxx && e_node.mny <= e_node.mxy && e_node.mnz <= e_node.mxz;
+    const bool inner = ok && e_kind == 0;
+    const bool leafc = ok && e_kind != 0;
+    if (__any_sync(FULL, leafc && e_cnt > 15u)) {
+        if (lane == 0) raise_error(err, SQ_DEVERR_NODE_COUNT);
+        return;
+    }
+    const uint32_t cntk = leafc ? e_cnt : 0u;
+    const uint32_t imask = __ballot_sync(FULL, inner) & 0xFFu;
+    const uint32_t valid = __ballot_sync(FULL, ok) & 0xFFu;
+    const uint32_t leafrec = __ballot_sync(FULL, lane < nc && node_is_leaf(e_node.count_flags)) & 0xFFu;
+    uint32_t incl = cntk;
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const uint32_t n_tris = __shfl_sync(FULL, incl, 7);
+    const uint32_t tri_off = incl - cntk;
+    const uint32_t n_inner = __popc(imask);
+    uint32_t child_base = 0, tri_base = 0;
+    if (lane == 0) {
+        child_base = n_inner ? reserve(n_inner) : 0u;
+        tri_base = n_tris ? atomicAdd(tri_counter, n_tris) : 0u;
+    }
+    child_base = __shfl_sync(FULL, child_base, 0);
+    tri_base = __shfl_sync(FULL, tri_base, 0);
+    // quantised child planes, one slot per lane
     const float lo[3] = {self.mnx, self.mny, self.mnz}, hi[3] = {self.mxx, self.mxy, self.mxz};
-    Node8 nd;
-    nd.ox = lo[0]; nd.oy = lo[1]; nd.oz = lo[2];
     int e[3];
+#pragma unroll
     for (int a = 0; a < 3; ++a) e[a] = quant_exp(lo[a], hi[a]);
-    uint32_t imask = 0, counts = 0, valid = 0;
-    uint32_t inner_rank = 0, tri_off = 0;
-    for (int k = 0; k < 8; ++k)
-        for (int a = 0; a < 3; ++a) { nd.qlo[a][k] = 255; nd.qhi[a][k] = 0; }
-    for (int k = 0; k < nc; ++k) {
-        if (!ok[k]) continue;
-        const Node r = rec[ch[k].rec];
-        const float cl[3] = {r.mnx, r.mny, r.mnz}, chh[3] = {r.mxx, r.mxy, r.mxz};
-        valid |= 1u << k;
+    uint32_t ql[3] = {255u, 255u, 255u}, qh[3] = {0u, 0u, 0u};
+    if (ok) {
+        const float cl[3] = {e_node.mnx, e_node.mny, e_node.mnz}, ch[3] = {e_node.mxx, e_node.mxy, e_node.mxz};
+#pragma unroll
         for (int a = 0; a < 3; ++a) {
-            nd.qlo[a][k] = quant_lo(cl[a], lo[a], e[a]);
-            nd.qhi[a][k] = quant_hi(chh[a], lo[a], e[a]);
-        }
-        if (ch[k].kind == 0) {
-            imask |= 1u << k;
-            publish(child_base + inner_rank, ch[k].rec);
-            inner_rank++;
-        } else {
-            counts |= cnt[k] << (4 * k);
-            for (uint32_t j = 0; j < cnt[k]; ++j) {
-                // a leaf record is its own triangle; a cluster's are its leaves
-                const uint32_t id = node_is_leaf(r.count_flags) ? r.child + j : rec[r.child + j].child;
-                float t[9];
-                load_tri(tris, id, t);
-                float4* d = tris8 + 3ull * (tri_base + tri_off + j);
-                d[0] = make_float4(t[0], t[1], t[2], __uint_as_float(id));
-                d[1] = make_float4(t[3], t[4], t[5], 0.0f);
-                d[2] = make_float4(t[6], t[7], t[8], 0.0f);
-            }
-            tri_off += cnt[k];
+            ql[a] = quant_lo(cl[a], lo[a], e[a]);
+            qh[a] = quant_hi(ch[a], lo[a], e[a]);
         }
     }
-    nd.exps_imask = (uint32_t)(e[0] + 127) | ((uint32_t)(e[1] + 127) << 8) | ((uint32_t)(e[2] + 127) << 16) | (imask << 24);
-    nd.child_base = child_base;
-    nd.tri_base = tri_base;
-    nd.counts = counts;
-    nd.valid = valid;
-    nodes8[node_i] = nd;
-    return true;
+    // node words: qlo x (slots 0-3, 4-7), qlo y, qlo z, qhi x, qhi y, qhi z
+    uint32_t qw[12];
+    const bool slot = lane < 8;
+    const uint32_t sh = 8u * (uint32_t)(lane & 3);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+#pragma unroll
+        for (int w = 0; w < 2; ++w) {
+            const bool mine = slot && (lane >> 2) == w;
+            qw[a * 2 + w] = __reduce_or_sync(FULL, mine ? ql[a] << sh : 0u);
+            qw[6 + a * 2 + w] = __reduce_or_sync(FULL, mine ? qh[a] << sh : 0u);
+        }
+    }
+    const uint32_t counts = __reduce_or_sync(FULL, slot ? cntk << (4u * (uint32_t)lane) : 0u);
+    if (inner) publish(child_base + __popc(imask & ((1u << lane) - 1u)), e_rec);
+    // leaf triangles, spread over the warp: triangle t of the node belongs to
+    // the leaf slot whose [tri_off, tri_off + cnt) holds it
+    uint32_t off_k[8], cnt_k[8], child_k[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        off_k[k] = __shfl_sync(FULL, tri_off, k);
+        cnt_k[k] = __shfl_sync(FULL, cntk, k);
+        child_k[k] = __shfl_sync(FULL, e_node.child, k);
+    }
+    for (uint32_t t = (uint32_t)lane; t < n_tris; t += 32u) {
+        int k = 0;
+#pragma unroll
+        for (int q = 1; q < 8; ++q)
+            if (cnt_k[q] && off_k[q] <= t) k = q;
+        uint32_t kk_child = child_k[0], kk_off = off_k[0];
+#pragma unroll
+        for (int q = 1; q < 8; ++q)
+            if (q == k) { kk_child = child_k[q]; kk_off = off_k[q]; }
+        const uint32_t j = t - kk_off;
+        // a leaf record is its own triangle; a cluster's are its leaves
+        const uint32_t id = ((leafrec >> k) & 1u) ? kk_child + j : rec[kk_child + j].child;
+        float tv[9];
+        load_tri(tris, id, tv);
+        float4* d = tris8 + 3ull * (tri_base + t);
+        d[0] = make_float4(tv[0], tv[1], tv[2], __uint_as_float(id));
+        d[1] = make_float4(tv[3], tv[4], tv[5], 0.0f);
+        d[2] = make_float4(tv[6], tv[7], tv[8], 0.0f);
+    }
+    // the node: five 16-byte words, one per lane
+    if (lane < 5) {
+        float4 w;
+        if (lane == 0) {
+            const uint32_t ei = (uint32_t)(e[0] + 127) | ((uint32_t)(e[1] + 127) << 8) |
+                                ((uint32_t)(e[2] + 127) << 16) | (imask << 24);
+            w = make_float4(self.mnx, self.mny, self.mnz, __uint_as_float(ei));
+        } else if (lane == 1) {
+            w = make_float4(__uint_as_float(child_base), __uint_as_float(tri_base), __uint_as_float(counts),
+                            __uint_as_float(valid));
+        } else {
+            const int b = (lane - 2) * 4;
+            w = make_float4(__uint_as_float(qw[b]), __uint_as_float(qw[b + 1]), __uint_as_float(qw[b + 2]),
+                            __uint_as_float(qw[b + 3]));
+        }
+        reinterpret_cast<float4*>(nodes8 + node_i)[lane] = w;
+    }
 }
 
-// One level of the collapse: thread i builds node task_node[i] from binary
+// One level of the collapse: warp i builds node task_node[i] from binary
 // record tasks[i]; inner children are allocated contiguously from the node
 // counter and appended to the next level's task list.
 __global__ void __launch_bounds__(128) k_collapse_level(const Node* __restrict__ rec, uint32_t leaf0,
@@ -226,8 +288,8 @@ __global__ void __launch_bounds__(128) k_collapse_level(const Node* __restrict__
                                                         uint32_t* __restrict__ counters, uint32_t* __restrict__ next_tasks,
                                                         uint32_t* __restrict__ next_node, uint32_t capacity, uint32_t* err)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ntasks) return;
+    const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= ntasks) return;  // whole warps
     auto reserve = [&](uint32_t k) -> uint32_t {
         const uint32_t b0 = atomicAdd(counters + 0, k);
         if ((unsigned long long)b0 + k > capacity) { raise_error(err, SQ_DEVERR_SAH_QUEUE); return 0u; }
@@ -239,7 +301,7 @@ __global__ void __launch_bounds__(128) k_collapse_level(const Node* __restrict__
         next_tasks[j] = record;
         next_node[j] = node;
     };
-    collapse_node(rec, leaf0, tris, tasks[i], task_node[i], nodes8, tris8, counters + 1, err, reserve, publish);
+    collapse_node_warp(rec, leaf0, tris, tasks[i], task_node[i], nodes8, tris8, counters + 1, err, reserve, publish);
 }
 
 // Collapse without host synchronisation (so it can be captured in a CUDA
@@ -265,7 +327,8 @@ __global__ void __launch_bounds__(128) k_collapse_fixed(const Node* __restrict__
         return;
     }
     uint32_t* next_count = counts + level + 1;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < ntasks; i += gridDim.x * blockDim.x) {
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < ntasks; i += warps) {
         auto reserve = [&](uint32_t k) -> uint32_t {
             const uint32_t b0 = atomicAdd(node_counter, k);
             if ((unsigned long long)b0 + k > capacity) { raise_error(err, SQ_DEVERR_SAH_QUEUE); return 0u; }
@@ -277,7 +340,8 @@ __global__ void __launch_bounds__(128) k_collapse_fixed(const Node* __restrict__
             next_tasks[j] = record;
             next_node[j] = node;
         };
-        collapse_node(rec, leaf0, tris, tasks[i], task_node[i], nodes8, tris8, tri_counter, err, reserve, publish);
+        collapse_node_warp(rec, leaf0, tris, tasks[i], task_node[i], nodes8, tris8, tri_counter, err, reserve,
+                           publish);
     }
 }
 
@@ -1277,7 +1341,7 @@ int build_bvh8(const Node* rec, uint32_t root, uint32_t leaf0, const float* tris
     while (ntasks) {
         ++levels;
         if ((e = cudaMemsetAsync(counters + 2, 0, 4, s)) != cudaSuccess) return (int)e;
-        k_collapse_level<<<(ntasks + 127) / 128, 128, 0, s>>>(rec, leaf0, tris, ta, na, ntasks,
+        k_collapse_level<<<(ntasks + 3) / 4, 128, 0, s>>>(rec, leaf0, tris, ta, na, ntasks,
                                                                static_cast<Node8*>(nodes8), static_cast<float4*>(tris8),
                                                                counters, tb, nb, capacity, err);
         if ((e = cudaMemcpyAsync(host_ctl, counters, 12, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return (int)e;
