@@ -147,7 +147,7 @@ sq_status build_morton(sq_ctx* c, sq_bvh* b, const sq_build_params& p)
     const size_t z_words = z_flags + n;
     uint32_t* zero = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * z_words));
     uint32_t* alt = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * 2ull * n));
-    float4* info = static_cast<float4*>(dalloc(c, sizeof(float4) * 4ull * n));
+    float4* info = static_cast<float4*>(dalloc(c, sizeof(float4) * 6ull * n));  // 2 x 48 B per boundary
     b->codes = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * (size_t)n));
     b->perm = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * (size_t)n));
     if (!zero || !alt || !info || !b->codes || !b->perm) {

@@ -156,6 +156,7 @@ namespace sqk {
 void scene_bounds(const float* tris, uint32_t n, uint32_t mode, uint32_t* box_ord, cudaStream_t s);
 void morton_codes(const float* tris, uint32_t n, uint32_t mode, const uint32_t* box_ord, uint32_t* keys,
                   uint32_t* vals, uint32_t* hist, uint32_t digit_bits, uint32_t passes, cudaStream_t s);
+// flags: n zeroed words; info: 6n float4 (a 48-byte record per boundary side)
 void lbvh_climb(const uint32_t* codes, const uint32_t* perm, const float* tris, uint32_t n, sq::Node* nodes,
                 uint32_t* flags, float4* info, uint32_t* err, cudaStream_t s);
 

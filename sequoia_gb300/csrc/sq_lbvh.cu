@@ -173,68 +173,90 @@ __global__ void __launch_bounds__(256) k_lbvh_climb(const uint32_t* __restrict__
                                                     const float* __restrict__ tris, uint32_t n, Node* __restrict__ nodes,
                                                     uint32_t* __restrict__ flags, float4* __restrict__ info, uint32_t* err)
 {
+    constexpr uint32_t FULL = 0xFFFFFFFFu;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t code = codes[i];
-    if (i > 0 && codes[i - 1] == code) return;  // not a run head
-    uint32_t e = i + 1;
-    while (e < n && e < i + 8 && codes[e] == code) ++e;
-    if (e == i + 8 && e < n && codes[e] == code) {
-        uint32_t lo = e, hi = n;
-        while (lo < hi) {
-            const uint32_t mid = lo + ((hi - lo) >> 1);
-            if (codes[mid] == code) lo = mid + 1; else hi = mid;
-        }
-        e = lo;
-    }
+    const int lane = (int)(threadIdx.x & 31u);
     const uint32_t leaf0 = 2u * n + 2u;
-    // leaf records of the run and the run box
+    // this lane's node: [l, r) with its box and split, while `active`
+    bool active = false;
+    uint32_t l = 0, r = 0, split = 0;
+    uint32_t dl = 0, dr = 0;  // code XOR at boundaries l and r (where they are inside (0, n))
     Box box;
     box_reset(box);
-    for (uint32_t p = i; p < e; ++p) {
-        const uint32_t t = perm[p];
-        float tv[9];
-        load_tri(tris, t, tv);
-        const Box b = tri_box(tv);
-        store_node(nodes + leaf0 + p, b, t, 1u, kLeafFlag);
-        box_grow(box, b);
-    }
-    uint32_t l = i, r = e, split = 0;
-    if (e - i >= 8) run_subtree(i, e, leaf0, nodes, box, split, err);
-
-    for (;;) {
-        if (l == 0 && r == n) {
-            if (n >= 8) store_node(nodes, box, 2u * split, 2u, 0);
-            else store_node(nodes, box, leaf0, n, 0);
-            return;
+    // codes of this position and its neighbours (shuffled within the warp)
+    const uint32_t W = i - (uint32_t)lane;  // the warp's first position
+    const uint32_t code = i < n ? codes[i] : 0u;
+    uint32_t prev = __shfl_up_sync(FULL, code, 1), next = __shfl_down_sync(FULL, code, 1);
+    if (lane == 0 && i > 0 && i < n) prev = codes[i - 1];
+    if (lane == 31 && i + 1 < n) next = codes[i + 1];
+    // d_own = code XOR at boundary i (between positions i - 1 and i); d_end =
+    // the XOR at boundary W + 32, just past the warp
+    const uint32_t d_own = prev ^ code;
+    const uint32_t d_end = __shfl_sync(FULL, code ^ next, 31);
+    if (i < n) {
+        if (i == 0 || prev != code) {  // a run head
+            uint32_t e = i + 1;
+            if (e < n && next == code) {
+                ++e;
+                while (e < n && e < i + 8 && codes[e] == code) ++e;
+            }
+            if (e == i + 8 && e < n && codes[e] == code) {
+                uint32_t lo = e, hi = n;
+                while (lo < hi) {
+                    const uint32_t mid = lo + ((hi - lo) >> 1);
+                    if (codes[mid] == code) lo = mid + 1; else hi = mid;
+                }
+                e = lo;
+            }
+            // leaf records of the run and the run box
+            for (uint32_t p = i; p < e; ++p) {
+                const uint32_t t = perm[p];
+                float tv[9];
+                load_tri(tris, t, tv);
+                const Box b = tri_box(tv);
+                store_node(nodes + leaf0 + p, b, t, 1u, kLeafFlag);
+                box_grow(box, b);
+            }
+            if (e - i >= 8) run_subtree(i, e, leaf0, nodes, box, split, err);
+            l = i;
+            r = e;
+            active = true;
         }
-        uint32_t p;
-        bool left;
+    }
+    {
+        // the XOR at the run's end comes from the lane that owns it when it is
+        // inside the warp
+        const bool r_in = active && r - W < 32u;
+        const uint32_t dr_in = __shfl_sync(FULL, d_own, r_in ? (int)(r - W) : lane);
+        if (active) {
+            dl = d_own;
+            if (r_in) dr = dr_in;
+            else if (r == W + 32u) dr = d_end;
+            else if (r < n) dr = codes[r - 1] ^ codes[r];
+        }
+    }
+
+    // The parent of a node over [l, r) splits at boundary l or r (whichever
+    // has the smaller code XOR with its neighbour); the node is its left
+    // child when the split is at r.
+    auto parent_of = [&](uint32_t& p, bool& left) {
         if (l == 0) { p = r; left = true; }
         else if (r == n) { p = l; left = false; }
-        else {
-            const uint32_t dl = codes[l - 1] ^ codes[l];
-            const uint32_t dr = codes[r - 1] ^ codes[r];
-            if (dr < dl) { p = r; left = true; } else { p = l; left = false; }
-        }
-        float4* mine = info + 2ull * (2ull * p + (left ? 0u : 1u));
-        mine[0] = make_float4(box.mn[0], box.mn[1], box.mn[2], __uint_as_float(left ? l : r));
-        mine[1] = make_float4(box.mx[0], box.mx[1], box.mx[2], __uint_as_float(split));
-        // release my record, acquire the sibling's (the first arrival stops)
-        const uint32_t old = atomic_add_acq_rel_u32(flags + p, 1u);
-        if (old == 0) return;
-        if (old != 1) { raise_error(err, SQ_DEVERR_TOPOLOGY); return; }
-        const float4* sib = info + 2ull * (2ull * p + (left ? 1u : 0u));
-        const float4 s0 = __ldcg(sib), s1 = __ldcg(sib + 1);
-        Box sb;
-        sb.mn[0] = s0.x; sb.mn[1] = s0.y; sb.mn[2] = s0.z;
-        sb.mx[0] = s1.x; sb.mx[1] = s1.y; sb.mx[2] = s1.z;
-        const uint32_t s_end = __float_as_uint(s0.w), s_split = __float_as_uint(s1.w);
-        uint32_t ll, rr;
+        else if (dr < dl) { p = r; left = true; }
+        else { p = l; left = false; }
+    };
+    auto write_root = [&]() {
+        if (n >= 8) store_node(nodes, box, 2u * split, 2u, 0);
+        else store_node(nodes, box, leaf0, n, 0);
+    };
+    // Merge this node with its sibling (ending or starting at s_end, with the
+    // code XOR s_d at that far boundary): write both children's records when
+    // the parent is an inner node, and continue with the parent.
+    auto merge = [&](uint32_t p, bool left, uint32_t s_end, const Box& sb, uint32_t s_split, uint32_t s_d) {
+        uint32_t ll, rr, lsplit, rsplit;
         Box lb, rb;
-        uint32_t lsplit, rsplit;
-        if (left) { ll = l; rr = s_end; lb = box; rb = sb; lsplit = split; rsplit = s_split; }
-        else { ll = s_end; rr = r; lb = sb; rb = box; lsplit = s_split; rsplit = split; }
+        if (left) { ll = l; rr = s_end; lb = box; rb = sb; lsplit = split; rsplit = s_split; dr = s_d; }
+        else { ll = s_end; rr = r; lb = sb; rb = box; lsplit = s_split; rsplit = split; dl = s_d; }
         if (rr - ll >= 8) {
             write_child(nodes, 2u * p, ll, p, lb, lsplit, leaf0);
             write_child(nodes, 2u * p + 1u, p, rr, rb, rsplit, leaf0);
@@ -244,6 +266,70 @@ __global__ void __launch_bounds__(256) k_lbvh_climb(const uint32_t* __restrict__
         l = ll;
         r = rr;
         split = p;
+    };
+
+    // Warp phase: nodes whose two children both finish inside this warp are
+    // merged through shuffles (the lanes of the two children find each other
+    // by their common parent), in rounds, until a round merges nothing; only
+    // the nodes left then take the global protocol below.  Most small
+    // subtrees never touch the sibling records or the flags.
+    for (;;) {
+        if (active && l == 0 && r == n) { write_root(); active = false; }
+        const uint32_t A = __ballot_sync(FULL, active);
+        if (!A) break;
+        bool merged = false;
+        if (active) {
+            uint32_t p;
+            bool left;
+            parent_of(p, left);
+            const uint32_t grp = __match_any_sync(A, p);
+            if (__popc(grp) == 2) {
+                const int other = __ffs(grp & ~(1u << lane)) - 1;
+                const uint32_t o_r = __shfl_sync(grp, r, other);
+                const uint32_t o_dr = __shfl_sync(grp, dr, other);
+                const uint32_t o_split = __shfl_sync(grp, split, other);
+                Box ob;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    ob.mn[k] = __shfl_sync(grp, box.mn[k], other);
+                    ob.mx[k] = __shfl_sync(grp, box.mx[k], other);
+                }
+                if (left) merge(p, true, o_r, ob, o_split, o_dr);
+                else active = false;
+                merged = true;
+            }
+        }
+        if (!__any_sync(FULL, merged)) break;
+    }
+
+    if (!active) return;
+
+    // Global protocol: publish this node's range end, box and split beside
+    // its parent boundary, count the arrival; the second arrival continues
+    // with the union of both children.
+    for (;;) {
+        if (l == 0 && r == n) {
+            write_root();
+            return;
+        }
+        uint32_t p;
+        bool left;
+        parent_of(p, left);
+        // record: box, far end, split and the code XOR at the far end
+        float4* mine = info + 3ull * (2ull * p + (left ? 0u : 1u));
+        mine[0] = make_float4(box.mn[0], box.mn[1], box.mn[2], __uint_as_float(left ? l : r));
+        mine[1] = make_float4(box.mx[0], box.mx[1], box.mx[2], __uint_as_float(split));
+        mine[2] = make_float4(__uint_as_float(left ? dl : dr), 0.0f, 0.0f, 0.0f);
+        // release my record, acquire the sibling's (the first arrival stops)
+        const uint32_t old = atomic_add_acq_rel_u32(flags + p, 1u);
+        if (old == 0) return;
+        if (old != 1) { raise_error(err, SQ_DEVERR_TOPOLOGY); return; }
+        const float4* sib = info + 3ull * (2ull * p + (left ? 1u : 0u));
+        const float4 s0 = __ldcg(sib), s1 = __ldcg(sib + 1), s2 = __ldcg(sib + 2);
+        Box sb;
+        sb.mn[0] = s0.x; sb.mn[1] = s0.y; sb.mn[2] = s0.z;
+        sb.mx[0] = s1.x; sb.mx[1] = s1.y; sb.mx[2] = s1.z;
+        merge(p, left, __float_as_uint(s0.w), sb, __float_as_uint(s1.w), __float_as_uint(s2.x));
     }
 }
 
