@@ -52,6 +52,10 @@ WORKLOAD = dict(name="soup_2m", tris=2_000_000, clusters=64, seed=2, width=3840,
                 eye=(0.0, 0.0, -40.0), target=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0), vfov=60.0)
 STRESS = dict(tris=8_000_000, clusters=256, seed=5, rays=1 << 24, batches=64)
 LBVH_KERNELS = 7  # scene bounds, Morton codes, 4 onesweep passes, climb
+# DRAM bytes (read + write) of one k_trace8_tiles<closest> launch on this
+# workload, from the ncu capture summarised in profiles/k_trace8_tiles_soup2m.md
+TRACE8_DRAM_BYTES = 123.8e6 + 112.1e6
+TRACE8_DRAM_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch (profiles/k_trace8_tiles_soup2m.md)"
 
 
 def measured_peaks():
@@ -464,7 +468,8 @@ def main():
                     "requested_bytes": req_bytes / rays_total},
         "hit_rays": int((hits_np[:, 0] != -1).sum()),
         "roofline": {"bound": "hbm", "kernel": "k_trace8<closest>", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": TRACE8_DRAM_BYTES, "traffic_source": TRACE8_DRAM_SOURCE,
                      "bytes_model": "kernel-counted requested bytes: 80 B per wide node loaded, 48 B per "
                                     "triangle tested, 15 B of outputs per ray"},
         "build_roofline": {"bound": "hbm", "achieved": build_gbs, "peak": peak, "unit": "GB/s",
