@@ -30,6 +30,7 @@
 #include "sq_common.cuh"
 
 #include <algorithm>
+#include <type_traits>
 #include <utility>
 
 namespace {
@@ -499,6 +500,40 @@ __device__ __forceinline__ bool no_nan_slabs(const Pre8& r)
     return ok;
 }
 
+// Affine child-box distances.  For a NaN-free ray the distance to a child's
+// plane on axis a is, in exact arithmetic,
+//     (org + q * 2^e - o) * inv = q * A + C,  A = 2^e * inv,  C = (org - o) * inv,
+// so each of a child's six planes costs one fma once A and C are known for
+// the node.  A is exact (a power of two times inv).  The rounded results
+// differ from the exact form (dequantise, subtract, multiply: three
+// roundings), so the near distance is computed from C - E and the far from
+// C + E, with the margin E = 2^-19 * M + 2^-125 where
+//     M = (|org| + 255 * 2^e + |o| + 2^-126) * |inv|
+// bounds every term whose rounding matters (|q A|, |C|, the plane and the
+// slab distance themselves).  The worst case of the roundings sums to about
+// 8 * 2^-24 * M (plus subnormal absolute errors well under 2^-125), so the
+// affine near distance is never above, and the far never below, what the
+// exact form computes for the same quantised box, which in turn is never
+// tighter than the FP32 box.  The test therefore passes for every child the
+// exact test passes (it may pass a few more), and the hits are unchanged.
+// A node whose M is not finite (coordinates near FLT_MAX) uses the exact form.
+__device__ __forceinline__ bool node_affine(const float* org, const float* sc, const Pre8& rp, float* A, float* Cn,
+                                            float* Cf)
+{
+    float msum = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        A[a] = sc[a] * rp.inv[a];
+        const float C = (org[a] - rp.o[a]) * rp.inv[a];
+        const float M = (fmaf(255.0f, sc[a], fabsf(org[a]) + fabsf(rp.o[a])) + 0x1p-126f) * fabsf(rp.inv[a]);
+        const float E = fmaf(M, 0x1p-19f, 0x1p-125f);
+        Cn[a] = C - E;
+        Cf[a] = C + E;
+        msum += M;
+    }
+    return isfinite(msum);
+}
+
 struct Res8 {
     uint32_t id;
     float t;
@@ -553,44 +588,58 @@ __device__ Res8 trace8_impl(const Node8* __restrict__ nodes, uint32_t root, cons
         float ht[8];
         int nh = 0;
         uint32_t inner_rank = 0, tri_off = 0;
+        float A[3], Cn[3], Cf[3];
+        const bool aff = SIGNED && node_affine(org, sc, rp, A, Cn, Cf);
+        // the child loop, compiled once per distance form (branching per node,
+        // not per child, keeps one form's registers live at a time)
+        auto scan = [&](auto form) {
+            constexpr bool AFF = decltype(form)::value;
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const uint32_t cnt = (counts >> (4 * k)) & 0xFu;
-            const bool is_inner = (imask >> k) & 1u;
-            if ((valid >> k) & 1u) {
-                const int w = k >> 2;
-                const uint32_t j = (uint32_t)(k & 3);
-                float ta[3], tb[3];
+            for (int k = 0; k < 8; ++k) {
+                const uint32_t cnt = (counts >> (4 * k)) & 0xFu;
+                const bool is_inner = (imask >> k) & 1u;
+                if ((valid >> k) & 1u) {
+                    const int w = k >> 2;
+                    const uint32_t j = (uint32_t)(k & 3);
+                    float ta[3], tb[3];
 #pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    const float ba = fmaf(qbyte(qa[a * 2 + w], j), sc[a], org[a]);
-                    const float bb = fmaf(qbyte(qb[a * 2 + w], j), sc[a], org[a]);
-                    ta[a] = (ba - rp.o[a]) * rp.inv[a];
-                    tb[a] = (bb - rp.o[a]) * rp.inv[a];
+                    for (int a = 0; a < 3; ++a) {
+                        if (AFF) {
+                            ta[a] = fmaf(qbyte(qa[a * 2 + w], j), A[a], Cn[a]);
+                            tb[a] = fmaf(qbyte(qb[a * 2 + w], j), A[a], Cf[a]);
+                        } else {
+                            const float ba = fmaf(qbyte(qa[a * 2 + w], j), sc[a], org[a]);
+                            const float bb = fmaf(qbyte(qb[a * 2 + w], j), sc[a], org[a]);
+                            ta[a] = (ba - rp.o[a]) * rp.inv[a];
+                            tb[a] = (bb - rp.o[a]) * rp.inv[a];
+                        }
+                    }
+                    tests++;
+                    float n, f;
+                    if (SIGNED) {
+                        n = fmaxf(fmaxf(fmaxf(ta[0], ta[1]), ta[2]), rp.tmin);
+                        f = fminf(fminf(tb[0], tb[1]), tb[2]);
+                    } else {
+                        n = fmaxf(fmaxf(fmaxf(fminf(ta[0], tb[0]), fminf(ta[1], tb[1])), fminf(ta[2], tb[2])), rp.tmin);
+                        f = fminf(fminf(fmaxf(ta[0], tb[0]), fmaxf(ta[1], tb[1])), fmaxf(ta[2], tb[2]));
+                    }
+                    f = f * kRobust;
+                    if (n <= f && n <= best_t * kRobust) {
+                        const uint32_t ent = is_inner ? (child_base + inner_rank)
+                                                      : (0x80000000u | (cnt << 27) | (tri_base + tri_off));
+                        int b = nh - 1;
+                        while (b >= 0 && ht[b] > n) { hn[b + 1] = hn[b]; ht[b + 1] = ht[b]; --b; }
+                        hn[b + 1] = ent;
+                        ht[b + 1] = n;
+                        nh++;
+                    }
                 }
-                tests++;
-                float n, f;
-                if (SIGNED) {
-                    n = fmaxf(fmaxf(fmaxf(ta[0], ta[1]), ta[2]), rp.tmin);
-                    f = fminf(fminf(tb[0], tb[1]), tb[2]);
-                } else {
-                    n = fmaxf(fmaxf(fmaxf(fminf(ta[0], tb[0]), fminf(ta[1], tb[1])), fminf(ta[2], tb[2])), rp.tmin);
-                    f = fminf(fminf(fmaxf(ta[0], tb[0]), fmaxf(ta[1], tb[1])), fmaxf(ta[2], tb[2]));
-                }
-                f = f * kRobust;
-                if (n <= f && n <= best_t * kRobust) {
-                    const uint32_t ent = is_inner ? (child_base + inner_rank)
-                                                  : (0x80000000u | (cnt << 27) | (tri_base + tri_off));
-                    int b = nh - 1;
-                    while (b >= 0 && ht[b] > n) { hn[b + 1] = hn[b]; ht[b + 1] = ht[b]; --b; }
-                    hn[b + 1] = ent;
-                    ht[b + 1] = n;
-                    nh++;
-                }
+                inner_rank += is_inner;
+                tri_off += cnt;
             }
-            inner_rank += is_inner;
-            tri_off += cnt;
-        }
+        };
+        if (aff) scan(std::true_type{});
+        else scan(std::false_type{});
         if (sp + nh > kStack8) { overflow = true; break; }
         for (int a = nh - 1; a >= 0; --a) { st_e[sp] = hn[a]; st_t[sp] = ht[a]; sp++; }
         have = false;
@@ -731,67 +780,80 @@ __device__ __forceinline__ void visit8(Lane8& L, const Node8* __restrict__ nodes
     float near_t = 0.0f;
     const int seg = L.sp;
     uint32_t inner_rank = 0, tri_off = 0;
+    float A[3], Cn[3], Cf[3];
+    const bool aff = SIGNED && node_affine(org, sc, rp, A, Cn, Cf);
+    // the child loop, compiled once per distance form (see the tiles path)
+    auto scan = [&](auto form) {
+        constexpr bool AFF = decltype(form)::value;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const uint32_t cnt = (counts >> (4 * k)) & 0xFu;
-        const bool is_inner = (imask >> k) & 1u;
-        if ((valid >> k) & 1u) {
-            const int w = k >> 2;
-            const uint32_t j = (uint32_t)(k & 3);
-            float ta[3], tb[3];
+        for (int k = 0; k < 8; ++k) {
+            const uint32_t cnt = (counts >> (4 * k)) & 0xFu;
+            const bool is_inner = (imask >> k) & 1u;
+            if ((valid >> k) & 1u) {
+                const int w = k >> 2;
+                const uint32_t j = (uint32_t)(k & 3);
+                float ta[3], tb[3];
 #pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                const float ba = fmaf(qbyte(qa[a * 2 + w], j), sc[a], org[a]);
-                const float bb = fmaf(qbyte(qb[a * 2 + w], j), sc[a], org[a]);
-                ta[a] = (ba - rp.o[a]) * rp.inv[a];
-                tb[a] = (bb - rp.o[a]) * rp.inv[a];
-            }
-            L.tests++;
-            float n, f;
-            if (SIGNED) {
-                n = fmaxf(fmaxf(fmaxf(ta[0], ta[1]), ta[2]), rp.tmin);
-                f = fminf(fminf(tb[0], tb[1]), tb[2]);
-            } else {
-                n = fmaxf(fmaxf(fmaxf(fminf(ta[0], tb[0]), fminf(ta[1], tb[1])), fminf(ta[2], tb[2])), rp.tmin);
-                f = fminf(fminf(fmaxf(ta[0], tb[0]), fmaxf(ta[1], tb[1])), fmaxf(ta[2], tb[2]));
-            }
-            f = f * kRobust;
-            if (n <= f && n <= lim) {
-                uint32_t ent = is_inner ? (child_base + inner_rank) : (0x80000000u | (cnt << 27) | (tri_base + tri_off));
-                float et = n;
-                if (near_e == kNoHit) {
-                    near_e = ent;
-                    near_t = n;
-                } else {
-                    // Children are visited in ascending (entry distance, slot)
-                    // order.  The pushed entries keep that order from the top;
-                    // a new child has the largest slot so far and goes below
-                    // entries of equal distance, a displaced nearest has the
-                    // smallest and goes above them.
-                    bool displaced = false;
-                    if (n < near_t) {
-                        const uint32_t te = near_e; const float tt = near_t;
-                        near_e = ent; near_t = n;
-                        ent = te; et = tt;
-                        displaced = true;
-                    }
-                    if (L.sp >= kStack8) {
-                        L.overflow = true;
+                for (int a = 0; a < 3; ++a) {
+                    if (AFF) {
+                        ta[a] = fmaf(qbyte(qa[a * 2 + w], j), A[a], Cn[a]);
+                        tb[a] = fmaf(qbyte(qb[a * 2 + w], j), A[a], Cf[a]);
                     } else {
-                        int b = L.sp - 1;
-                        while (b >= seg && (st_t[b] < et || (!displaced && st_t[b] == et))) {
-                            st_e[b + 1] = st_e[b]; st_t[b + 1] = st_t[b]; --b;
+                        const float ba = fmaf(qbyte(qa[a * 2 + w], j), sc[a], org[a]);
+                        const float bb = fmaf(qbyte(qb[a * 2 + w], j), sc[a], org[a]);
+                        ta[a] = (ba - rp.o[a]) * rp.inv[a];
+                        tb[a] = (bb - rp.o[a]) * rp.inv[a];
+                    }
+                }
+                L.tests++;
+                float n, f;
+                if (SIGNED) {
+                    n = fmaxf(fmaxf(fmaxf(ta[0], ta[1]), ta[2]), rp.tmin);
+                    f = fminf(fminf(tb[0], tb[1]), tb[2]);
+                } else {
+                    n = fmaxf(fmaxf(fmaxf(fminf(ta[0], tb[0]), fminf(ta[1], tb[1])), fminf(ta[2], tb[2])), rp.tmin);
+                    f = fminf(fminf(fmaxf(ta[0], tb[0]), fmaxf(ta[1], tb[1])), fmaxf(ta[2], tb[2]));
+                }
+                f = f * kRobust;
+                if (n <= f && n <= lim) {
+                    uint32_t ent = is_inner ? (child_base + inner_rank) : (0x80000000u | (cnt << 27) | (tri_base + tri_off));
+                    float et = n;
+                    if (near_e == kNoHit) {
+                        near_e = ent;
+                        near_t = n;
+                    } else {
+                        // Children are visited in ascending (entry distance, slot)
+                        // order.  The pushed entries keep that order from the top;
+                        // a new child has the largest slot so far and goes below
+                        // entries of equal distance, a displaced nearest has the
+                        // smallest and goes above them.
+                        bool displaced = false;
+                        if (n < near_t) {
+                            const uint32_t te = near_e; const float tt = near_t;
+                            near_e = ent; near_t = n;
+                            ent = te; et = tt;
+                            displaced = true;
                         }
-                        st_e[b + 1] = ent;
-                        st_t[b + 1] = et;
-                        L.sp++;
+                        if (L.sp >= kStack8) {
+                            L.overflow = true;
+                        } else {
+                            int b = L.sp - 1;
+                            while (b >= seg && (st_t[b] < et || (!displaced && st_t[b] == et))) {
+                                st_e[b + 1] = st_e[b]; st_t[b + 1] = st_t[b]; --b;
+                            }
+                            st_e[b + 1] = ent;
+                            st_t[b + 1] = et;
+                            L.sp++;
+                        }
                     }
                 }
             }
+            inner_rank += is_inner;
+            tri_off += cnt;
         }
-        inner_rank += is_inner;
-        tri_off += cnt;
-    }
+    };
+    if (aff) scan(std::true_type{});
+    else scan(std::false_type{});
     if (L.overflow) { L.cur = kNoHit; return; }
     // the next node: the nearest child, else the stack (leaves tested on the way)
     uint32_t e = near_e;
