@@ -70,3 +70,42 @@ def test_wide_terrain_bounce(ctx, oracle):
     b2, _ = ctx.trace(bvh, "closest", rays=br, binary=True)
     b8, _ = ctx.trace(bvh, "closest", rays=br)
     assert np.array_equal(b8["id"], b2["id"]) and np.array_equal(b8["t"], b2["t"])
+
+
+@pytest.mark.parametrize("offset,scale", [((1.0e4, -3.0e3, 5.0e3), 0.01), ((-2.5e5, 7.0e4, 1.0e5), 0.5),
+                                          ((0.0, 0.0, 0.0), 1.0e-3)])
+def test_wide_far_from_origin(ctx, offset, scale):
+    """Small geometry far from the origin, rays grazing it from nearby and
+    from far away: the slab distances cancel heavily, which is where the
+    affine child test's rounding margin matters.  Hits must stay identical to
+    the FP32 binary traversal."""
+    from sequoia_gb300 import scenes
+    base = scenes.displaced_icosphere(4, seed=9).astype(np.float64)
+    tris = (base * scale + np.tile(np.asarray(offset, np.float64), 3)).astype(np.float32)
+    bvh = ctx.build(tris, "morton", wide=True)
+    lo, hi = scenes.scene_box(tris)
+    ext = float((hi - lo).max())
+    rng = np.random.default_rng(11)
+    n = 200_000
+    rays = np.zeros((n, 8), np.float32)
+    centre = (lo.astype(np.float64) + hi) / 2
+    # origins on spheres of radius 0.6 .. 1000 extents, aimed at jittered points of the box
+    rad = ext * np.exp(rng.uniform(np.log(0.6), np.log(1000.0), n))
+    dirs = rng.standard_normal((n, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    org = centre + dirs * rad[:, None]
+    aim = centre + (rng.uniform(-0.6, 0.6, (n, 3)) * ext)
+    d = aim - org
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays[:, 0:3] = org
+    rays[:, 4:7] = d
+    rays[:, 7] = 3.4e38
+    h2, _ = ctx.trace(bvh, "closest", rays=rays, binary=True)
+    h8, _ = ctx.trace(bvh, "closest", rays=rays)
+    assert (h2["id"] != 0xFFFFFFFF).sum() > n // 10
+    assert np.array_equal(h8["id"], h2["id"])
+    assert np.array_equal(h8["t"], h2["t"])
+    a2, _ = ctx.trace(bvh, "anyhit", rays=rays, binary=True)
+    a8, _ = ctx.trace(bvh, "anyhit", rays=rays)
+    assert np.array_equal(a8["id"] != 0xFFFFFFFF, a2["id"] != 0xFFFFFFFF)
+    assert ctx.sync() == 0
