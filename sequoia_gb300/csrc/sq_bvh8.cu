@@ -99,30 +99,49 @@ __device__ __forceinline__ uint8_t quant_hi(float v, float origin, int e)
 }
 
 
-// Build the 8-wide node `node_i` from binary record `rec_i` with one warp:
-// lane k < 8 holds candidate child slot k (its binary record in registers),
-// so the records a step opens are loaded in parallel and the six dequantised
-// planes of each slot are computed by the slot's own lane.  The decisions are
-// those of a sequential scan over the slots: open the first child of largest
-// surface area that still fits, until none does.  Inner children become
-// nodes [child_base, child_base + n) where child_base comes from reserve(n)
-// (called by lane 0); publish(node, record) is called by the child's lane.
+// Build 8-wide nodes from binary records, eight lanes per node and four
+// nodes per warp.  Lane k of a group holds candidate child slot k (its binary
+// record in registers), so the records a step opens are loaded in parallel
+// and the six dequantised planes of each slot are computed by the slot's own
+// lane.  The decisions are those of a sequential scan over the slots: open
+// the first child of largest surface area that still fits, until none does.
+// All 32 lanes must call this; a group whose `active` is false only takes
+// part in the warp-wide shuffles.  Inner children become nodes
+// [child_base, child_base + n) where child_base comes from reserve(n)
+// (called by the group's first lane); publish(node, record) is called by the
+// child's lane.  sm: this warp's staging area (kGroupSmem per warp).
+struct GroupSmem {
+    Node8 node[4];
+    uint32_t off[4][8], cnt[4][8], child[4][8];
+};
+
 template <class Reserve, class Publish>
-__device__ void collapse_node_warp(const Node* __restrict__ rec, uint32_t leaf0, const float* __restrict__ tris,
-                                   uint32_t rec_i, uint32_t node_i, Node8* __restrict__ nodes8,
-                                   float4* __restrict__ tris8, uint32_t* __restrict__ tri_counter, uint32_t* err,
-                                   Reserve reserve, Publish publish)
+__device__ void collapse_node_group(const Node* __restrict__ rec, uint32_t leaf0, const float* __restrict__ tris,
+                                    bool active, uint32_t rec_i, uint32_t node_i, Node8* __restrict__ nodes8,
+                                    float4* __restrict__ tris8, uint32_t* __restrict__ tri_counter, uint32_t* err,
+                                    GroupSmem& sm, Reserve reserve, Publish publish)
 {
     constexpr uint32_t FULL = 0xFFFFFFFFu;
     const int lane = (int)(threadIdx.x & 31u);
-    const Node self = rec[rec_i];
-    const uint32_t c0 = self.child, cn = node_count(self.count_flags);
-    if (cn > 8) {
-        if (lane == 0) raise_error(err, SQ_DEVERR_NODE_COUNT);
-        return;
+    const int k = lane & 7;   // slot of this lane
+    const int g = lane >> 3;  // group (node) of this lane
+    const int gs = lane & ~7; // first lane of the group
+    auto gballot = [&](bool pr) -> uint32_t { return (__ballot_sync(FULL, pr) >> gs) & 0xFFu; };
+    Node self;
+    uint32_t c0 = 0, cn = 0;
+    if (active) {
+        self = rec[rec_i];
+        c0 = self.child;
+        cn = node_count(self.count_flags);
+        if (cn > 8) {
+            if (k == 0) raise_error(err, SQ_DEVERR_NODE_COUNT);
+            active = false;
+        }
     }
     // slot state of this lane
     Node e_node;
+    e_node.child = 0;
+    e_node.count_flags = 0;
     uint32_t e_rec = 0, e_kind = 0, e_cnt = 0;
     float e_sa = 0.0f;
     auto load_entry = [&](uint32_t i) {
@@ -133,164 +152,163 @@ __device__ void collapse_node_warp(const Node* __restrict__ rec, uint32_t leaf0,
         if (node_is_leaf(e_node.count_flags)) e_kind = 2;
         else e_kind = (e_node.child < leaf0 && e_cnt > 0) ? 0u : 1u;
     };
-    if (lane < (int)cn) load_entry(c0 + (uint32_t)lane);
+    if (active && k < (int)cn) load_entry(c0 + (uint32_t)k);
     // the start set is a binary record's two children or a cluster's leaves;
     // open the child of largest area (a binary record into its two children,
     // a leaf cluster into its single-triangle leaves) while it fits in 8 slots
-    int nc = (int)cn;
+    int nc = active ? (int)cn : 0;
+    bool opening = active;
     for (;;) {
-        const bool can = lane < nc && (e_kind == 0 ? (nc + 1 <= 8) : (e_kind == 1 && nc + (int)e_cnt - 1 <= 8));
-        const uint32_t canm = __ballot_sync(FULL, can);
-        if (!canm) break;
+        const bool can = opening && k < nc &&
+                         (e_kind == 0 ? (nc + 1 <= 8) : (e_kind == 1 && nc + (int)e_cnt - 1 <= 8));
+        const uint32_t canm = gballot(can);
+        opening = opening && canm != 0;
+        if (!__any_sync(FULL, opening)) break;
         int best = -1;
         float bsa = 0.0f;
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const float sk = __shfl_sync(FULL, e_sa, k);
-            if (((canm >> k) & 1u) && (best < 0 || sk > bsa)) { best = k; bsa = sk; }
+        for (int q = 0; q < 8; ++q) {
+            const float sq = __shfl_sync(FULL, e_sa, q, 8);
+            if (((canm >> q) & 1u) && (best < 0 || sq > bsa)) { best = q; bsa = sq; }
         }
-        const uint32_t bkind = __shfl_sync(FULL, e_kind, best), bcnt = __shfl_sync(FULL, e_cnt, best);
-        const uint32_t bchild = __shfl_sync(FULL, e_node.child, best);
+        const int bs = best < 0 ? 0 : best;
+        const uint32_t bkind = __shfl_sync(FULL, e_kind, bs, 8), bcnt = __shfl_sync(FULL, e_cnt, bs, 8);
+        const uint32_t bchild = __shfl_sync(FULL, e_node.child, bs, 8);
         const uint32_t m = bkind == 0 ? 2u : bcnt;
-        if (m == 0) {
-            // drop the empty cluster: the last slot moves into its place
-            --nc;
+        const bool drop = opening && m == 0;
+        if (__any_sync(FULL, drop)) {
+            // drop the empty cluster: the group's last slot moves into its place
+            const int src = nc > 0 ? nc - 1 : 0;
             Node t;
-            t.mnx = __shfl_sync(FULL, e_node.mnx, nc); t.mny = __shfl_sync(FULL, e_node.mny, nc);
-            t.mnz = __shfl_sync(FULL, e_node.mnz, nc); t.count_flags = __shfl_sync(FULL, e_node.count_flags, nc);
-            t.mxx = __shfl_sync(FULL, e_node.mxx, nc); t.mxy = __shfl_sync(FULL, e_node.mxy, nc);
-            t.mxz = __shfl_sync(FULL, e_node.mxz, nc); t.child = __shfl_sync(FULL, e_node.child, nc);
-            const uint32_t trec = __shfl_sync(FULL, e_rec, nc), tkind = __shfl_sync(FULL, e_kind, nc);
-            const uint32_t tcnt = __shfl_sync(FULL, e_cnt, nc);
-            const float tsa = __shfl_sync(FULL, e_sa, nc);
-            if (lane == best) { e_node = t; e_rec = trec; e_kind = tkind; e_cnt = tcnt; e_sa = tsa; }
-            continue;
+            t.mnx = __shfl_sync(FULL, e_node.mnx, src, 8); t.mny = __shfl_sync(FULL, e_node.mny, src, 8);
+            t.mnz = __shfl_sync(FULL, e_node.mnz, src, 8);
+            t.count_flags = __shfl_sync(FULL, e_node.count_flags, src, 8);
+            t.mxx = __shfl_sync(FULL, e_node.mxx, src, 8); t.mxy = __shfl_sync(FULL, e_node.mxy, src, 8);
+            t.mxz = __shfl_sync(FULL, e_node.mxz, src, 8); t.child = __shfl_sync(FULL, e_node.child, src, 8);
+            const uint32_t trec = __shfl_sync(FULL, e_rec, src, 8), tkind = __shfl_sync(FULL, e_kind, src, 8);
+            const uint32_t tcnt = __shfl_sync(FULL, e_cnt, src, 8);
+            const float tsa = __shfl_sync(FULL, e_sa, src, 8);
+            if (drop) {
+                if (k == best) { e_node = t; e_rec = trec; e_kind = tkind; e_cnt = tcnt; e_sa = tsa; }
+                --nc;
+            }
         }
-        if (lane == best) load_entry(bchild);
-        else if (lane >= nc && lane < nc + (int)m - 1) load_entry(bchild + 1u + (uint32_t)(lane - nc));
-        nc += (int)m - 1;
+        if (opening && m != 0) {
+            if (k == best) load_entry(bchild);
+            else if (k >= nc && k < nc + (int)m - 1) load_entry(bchild + 1u + (uint32_t)(k - nc));
+            nc += (int)m - 1;
+        }
     }
     // a cluster of 2..8 triangles that did not fit becomes a wide child node
     // of its own (its triangles one per slot), so every triangle keeps its own
     // box; larger clusters stay leaf children of up to 15 triangles
-    if (lane < nc && e_kind == 1 && e_cnt >= 2 && e_cnt <= 8) e_kind = 0;
+    if (k < nc && e_kind == 1 && e_cnt >= 2 && e_cnt <= 8) e_kind = 0;
     // children with an empty box (empty grid cells and subtrees of them) take
     // no slot
-    const bool ok = lane < nc && e_node.mnx <= e_node.mxx && e_node.mny <= e_node.mxy && e_node.mnz <= e_node.mxz;
+    const bool ok = k < nc && e_node.mnx <= e_node.mxx && e_node.mny <= e_node.mxy && e_node.mnz <= e_node.mxz;
     const bool inner = ok && e_kind == 0;
     const bool leafc = ok && e_kind != 0;
-    if (__any_sync(FULL, leafc && e_cnt > 15u)) {
-        if (lane == 0) raise_error(err, SQ_DEVERR_NODE_COUNT);
-        return;
+    if (gballot(leafc && e_cnt > 15u)) {
+        if (active && k == 0) raise_error(err, SQ_DEVERR_NODE_COUNT);
+        active = false;
     }
     const uint32_t cntk = leafc ? e_cnt : 0u;
-    const uint32_t imask = __ballot_sync(FULL, inner) & 0xFFu;
-    const uint32_t valid = __ballot_sync(FULL, ok) & 0xFFu;
-    const uint32_t leafrec = __ballot_sync(FULL, lane < nc && node_is_leaf(e_node.count_flags)) & 0xFFu;
+    const uint32_t imask = gballot(inner);
+    const uint32_t valid = gballot(ok);
+    const uint32_t leafrec = gballot(k < nc && node_is_leaf(e_node.count_flags));
     uint32_t incl = cntk;
 #pragma unroll
     for (int o = 1; o < 8; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(FULL, incl, o);
-        if (lane >= o) incl += y;
+        const uint32_t y = __shfl_up_sync(FULL, incl, o, 8);
+        if (k >= o) incl += y;
     }
-    const uint32_t n_tris = __shfl_sync(FULL, incl, 7);
+    const uint32_t n_tris = __shfl_sync(FULL, incl, 7, 8);
     const uint32_t tri_off = incl - cntk;
     const uint32_t n_inner = __popc(imask);
     uint32_t child_base = 0, tri_base = 0;
-    if (lane == 0) {
+    if (active && k == 0) {
         child_base = n_inner ? reserve(n_inner) : 0u;
         tri_base = n_tris ? atomicAdd(tri_counter, n_tris) : 0u;
     }
-    child_base = __shfl_sync(FULL, child_base, 0);
-    tri_base = __shfl_sync(FULL, tri_base, 0);
-    // quantised child planes, one slot per lane
-    const float lo[3] = {self.mnx, self.mny, self.mnz}, hi[3] = {self.mxx, self.mxy, self.mxz};
-    int e[3];
+    child_base = __shfl_sync(FULL, child_base, 0, 8);
+    tri_base = __shfl_sync(FULL, tri_base, 0, 8);
+    // quantised child planes, one slot per lane, staged in shared memory
+    Node8& sn = sm.node[g];
+    int e[3] = {0, 0, 0};
+    if (active) {
+        const float lo[3] = {self.mnx, self.mny, self.mnz}, hi[3] = {self.mxx, self.mxy, self.mxz};
 #pragma unroll
-    for (int a = 0; a < 3; ++a) e[a] = quant_exp(lo[a], hi[a]);
-    uint32_t ql[3] = {255u, 255u, 255u}, qh[3] = {0u, 0u, 0u};
-    if (ok) {
-        const float cl[3] = {e_node.mnx, e_node.mny, e_node.mnz}, ch[3] = {e_node.mxx, e_node.mxy, e_node.mxz};
+        for (int a = 0; a < 3; ++a) e[a] = quant_exp(lo[a], hi[a]);
+        uint32_t ql[3] = {255u, 255u, 255u}, qh[3] = {0u, 0u, 0u};
+        if (ok) {
+            const float cl[3] = {e_node.mnx, e_node.mny, e_node.mnz}, ch[3] = {e_node.mxx, e_node.mxy, e_node.mxz};
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            ql[a] = quant_lo(cl[a], lo[a], e[a]);
-            qh[a] = quant_hi(ch[a], lo[a], e[a]);
+            for (int a = 0; a < 3; ++a) {
+                ql[a] = quant_lo(cl[a], lo[a], e[a]);
+                qh[a] = quant_hi(ch[a], lo[a], e[a]);
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a) { sn.qlo[a][k] = (uint8_t)ql[a]; sn.qhi[a][k] = (uint8_t)qh[a]; }
+        sm.off[g][k] = tri_off;
+        sm.cnt[g][k] = cntk;
+        sm.child[g][k] = e_node.child;
+        if (inner) publish(child_base + __popc(imask & ((1u << k) - 1u)), e_rec);
+    }
+    __syncwarp();
+    if (active && k == 0) {
+        uint32_t counts = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) counts |= sm.cnt[g][q] << (4 * q);
+        sn.ox = self.mnx; sn.oy = self.mny; sn.oz = self.mnz;
+        sn.exps_imask = (uint32_t)(e[0] + 127) | ((uint32_t)(e[1] + 127) << 8) | ((uint32_t)(e[2] + 127) << 16) |
+                        (imask << 24);
+        sn.child_base = child_base;
+        sn.tri_base = tri_base;
+        sn.counts = counts;
+        sn.valid = valid;
+    }
+    __syncwarp();
+    if (active) {
+        // the node: five 16-byte words
+        if (k < 5) reinterpret_cast<float4*>(nodes8 + node_i)[k] = reinterpret_cast<const float4*>(&sn)[k];
+        // leaf triangles, spread over the group: triangle t of the node
+        // belongs to the leaf slot whose [off, off + cnt) holds it
+        for (uint32_t t = (uint32_t)k; t < n_tris; t += 8u) {
+            int q = 0;
+#pragma unroll
+            for (int r = 1; r < 8; ++r)
+                if (sm.cnt[g][r] && sm.off[g][r] <= t) q = r;
+            const uint32_t j = t - sm.off[g][q], qc = sm.child[g][q];
+            // a leaf record is its own triangle; a cluster's are its leaves
+            const uint32_t id = ((leafrec >> q) & 1u) ? qc + j : rec[qc + j].child;
+            float tv[9];
+            load_tri(tris, id, tv);
+            float4* d = tris8 + 3ull * (tri_base + t);
+            d[0] = make_float4(tv[0], tv[1], tv[2], __uint_as_float(id));
+            d[1] = make_float4(tv[3], tv[4], tv[5], 0.0f);
+            d[2] = make_float4(tv[6], tv[7], tv[8], 0.0f);
         }
     }
-    // node words: qlo x (slots 0-3, 4-7), qlo y, qlo z, qhi x, qhi y, qhi z
-    uint32_t qw[12];
-    const bool slot = lane < 8;
-    const uint32_t sh = 8u * (uint32_t)(lane & 3);
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-#pragma unroll
-        for (int w = 0; w < 2; ++w) {
-            const bool mine = slot && (lane >> 2) == w;
-            qw[a * 2 + w] = __reduce_or_sync(FULL, mine ? ql[a] << sh : 0u);
-            qw[6 + a * 2 + w] = __reduce_or_sync(FULL, mine ? qh[a] << sh : 0u);
-        }
-    }
-    const uint32_t counts = __reduce_or_sync(FULL, slot ? cntk << (4u * (uint32_t)lane) : 0u);
-    if (inner) publish(child_base + __popc(imask & ((1u << lane) - 1u)), e_rec);
-    // leaf triangles, spread over the warp: triangle t of the node belongs to
-    // the leaf slot whose [tri_off, tri_off + cnt) holds it
-    uint32_t off_k[8], cnt_k[8], child_k[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        off_k[k] = __shfl_sync(FULL, tri_off, k);
-        cnt_k[k] = __shfl_sync(FULL, cntk, k);
-        child_k[k] = __shfl_sync(FULL, e_node.child, k);
-    }
-    for (uint32_t t = (uint32_t)lane; t < n_tris; t += 32u) {
-        int k = 0;
-#pragma unroll
-        for (int q = 1; q < 8; ++q)
-            if (cnt_k[q] && off_k[q] <= t) k = q;
-        uint32_t kk_child = child_k[0], kk_off = off_k[0];
-#pragma unroll
-        for (int q = 1; q < 8; ++q)
-            if (q == k) { kk_child = child_k[q]; kk_off = off_k[q]; }
-        const uint32_t j = t - kk_off;
-        // a leaf record is its own triangle; a cluster's are its leaves
-        const uint32_t id = ((leafrec >> k) & 1u) ? kk_child + j : rec[kk_child + j].child;
-        float tv[9];
-        load_tri(tris, id, tv);
-        float4* d = tris8 + 3ull * (tri_base + t);
-        d[0] = make_float4(tv[0], tv[1], tv[2], __uint_as_float(id));
-        d[1] = make_float4(tv[3], tv[4], tv[5], 0.0f);
-        d[2] = make_float4(tv[6], tv[7], tv[8], 0.0f);
-    }
-    // the node: five 16-byte words, one per lane
-    if (lane < 5) {
-        float4 w;
-        if (lane == 0) {
-            const uint32_t ei = (uint32_t)(e[0] + 127) | ((uint32_t)(e[1] + 127) << 8) |
-                                ((uint32_t)(e[2] + 127) << 16) | (imask << 24);
-            w = make_float4(self.mnx, self.mny, self.mnz, __uint_as_float(ei));
-        } else if (lane == 1) {
-            w = make_float4(__uint_as_float(child_base), __uint_as_float(tri_base), __uint_as_float(counts),
-                            __uint_as_float(valid));
-        } else {
-            const int b = (lane - 2) * 4;
-            w = make_float4(__uint_as_float(qw[b]), __uint_as_float(qw[b + 1]), __uint_as_float(qw[b + 2]),
-                            __uint_as_float(qw[b + 3]));
-        }
-        reinterpret_cast<float4*>(nodes8 + node_i)[lane] = w;
-    }
+    __syncwarp();  // the staging area is reused by the warp's next nodes
 }
 
-// One level of the collapse: warp i builds node task_node[i] from binary
-// record tasks[i]; inner children are allocated contiguously from the node
-// counter and appended to the next level's task list.
-__global__ void __launch_bounds__(128) k_collapse_level(const Node* __restrict__ rec, uint32_t leaf0,
-                                                        const float* __restrict__ tris, const uint32_t* __restrict__ tasks,
-                                                        const uint32_t* __restrict__ task_node, uint32_t ntasks,
-                                                        Node8* __restrict__ nodes8, float4* __restrict__ tris8,
-                                                        uint32_t* __restrict__ counters, uint32_t* __restrict__ next_tasks,
-                                                        uint32_t* __restrict__ next_node, uint32_t capacity, uint32_t* err)
+// One level of the collapse: group i (four per warp) builds node
+// task_node[i] from binary record tasks[i]; inner children are allocated
+// contiguously from the node counter and appended to the next level's list.
+constexpr int kCollapseBlock = 128;
+
+__global__ void __launch_bounds__(kCollapseBlock) k_collapse_level(
+    const Node* __restrict__ rec, uint32_t leaf0, const float* __restrict__ tris, const uint32_t* __restrict__ tasks,
+    const uint32_t* __restrict__ task_node, uint32_t ntasks, Node8* __restrict__ nodes8, float4* __restrict__ tris8,
+    uint32_t* __restrict__ counters, uint32_t* __restrict__ next_tasks, uint32_t* __restrict__ next_node,
+    uint32_t capacity, uint32_t* err)
 {
-    const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (i >= ntasks) return;  // whole warps
+    __shared__ GroupSmem s_group[kCollapseBlock / 32];
+    const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (4u * w >= ntasks) return;  // whole warps
+    const uint32_t i = 4u * w + ((threadIdx.x & 31u) >> 3);
+    const bool active = i < ntasks;
     auto reserve = [&](uint32_t k) -> uint32_t {
         const uint32_t b0 = atomicAdd(counters + 0, k);
         if ((unsigned long long)b0 + k > capacity) { raise_error(err, SQ_DEVERR_SAH_QUEUE); return 0u; }
@@ -302,7 +320,8 @@ __global__ void __launch_bounds__(128) k_collapse_level(const Node* __restrict__
         next_tasks[j] = record;
         next_node[j] = node;
     };
-    collapse_node_warp(rec, leaf0, tris, tasks[i], task_node[i], nodes8, tris8, counters + 1, err, reserve, publish);
+    collapse_node_group(rec, leaf0, tris, active, active ? tasks[i] : 0u, active ? task_node[i] : 0u, nodes8, tris8,
+                        counters + 1, err, s_group[threadIdx.x >> 5], reserve, publish);
 }
 
 // Collapse without host synchronisation (so it can be captured in a CUDA
@@ -327,9 +346,12 @@ __global__ void __launch_bounds__(128) k_collapse_fixed(const Node* __restrict__
         if (blockIdx.x == 0 && threadIdx.x == 0) raise_error(err, SQ_DEVERR_SAH_QUEUE);
         return;
     }
+    __shared__ GroupSmem s_group[4];
     uint32_t* next_count = counts + level + 1;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < ntasks; i += warps) {
+    for (uint32_t base = 4u * ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); base < ntasks; base += 4u * warps) {
+        const uint32_t i = base + ((threadIdx.x & 31u) >> 3);
+        const bool active = i < ntasks;
         auto reserve = [&](uint32_t k) -> uint32_t {
             const uint32_t b0 = atomicAdd(node_counter, k);
             if ((unsigned long long)b0 + k > capacity) { raise_error(err, SQ_DEVERR_SAH_QUEUE); return 0u; }
@@ -341,9 +363,115 @@ __global__ void __launch_bounds__(128) k_collapse_fixed(const Node* __restrict__
             next_tasks[j] = record;
             next_node[j] = node;
         };
-        collapse_node_warp(rec, leaf0, tris, tasks[i], task_node[i], nodes8, tris8, tri_counter, err, reserve,
-                           publish);
+        collapse_node_group(rec, leaf0, tris, active, active ? tasks[i] : 0u, active ? task_node[i] : 0u, nodes8,
+                            tris8, tri_counter, err, s_group[threadIdx.x >> 5], reserve, publish);
     }
+}
+
+// All levels in one cooperative launch (every block is resident): a
+// grid-stride loop over a level's tasks, a grid barrier, the next level.  No
+// host round trip per level.  The barrier's wait is bounded: a block that
+// polls more than kBarrierSpins times raises SQ_DEVERR_SAH_QUEUE and returns
+// (the other blocks then time out at their next barrier too).  Task lists
+// are read through L2 (__ldcg): the same lists are rewritten every other
+// level, so an SM's L1 may hold stale lines of them.
+constexpr uint32_t kBarrierSpins = 1u << 24;
+
+__device__ bool grid_barrier(uint32_t* bar, uint32_t nblocks, uint32_t* err)
+{
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        const uint32_t gen = ld_acquire_u32(bar + 1);
+        __threadfence();
+        if (atomicAdd(bar, 1u) + 1u == nblocks) {
+            // last arrival: reset the count, then open the next generation
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            uint32_t spins = 0;
+            while (ld_acquire_u32(bar + 1) == gen) {
+                if (++spins > kBarrierSpins) {
+                    raise_error(err, SQ_DEVERR_SAH_QUEUE);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+__global__ void __launch_bounds__(256) k_collapse_coop(const Node* __restrict__ rec, uint32_t leaf0,
+                                                       const float* __restrict__ tris, uint32_t* __restrict__ ws,
+                                                       uint32_t capacity, Node8* __restrict__ nodes8,
+                                                       float4* __restrict__ tris8, uint32_t* err)
+{
+    // ws: [0] node counter, [1] triangle counter, [2..3] barrier, [4] levels
+    // done, [8 .. 8 + kFixedLevels) level task counts, then the two (record,
+    // node) task lists of `capacity` entries each
+    uint32_t* node_counter = ws;
+    uint32_t* tri_counter = ws + 1;
+    uint32_t* bar = ws + 2;
+    uint32_t* counts = ws + 8;
+    uint32_t* ta = counts + kFixedLevels + 8;
+    uint32_t* na = ta + capacity;
+    uint32_t* tb = na + capacity;
+    uint32_t* nb = tb + capacity;
+    __shared__ GroupSmem s_group[8];
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    for (uint32_t level = 0;; ++level) {
+        const uint32_t ntasks = ld_acquire_u32(counts + level);
+        if (ntasks == 0) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) ws[4] = level;
+            return;
+        }
+        if (level + 1 >= kFixedLevels) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) raise_error(err, SQ_DEVERR_SAH_QUEUE);
+            return;
+        }
+        const uint32_t* tasks = (level & 1) ? tb : ta;
+        const uint32_t* task_node = (level & 1) ? nb : na;
+        uint32_t* next_tasks = (level & 1) ? ta : tb;
+        uint32_t* next_node = (level & 1) ? na : nb;
+        uint32_t* next_count = counts + level + 1;
+        for (uint32_t base = 4u * wid; base < ntasks; base += 4u * warps) {
+            const uint32_t i = base + ((threadIdx.x & 31u) >> 3);
+            const bool active = i < ntasks;
+            auto reserve = [&](uint32_t k) -> uint32_t {
+                const uint32_t b0 = atomicAdd(node_counter, k);
+                if ((unsigned long long)b0 + k > capacity) { raise_error(err, SQ_DEVERR_SAH_QUEUE); return 0u; }
+                return b0;
+            };
+            auto publish = [&](uint32_t node, uint32_t record) {
+                if (node >= capacity) return;
+                const uint32_t j = atomicAdd(next_count, 1u);
+                next_tasks[j] = record;
+                next_node[j] = node;
+            };
+            collapse_node_group(rec, leaf0, tris, active, active ? __ldcg(tasks + i) : 0u,
+                                active ? __ldcg(task_node + i) : 0u, nodes8, tris8, tri_counter, err,
+                                s_group[threadIdx.x >> 5], reserve, publish);
+        }
+        if (!grid_barrier(bar, gridDim.x, err)) return;
+    }
+}
+
+// Seed of the cooperative collapse: one root task (record `root`, node 0).
+__global__ void k_coop_seed(uint32_t* __restrict__ ws, uint32_t root, uint32_t capacity)
+{
+    uint32_t* counts = ws + 8;
+    uint32_t* ta = counts + kFixedLevels + 8;
+    ws[0] = 1u;       // node 0 is the root
+    ta[0] = root;
+    ta[capacity] = 0u;  // its node index (na[0])
+    counts[0] = 1u;
 }
 
 __global__ void k_fixed_seed(const uint32_t* __restrict__ roots, uint32_t nroots, uint32_t* __restrict__ tasks,
@@ -1384,7 +1512,7 @@ size_t bvh8_tri_bytes(uint32_t n) { return sizeof(float4) * 3ull * ((size_t)n + 
 // reads each level's task count from pinned memory).  ws: bvh8_ws_words(n)
 // words; host_ctl: pinned, 4 words.  Returns 0 or a cudaError_t; the node
 // count is host_ctl[0] and the number of levels host_ctl[3].
-int build_bvh8(const Node* rec, uint32_t root, uint32_t leaf0, const float* tris, uint32_t n, void* nodes8, void* tris8,
+static int build_bvh8_levels(const Node* rec, uint32_t root, uint32_t leaf0, const float* tris, uint32_t n, void* nodes8, void* tris8,
                uint32_t* ws, uint32_t* host_ctl, uint32_t* err, cudaStream_t s)
 {
     const uint32_t capacity = bvh8_capacity(n);
@@ -1403,7 +1531,7 @@ int build_bvh8(const Node* rec, uint32_t root, uint32_t leaf0, const float* tris
     while (ntasks) {
         ++levels;
         if ((e = cudaMemsetAsync(counters + 2, 0, 4, s)) != cudaSuccess) return (int)e;
-        k_collapse_level<<<(ntasks + 3) / 4, 128, 0, s>>>(rec, leaf0, tris, ta, na, ntasks,
+        k_collapse_level<<<(ntasks + 15) / 16, kCollapseBlock, 0, s>>>(rec, leaf0, tris, ta, na, ntasks,
                                                                static_cast<Node8*>(nodes8), static_cast<float4*>(tris8),
                                                                counters, tb, nb, capacity, err);
         if ((e = cudaMemcpyAsync(host_ctl, counters, 12, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return (int)e;
@@ -1413,6 +1541,35 @@ int build_bvh8(const Node* rec, uint32_t root, uint32_t leaf0, const float* tris
         std::swap(na, nb);
     }
     host_ctl[3] = levels;
+    return (int)cudaGetLastError();
+}
+
+int build_bvh8(const Node* rec, uint32_t root, uint32_t leaf0, const float* tris, uint32_t n, void* nodes8, void* tris8,
+               uint32_t* ws, uint32_t* host_ctl, uint32_t* err, cudaStream_t s)
+{
+    static int grid = -1;
+    if (grid < 0) {
+        int per_sm = 0, sms = 0, dev = 0, coop = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collapse_coop, 256, 0);
+        grid = (coop && per_sm > 0 && sms > 0) ? per_sm * sms : 0;
+    }
+    if (grid == 0) return build_bvh8_levels(rec, root, leaf0, tris, n, nodes8, tris8, ws, host_ctl, err, s);
+    const uint32_t capacity = bvh8_capacity(n);
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(ws, 0, sizeof(uint32_t) * (16 + kFixedLevels), s)) != cudaSuccess) return (int)e;
+    k_coop_seed<<<1, 1, 0, s>>>(ws, root, capacity);
+    void* args[] = {(void*)&rec, (void*)&leaf0, (void*)&tris, (void*)&ws, (void*)&capacity, (void*)&nodes8,
+                    (void*)&tris8, (void*)&err};
+    if ((e = cudaLaunchCooperativeKernel((const void*)k_collapse_coop, dim3(grid), dim3(256), args, 0, s)) !=
+        cudaSuccess)
+        return (int)e;
+    // node count -> host_ctl[0], levels -> host_ctl[3]
+    if ((e = cudaMemcpyAsync(host_ctl, ws, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return (int)e;
+    if ((e = cudaMemcpyAsync(host_ctl + 3, ws + 4, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return (int)e;
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return (int)e;
     return (int)cudaGetLastError();
 }
 
