@@ -36,7 +36,7 @@ namespace {
 using namespace sq;
 
 constexpr uint32_t kChunk = 2048;
-constexpr uint32_t kSmall = 1024;
+constexpr uint32_t kSmall = 128;
 constexpr int kMaxBins = 32;
 constexpr int kBinWords = 13;  // -pmin xyz, pmax xyz, -cmin xyz, cmax xyz (ordered ints), count
 constexpr int kStackDepth = 24;
