@@ -69,12 +69,14 @@ struct Error : std::runtime_error {
     Error(sq_status s, const std::string& m) : std::runtime_error(m), status(s) {}
 };
 
-// src/builder.h:78-104.  Builders with no GPU counterpart of their own build
-// the tree of the nearest one: horizontal -> the SAH tree of build_hierarchy
-// (the reference's horizontal top levels are a different split policy);
-// grid_sse and grid_m128 -> build_hierarchy_grid with each cell node bounded
-// by its own triangles (build_hierarchy_grid gives cell nodes the scene box,
-// src/builder.cpp:2173-2174, and the SIMD variants do not).
+// src/builder.h:78-104.  The reference's variants build the same logical
+// trees as the GPU builders they map to: build_hierarchy_horizontal bins its
+// top levels by a parallel reduction (src/builder.cpp:400-426, 1479-1574)
+// into the same bins as build_hierarchy, so it is the SAH tree; grid_sse and
+// grid_m128 are build_hierarchy_grid with each cell node bounded by its own
+// triangles (build_hierarchy_grid gives cell nodes the scene box,
+// src/builder.cpp:2173-2174).  Both equivalences are checked against the
+// reference's own trees.
 class Builder {
 public:
     static Hierarchy build_hierarchy(std::vector<Triangle>& primitives);

@@ -11,6 +11,8 @@ reference's own functions return for them:
   sah{8,16,32}_nodes / _root    Builder::build_hierarchy (src/builder.cpp:1576),
                                 only where the reference's tree is valid
   grid_nodes / grid_root        Builder::build_hierarchy_grid (src/builder.cpp:2133)
+  horizontal_*, grid_sse_*,     build_hierarchy_horizontal / _grid_sse / _grid_m128
+  grid_avx_*                    (src/builder.cpp:1621, 1993, 2064), where valid
   cam, w, h, heat               trace() heatmap on the 8-bin SAH tree
                                 (src/tracer.cpp:195)
   ref_hit, ref_tests            traverse() per ray     (src/tracer.cpp:47) for
@@ -63,6 +65,13 @@ def make(name, tris, w=160, h=120):
     if valid(gnodes, groot, n):
         out["grid_nodes"] = gnodes
         out["grid_root"] = np.uint32(groot)
+    # the builders the drop-in maps onto the ones above (horizontal -> SAH,
+    # grid_sse / grid_avx -> grid with cell nodes bounded by their triangles)
+    for key, kind in (("horizontal", "horizontal"), ("grid_sse", "grid_sse"), ("grid_avx", "grid_avx")):
+        knodes, kroot = O.ref_build(kind, tris, "b8")
+        if valid(knodes, kroot, n):
+            out[key + "_nodes"] = knodes
+            out[key + "_root"] = np.uint32(kroot)
     lo, hi = scenes.scene_box(tris)
     centre = (lo + hi) * np.float32(0.5)
     cam = np.array([centre[0], centre[1], np.float32(2) * lo[2] - centre[2]], np.float32)

@@ -68,6 +68,17 @@ def test_sah_matches_reference_golden(ctx, name):
         bvh = ctx.build(g["tris"], "grid", bins=8, leaf=8, flags=1)
         nodes, root = bvh.export_node1()
         assert canon(nodes, root) == canon(g["grid_nodes"], int(g["grid_root"]))
+    # the builders the C++ drop-in maps onto these (horizontal -> SAH,
+    # grid_sse / grid_m128 -> grid with cell nodes bounded by their triangles)
+    if "horizontal_nodes" in g:
+        bvh = ctx.build(g["tris"], "sah", bins=8, leaf=8)
+        nodes, root = bvh.export_node1()
+        assert canon(nodes, root) == canon(g["horizontal_nodes"], int(g["horizontal_root"]))
+    for key in ("grid_sse", "grid_avx"):
+        if key + "_nodes" in g:
+            bvh = ctx.build(g["tris"], "grid", bins=8, leaf=8, flags=0)
+            nodes, root = bvh.export_node1()
+            assert canon(nodes, root) == canon(g[key + "_nodes"], int(g[key + "_root"])), key
 
 
 def test_sah_soup_2m_32bins(ctx, oracle):

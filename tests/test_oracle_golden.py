@@ -78,3 +78,24 @@ def test_oracle_trees_valid(oracle, golden):
                   lambda t: oracle.build_grid(t, 8, 8)[:2]):
         nodes, root = build(golden["tris"])
         assert (oracle.leaf_reach(nodes, root, n) == 1).all()
+
+
+def test_mapped_builders_match_reference(oracle, golden):
+    """The drop-in builds the SAH tree for build_hierarchy_horizontal and the
+    grid tree with cell nodes bounded by their own triangles for
+    build_hierarchy_grid_sse / _grid_m128: the reference's own trees for those
+    builders are the same logical trees (where the reference's layout is
+    valid)."""
+    import sys
+    sys.setrecursionlimit(100000)
+    checked = 0
+    if "horizontal_nodes" in golden:
+        on, oroot, _ = oracle.build_sah(golden["tris"], 8, 8)
+        assert canon(golden["horizontal_nodes"], int(golden["horizontal_root"])) == canon(on, oroot)
+        checked += 1
+    for key in ("grid_sse", "grid_avx"):
+        if key + "_nodes" in golden:
+            on, oroot, _ = oracle.build_grid(golden["tris"], 8, 8, scene_bounds_cells=False)
+            assert canon(golden[key + "_nodes"], int(golden[key + "_root"])) == canon(on, oroot)
+            checked += 1
+    assert checked >= 1
