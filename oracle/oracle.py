@@ -61,6 +61,7 @@ def _declare(L):
         "sqo_trace": (i32, [vp, u32, vp, vp, u32, i32, vp, vp, vp]),
         "sqo_brute_closest": (None, [vp, u32, vp, u32, vp, vp]),
         "sqo_heatmap": (None, [vp, u32, vp]),
+        "sqo_trace_coherent": (i32, [vp, u32, u32, u32, vp, i32, u32, vp]),
         "sqo_reintersect_f64": (None, [vp, vp, u32, vp, vp]),
         "sqo_canonical_bfs": (u32, [vp, u32, u32, vp, u32]),
         "sqo_leaf_reach": (u32, [vp, u32, u32, u32, vp]),
@@ -192,6 +193,16 @@ def heatmap(tests):
     tests = np.ascontiguousarray(tests, np.uint32)
     rgb = np.empty(len(tests) * 3, np.uint8)
     lib().sqo_heatmap(_p(tests), len(tests), _p(rgb))
+    return rgb
+
+
+def trace_coherent(nodes, root, w, h, origin, bundle, k):
+    """trace_packet<k> / trace_bundle<k> heatmap bytes (w*h*3)."""
+    o = np.asarray(origin, np.float32)
+    rgb = np.zeros(w * h * 3, np.uint8)
+    rc = lib().sqo_trace_coherent(_p(np.ascontiguousarray(nodes)), root, w, h, _p(o), int(bundle), k, _p(rgb))
+    if rc != 0:
+        raise ValueError("sqo_trace_coherent failed (%d)" % rc)
     return rgb
 
 

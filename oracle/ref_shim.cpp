@@ -134,8 +134,9 @@ static Hierarchy make_h(Node1* nodes, uint32_t node_count, uint32_t root, std::v
     return h;
 }
 
-// trace (src/tracer.cpp:195) / trace_packet<8> / trace_bundle<64>.
-// tracer: 0 basic, 1 packet<8>, 2 bundle<64>.  img: w*h*3 bytes.
+// trace (src/tracer.cpp:195) / trace_packet<K> / trace_bundle<K>.
+// tracer: 0 basic, 1 packet<8>, 2 bundle<64>, 100 + K packet<K> (K = 1, 2,
+// 4, 8), 200 + K bundle<K> (K = 16, 64).  img: w*h*3 bytes.
 int ref_trace(int tracer, const Node1* nodes, uint32_t node_count, uint32_t root,
               const float* tris, uint32_t n, uint32_t w, uint32_t h, const float* origin,
               uint8_t* img)
@@ -149,6 +150,12 @@ int ref_trace(int tracer, const Node1* nodes, uint32_t node_count, uint32_t root
     case 0: r = trace(hh, w, h, o); break;
     case 1: r = trace_packet<8>(hh, w, h, o); break;
     case 2: r = trace_bundle<64>(hh, w, h, o); break;
+    case 101: r = trace_packet<1>(hh, w, h, o); break;
+    case 102: r = trace_packet<2>(hh, w, h, o); break;
+    case 104: r = trace_packet<4>(hh, w, h, o); break;
+    case 108: r = trace_packet<8>(hh, w, h, o); break;
+    case 216: r = trace_bundle<16>(hh, w, h, o); break;
+    case 264: r = trace_bundle<64>(hh, w, h, o); break;
     default: return 1;
     }
     memcpy(img, r, (size_t)w * h * 3);

@@ -970,6 +970,211 @@ int sqo_trace(const sqo_node1* nodes, uint32_t root, const float* tris,
     return err;
 }
 
+/* ---------------------------------------------------------------- packets */
+
+/* The reference camera ray through pixel (x, y), src/tracer.cpp:207-216
+ * (the same per-pixel arithmetic as trace_packet / trace_bundle,
+ * src/tracer.cpp:246-256, 323-329). */
+static inline void camera_dir(uint32_t x, uint32_t y, uint32_t w, uint32_t h, float d[3])
+{
+    float aspect = (float)w / (float)h;
+    float nx = (((float)x + 0.5f) / (float)w) * 2.0f - 1.0f;
+    float ny = (((float)y + 0.5f) / (float)h) * 2.0f - 1.0f;
+    nx = nx * aspect;
+    float l2 = nx * nx + ny * ny;
+    l2 = l2 + 1.0f * 1.0f;
+    float len = sqrtf(l2);
+    d[0] = nx / len;
+    d[1] = ny / len;
+    d[2] = 1.0f / len;
+}
+
+#define SQO_PACKET_STACK 128 /* src/tracer.cpp:94 */
+
+/* traverse_packet_stack (src/tracer.cpp:88-123) for a packet of k rays
+ * sharing origin o, starting at nodes [index, index + count): a node's
+ * children are visited when any ray of the packet hits the node's box; the
+ * packet counts one test per node box.  Triangle tests do not change the
+ * count.  Returns the count (or UINT32_MAX on a stack overflow). */
+static uint32_t packet_tests(const sqo_node1* nodes, uint32_t index, uint32_t count, const float* o,
+                             const float (*inv)[3], uint32_t k)
+{
+    uint32_t st_i[SQO_PACKET_STACK], st_c[SQO_PACKET_STACK];
+    uint32_t sp = 1, tests = 0;
+    st_i[0] = index;
+    st_c[0] = count;
+    while (sp > 0) {
+        --sp;
+        uint32_t bi = st_i[sp], bc = st_c[sp];
+        for (uint32_t c = 0; c < bc; ++c) {
+            const sqo_node1* nd = &nodes[bi + c];
+            int any = 0;
+            for (uint32_t r = 0; r < k; ++r) any |= box_ref(nd, o, inv[r], 10000.0f);
+            tests++;
+            if (any && !(nd->flags & 1u)) {
+                if (sp >= SQO_PACKET_STACK) return UINT32_MAX;
+                st_i[sp] = nd->child;
+                st_c[sp] = nd->count;
+                sp++;
+            }
+        }
+    }
+    return tests;
+}
+
+static inline uint8_t heat_byte(float tests)
+{
+    float x = tests / 200.0f;
+    float m = (x < 1.0f) ? x : 1.0f;
+    return (uint8_t)f2u(m * 255.0f);
+}
+
+/* trace_packet<k> (src/tracer.cpp:232-281): packets of k = kx * ky rays in
+ * kx x ky pixel blocks (kx = floor(sqrt(k))), rays in row order within the
+ * block; every pixel of a packet gets (tests / k) / 200 of the packet. */
+static int trace_packet_img(const sqo_node1* nodes, uint32_t root, uint32_t w, uint32_t h, const float o[3],
+                            uint32_t k, uint8_t* rgb)
+{
+    uint32_t kx = (uint32_t)floor(sqrt((double)k)), ky = k / kx;
+    int bad = 0;
+#pragma omp parallel for schedule(dynamic, 4) num_threads(sqo_get_threads())
+    for (long long jj = 0; jj < (long long)h; jj += ky) {
+        uint32_t j = (uint32_t)jj;
+        float inv[8][3];
+        for (uint32_t i = 0; i < w; i += kx) {
+            for (uint32_t m = 0; m < k; ++m) {
+                float d[3];
+                camera_dir(i + m % kx, j + m / kx, w, h, d);
+                for (int a = 0; a < 3; ++a) inv[m][a] = 1.0f / d[a];
+            }
+            uint32_t t = packet_tests(nodes, root, 1, o, (const float (*)[3])inv, k);
+            if (t == UINT32_MAX) bad = 1;
+            uint8_t b = heat_byte((float)t / (float)k);
+            for (uint32_t m = 0; m < k; ++m) {
+                size_t px = (size_t)(j + m / kx) * w + i + m % kx;
+                rgb[3 * px] = rgb[3 * px + 1] = rgb[3 * px + 2] = b;
+            }
+        }
+    }
+    return bad;
+}
+
+/* morton_lut (src/tracer.cpp:18-23): k with bits 1 and 2 exchanged */
+static inline uint32_t bundle_lut(uint32_t k) { return (k & ~6u) | ((k & 2u) << 1) | ((k & 4u) >> 1); }
+
+/* intersect_bundle_aabb (src/tracer.h:37-80): slabs of the box against the
+ * bundle's direction bounds (min, max and their midpoint) from its origin */
+static inline void bundle_box(const sqo_node1* nd, const float* pos, const float* imin, const float* imax,
+                              const float* imid, int* any_hit, int* mid_hit)
+{
+    float tmin_mid[3], tmin_any[3], tmax_mid[3], tmax_any[3];
+    for (int a = 0; a < 3; ++a) {
+        float lo = nd->min[a] - pos[a], hi = nd->max[a] - pos[a];
+        float t1a = lo * imin[a], t1b = lo * imax[a], t2a = hi * imin[a], t2b = hi * imax[a];
+        float t1 = lo * imid[a], t2 = hi * imid[a];
+        float t1min = rmin(t1a, t1b), t1max = smax(t1a, t1b);
+        float t2min = rmin(t2a, t2b), t2max = smax(t2a, t2b);
+        tmin_mid[a] = rmin(t1, t2);
+        tmin_any[a] = rmin(t1min, t2min);
+        tmax_mid[a] = smax(t1, t2);
+        tmax_any[a] = smax(t1max, t2max);
+    }
+    float front_mid = rmax(rmax(tmin_mid[0], tmin_mid[1]), tmin_mid[2]);
+    float front_any = rmax(rmax(tmin_any[0], tmin_any[1]), tmin_any[2]);
+    float back_mid = rmin(rmin(tmax_mid[0], tmax_mid[1]), tmax_mid[2]);
+    float back_any = rmin(rmin(tmax_any[0], tmax_any[1]), tmax_any[2]);
+    *mid_hit = back_mid >= front_mid;
+    *any_hit = back_any >= front_any;
+}
+
+/* trace_bundle<k> with packets of 8 (src/tracer.cpp:292-362, traverse_bundle
+ * 126-156): tiles of tw x th pixels (tw = floor(sqrt(k))), ray m*8 + n at
+ * tile position morton_lut[m*8 + n].  The bundle descends while its
+ * midpoint direction hits; where only some directions can hit, each packet
+ * of 8 continues alone from that node.  Pixel of packet m:
+ * bundle_tests / k + packet_tests[m] / 8. */
+static int trace_bundle_img(const sqo_node1* nodes, uint32_t root, uint32_t w, uint32_t h, const float o[3],
+                            uint32_t k, uint8_t* rgb)
+{
+    uint32_t tw = (uint32_t)floor(sqrt((double)k)), th = k / tw, np = k / 8;
+    int bad = 0;
+#pragma omp parallel for schedule(dynamic, 2) num_threads(sqo_get_threads())
+    for (long long jj = 0; jj < (long long)h; jj += th) {
+        uint32_t j = (uint32_t)jj;
+        float inv[64][3];
+        uint32_t px[64];
+        for (uint32_t i = 0; i < w; i += tw) {
+            float dmin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, dmax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+            for (uint32_t r = 0; r < k; ++r) {
+                uint32_t v = bundle_lut(r), x = i + v % tw, y = j + v / tw;
+                float d[3];
+                camera_dir(x, y, w, h, d);
+                for (int a = 0; a < 3; ++a) {
+                    inv[r][a] = 1.0f / d[a];
+                    dmin[a] = rmin(dmin[a], d[a]);
+                    dmax[a] = rmax(dmax[a], d[a]);
+                }
+                px[r] = y * w + x;
+            }
+            float imin[3], imax[3], imid[3];
+            for (int a = 0; a < 3; ++a) {
+                imin[a] = 1.0f / dmin[a];
+                imax[a] = 1.0f / dmax[a];
+                imid[a] = 1.0f / ((dmin[a] + dmax[a]) * 0.5f);
+            }
+            uint32_t btests = 0, ptests[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            uint32_t st_i[SQO_PACKET_STACK], st_c[SQO_PACKET_STACK], sp = 1;
+            st_i[0] = root;
+            st_c[0] = 1;
+            while (sp > 0) {
+                --sp;
+                uint32_t bi = st_i[sp], bc = st_c[sp];
+                for (uint32_t c = 0; c < bc; ++c) {
+                    const sqo_node1* nd = &nodes[bi + c];
+                    int any_hit, mid_hit;
+                    bundle_box(nd, o, imin, imax, imid, &any_hit, &mid_hit);
+                    btests++;
+                    if (mid_hit) {
+                        if (!(nd->flags & 1u)) {
+                            if (sp >= SQO_PACKET_STACK) { bad = 1; break; }
+                            st_i[sp] = nd->child;
+                            st_c[sp] = nd->count;
+                            sp++;
+                        }
+                    } else if (any_hit) {
+                        for (uint32_t m = 0; m < np; ++m) {
+                            uint32_t t = packet_tests(nodes, bi + c, 1, o, (const float (*)[3])(inv + 8 * m), 8);
+                            if (t == UINT32_MAX) bad = 1;
+                            else ptests[m] += t;
+                        }
+                    }
+                }
+            }
+            for (uint32_t r = 0; r < k; ++r) {
+                float t = (float)btests / (float)k + (float)ptests[r / 8] / 8.0f;
+                uint8_t b = heat_byte(t);
+                rgb[3 * (size_t)px[r]] = rgb[3 * (size_t)px[r] + 1] = rgb[3 * (size_t)px[r] + 2] = b;
+            }
+        }
+    }
+    return bad;
+}
+
+int sqo_trace_coherent(const sqo_node1* nodes, uint32_t root, uint32_t w, uint32_t h, const float origin[3],
+                       int bundle, uint32_t k, uint8_t* rgb)
+{
+    if (bundle) {
+        if (k != 16 && k != 64) return -1;
+        uint32_t tw = (uint32_t)floor(sqrt((double)k));
+        if (w % tw || h % (k / tw)) return -1;
+        return trace_bundle_img(nodes, root, w, h, origin, k, rgb);
+    }
+    if (k != 1 && k != 2 && k != 4 && k != 8) return -1;
+    uint32_t kx = (uint32_t)floor(sqrt((double)k));
+    if (w % kx || h % (k / kx)) return -1;
+    return trace_packet_img(nodes, root, w, h, origin, k, rgb);
+}
+
 void sqo_brute_closest(const float* tris, uint32_t n, const float* rays,
                        uint32_t nrays, uint32_t* ids, float* ts)
 {

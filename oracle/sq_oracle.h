@@ -113,6 +113,12 @@ void sqo_brute_closest(const float* tris, uint32_t n, const float* rays,
 
 /* Heatmap bytes (src/tracer.cpp:222-225): 3 bytes per ray */
 void sqo_heatmap(const uint32_t* tests, uint32_t n, uint8_t* rgb);
+/* trace_packet<k> (bundle = 0; k = 1, 2, 4, 8) or trace_bundle<k> (bundle =
+ * 1; k = 16, 64) heatmap of the reference camera at origin, w x h (w and h
+ * multiples of the packet or tile size).  Returns 0, 1 on a stack overflow,
+ * -1 on bad arguments. */
+int sqo_trace_coherent(const sqo_node1* nodes, uint32_t root, uint32_t w, uint32_t h, const float origin[3],
+                       int bundle, uint32_t k, uint8_t* rgb);
 
 /* FP64 re-intersection of hit (ray, triangle) pairs: t64 of the ray with the
  * triangle's plane, in double from the FP32 inputs.  NaN for misses.       */

@@ -15,6 +15,8 @@ reference's own functions return for them:
   grid_avx_*                    (src/builder.cpp:1621, 1993, 2064), where valid
   cam, w, h, heat               trace() heatmap on the 8-bin SAH tree
                                 (src/tracer.cpp:195)
+  packet{1,2,4,8}_heat,         trace_packet<k> / trace_bundle<k> heatmaps of
+  bundle{16,64}_heat            that tree and camera (src/tracer.cpp:232, 292)
   ref_hit, ref_tests            traverse() per ray     (src/tracer.cpp:47) for
                                 the reference-camera rays (regenerated by the
                                 oracle; trace()'s heatmap pins that generation)
@@ -79,6 +81,11 @@ def make(name, tris, w=160, h=120):
     assert valid(nodes, root, n), name
     out.update(cam=cam, w=np.uint32(w), h=np.uint32(h))
     out["heat"] = O.ref_trace(nodes, root, tris, w, h, cam, 0)
+    # trace_packet<k> / trace_bundle<k> heatmaps of the same tree and camera
+    for k in (1, 2, 4, 8):
+        out["packet%d_heat" % k] = O.ref_trace(nodes, root, tris, w, h, cam, 100 + k)
+    for k in (16, 64):
+        out["bundle%d_heat" % k] = O.ref_trace(nodes, root, tris, w, h, cam, 200 + k)
     rays = O.rays_reference_camera(w, h, cam)
     hit, tests = O.ref_traverse(nodes, root, tris, rays)
     out.update(ref_hit=hit, ref_tests=tests)

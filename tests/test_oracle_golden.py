@@ -1,6 +1,7 @@
 """The CPU oracle against golden outputs of the Sequoia reference itself
 (tests/golden, produced by tests/golden/make_golden.py)."""
 import numpy as np
+import pytest
 
 from conftest import load_golden
 
@@ -99,3 +100,13 @@ def test_mapped_builders_match_reference(oracle, golden):
             assert canon(golden[key + "_nodes"], int(golden[key + "_root"])) == canon(on, oroot)
             checked += 1
     assert checked >= 1
+
+
+@pytest.mark.parametrize("bundle,k", [(0, 1), (0, 2), (0, 4), (0, 8), (1, 16), (1, 64)])
+def test_packet_and_bundle_heatmaps(oracle, golden, bundle, k):
+    """trace_packet<k> / trace_bundle<k> (src/tracer.cpp:232-362): the
+    oracle's restatement gives the reference's heatmap bytes."""
+    w, h = int(golden["w"]), int(golden["h"])
+    key = ("bundle%d_heat" if bundle else "packet%d_heat") % k
+    got = oracle.trace_coherent(golden["sah8_nodes"], int(golden["sah8_root"]), w, h, golden["cam"], bundle, k)
+    assert np.array_equal(got, golden[key])
