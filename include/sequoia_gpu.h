@@ -146,8 +146,18 @@ typedef enum sq_trace_mode {
                              near-child order, no early exit, Moller-Trumbore
                              hit flag (src/tracer.cpp:47-65, src/tracer.h:12-116) */
     SQ_TRACE_CLOSEST = 1, /* near-child order, t shrink, watertight test         */
-    SQ_TRACE_ANYHIT = 2   /* as CLOSEST, stops at the first accepted hit         */
+    SQ_TRACE_ANYHIT = 2,  /* as CLOSEST, stops at the first accepted hit         */
+    SQ_TRACE_PACKET = 3,  /* trace_packet<k> (src/tracer.cpp:232-281): packets of
+                             k = 1, 2, 4 or 8 rays count box tests together;
+                             heatmap only (hits must be NULL), reference camera,
+                             width and height multiples of the packet block     */
+    SQ_TRACE_BUNDLE = 4   /* trace_bundle<k> (src/tracer.cpp:292-362): tiles of
+                             k = 16 or 64 rays tested as a bundle, split into
+                             packets of 8; same restrictions as PACKET          */
 } sq_trace_mode;
+/* The packet or bundle size k rides in bits 16..23 of the mode:
+ * SQ_TRACE_PACKET | SQ_TRACE_WIDTH(8), SQ_TRACE_BUNDLE | SQ_TRACE_WIDTH(64). */
+#define SQ_TRACE_WIDTH(k) ((uint32_t)(k) << 16)
 /* OR into the mode: trace the binary (Node1) tree even when the BVH also has
  * an 8-wide quantised tree.                                                  */
 #define SQ_TRACE_FORCE_BINARY 0x100u

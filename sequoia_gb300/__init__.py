@@ -19,7 +19,7 @@ import os
 
 import numpy as np
 
-__all__ = ["Context", "Bvh", "Hierarchy", "Builder", "trace", "traverse", "SequoiaError",
+__all__ = ["Context", "Bvh", "Hierarchy", "Builder", "trace", "trace_packet", "trace_bundle", "traverse", "SequoiaError",
            "NODE1", "HIT", "NO_HIT", "library_path", "load_library", "load_obj", "parse_obj",
            "encode_bmp", "write_bmp"]
 
@@ -29,7 +29,7 @@ NO_HIT = 0xFFFFFFFF
 NODE1 = np.dtype([("min", "<f4", 3), ("count", "<u2"), ("flags", "<u2"), ("max", "<f4", 3), ("child", "<u4")])
 HIT = np.dtype([("id", "<u4"), ("t", "<f4"), ("tests", "<u4")])
 
-MODES = {"ref": 0, "closest": 1, "anyhit": 2}
+MODES = {"ref": 0, "closest": 1, "anyhit": 2, "packet": 3, "bundle": 4}
 BUILDERS = {"morton": 0, "sah": 1, "recursive": 1, "grid": 2}
 STATUS = {0: "OK", 1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "device error",
           5: "unsupported", 6: "no CUDA device", 7: "exceeds a fixed capacity"}
@@ -342,14 +342,18 @@ class Context:
         return src, width * height
 
     def trace(self, bvh, mode="closest", rays=None, camera=None, width=0, height=0, origin=(0, 0, 0),
-              target=(0, 0, -1), up=(0, 1, 0), vfov=60.0, hits=True, heatmap=False, binary=False):
+              target=(0, 0, -1), up=(0, 1, 0), vfov=60.0, hits=True, heatmap=False, binary=False, k=0):
         """Trace rays; returns (hits structured array or None, heatmap bytes or None).
         `hits` / `heatmap` may also be device buffers to write into.  `binary`
-        forces the binary tree when the BVH also has an 8-wide one."""
+        forces the binary tree when the BVH also has an 8-wide one.  Modes
+        "packet" and "bundle" (trace_packet<k> / trace_bundle<k>) take the
+        packet size `k`, the reference camera and produce the heatmap only."""
+        if mode in ("packet", "bundle"):
+            hits, heatmap = False, (True if heatmap is False else heatmap)
         src, count = self._ray_source(rays, camera, width, height, origin, target, up, vfov)
         h_arr = np.empty(count, HIT) if hits is True else (hits if hits is not False else None)
         m_arr = np.empty(count * 3, np.uint8) if heatmap is True else (heatmap if heatmap is not False else None)
-        m = MODES[mode] | (0x100 if binary else 0)
+        m = MODES[mode] | (0x100 if binary else 0) | (int(k) << 16)
         self._check(load_library().sq_trace(self.handle, bvh.handle, C.byref(src), m, _addr(h_arr), _addr(m_arr)))
         return h_arr, m_arr
 
@@ -452,6 +456,22 @@ def trace(hierarchy, w, h, origin):
     ctx, bvh = _bvh_of(hierarchy)
     _, heat = ctx.trace(bvh, mode="ref", camera="reference", width=w, height=h, origin=origin,
                         hits=False, heatmap=True)
+    return heat
+
+
+def trace_packet(hierarchy, w, h, origin, k=8):
+    """trace_packet<k> (src/tracer.cpp:232-281): the heatmap bytes of packets
+    of k rays (1, 2, 4 or 8) counting box tests together."""
+    ctx, bvh = _bvh_of(hierarchy)
+    _, heat = ctx.trace(bvh, mode="packet", k=k, camera="reference", width=w, height=h, origin=origin)
+    return heat
+
+
+def trace_bundle(hierarchy, w, h, origin, k=64):
+    """trace_bundle<k> (src/tracer.cpp:292-362): the heatmap bytes of bundles
+    of k rays (16 or 64) split into packets of 8."""
+    ctx, bvh = _bvh_of(hierarchy)
+    _, heat = ctx.trace(bvh, mode="bundle", k=k, camera="reference", width=w, height=h, origin=origin)
     return heat
 
 

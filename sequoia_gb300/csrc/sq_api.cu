@@ -522,8 +522,23 @@ sq_status sq_trace(sq_ctx* c, const sq_bvh* b, const sq_ray_source* rays, uint32
 {
     if (!c || !b || !rays) return fail(c, SQ_ERR_INVALID, "sq_trace: null argument");
     const bool force_binary = (mode & SQ_TRACE_FORCE_BINARY) != 0;
-    mode &= ~SQ_TRACE_FORCE_BINARY;
-    if (mode > SQ_TRACE_ANYHIT) return fail(c, SQ_ERR_INVALID, "sq_trace: unknown mode %u", mode);
+    const uint32_t width_k = (mode >> 16) & 0xFFu;
+    mode &= 0xFFu;
+    if (mode > SQ_TRACE_BUNDLE) return fail(c, SQ_ERR_INVALID, "sq_trace: unknown mode %u", mode);
+    const bool coherent = mode == SQ_TRACE_PACKET || mode == SQ_TRACE_BUNDLE;
+    if (coherent) {
+        // trace_packet<k> / trace_bundle<k>: the reference camera, heatmap only
+        if (rays->kind != SQ_RAYS_REFERENCE_CAMERA)
+            return fail(c, SQ_ERR_INVALID, "sq_trace: packet and bundle modes trace the reference camera");
+        if (hits) return fail(c, SQ_ERR_UNSUPPORTED, "sq_trace: packet and bundle modes produce the heatmap only");
+        if (!heatmap_rgb) return fail(c, SQ_ERR_INVALID, "sq_trace: packet and bundle modes need a heatmap");
+        if (!sqk::coherent_shape_ok(mode == SQ_TRACE_BUNDLE, width_k, rays->width, rays->height))
+            return fail(c, SQ_ERR_INVALID,
+                        "sq_trace: %s width %u needs an image made of whole packet blocks (got %ux%u)",
+                        mode == SQ_TRACE_BUNDLE ? "bundle" : "packet", width_k, rays->width, rays->height);
+    } else if (width_k) {
+        return fail(c, SQ_ERR_INVALID, "sq_trace: a width applies to packet and bundle modes only");
+    }
     Guard g(c->device);
     sqk::TraceArgs a;
     memset(&a, 0, sizeof a);
@@ -604,7 +619,9 @@ sq_status sq_trace(sq_ctx* c, const sq_bvh* b, const sq_ray_source* rays, uint32
     SQ_CUDA(c, cudaMemsetAsync(c->ctrl + 1, 0, 11 * sizeof(uint32_t), s));
     SQ_CUDA(c, cudaEventRecord(c->ev[4], s));
     if (count > 0) {
-        if (b->nodes8 && mode != SQ_TRACE_REF && !force_binary) {
+        if (coherent) {
+            sqk::trace_coherent(a, mode == SQ_TRACE_BUNDLE, width_k, s);
+        } else if (b->nodes8 && mode != SQ_TRACE_REF && !force_binary) {
             sqk::Trace8Args w;
             memset(&w, 0, sizeof w);
             w.nodes = b->nodes8;

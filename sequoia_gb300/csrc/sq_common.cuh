@@ -198,6 +198,9 @@ struct TraceArgs {
     unsigned long long* stats;  // {box tests, triangle tests, bytes requested, node visits}
 };
 void trace(const TraceArgs& a, cudaStream_t s);
+// packet / bundle tracers of the reference (sq_coherent.cu): heatmap only
+bool coherent_shape_ok(uint32_t bundle, uint32_t k, uint32_t w, uint32_t h);
+void trace_coherent(const TraceArgs& a, uint32_t bundle, uint32_t k, cudaStream_t s);
 
 // 8-wide quantised BVH (sq_bvh8.cu)
 struct Trace8Args {

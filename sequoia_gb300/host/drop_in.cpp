@@ -164,10 +164,11 @@ Hierarchy Builder::build_hierarchy_morton2(std::vector<Triangle>&)
     throw Error(SQ_ERR_UNSUPPORTED, "sequoia: 64-bit Morton codes (build_hierarchy_morton2) are not implemented");
 }
 
-uint8_t* trace(Hierarchy& hierarchy, uint32_t w, uint32_t h, vec3f1 origin)
+namespace {
+
+// The device tree of a Hierarchy: the one Builder made, else an upload.
+sq_bvh* tree_locked(sq_ctx* c, Hierarchy& hierarchy)
 {
-    std::lock_guard<std::mutex> lock(g_mu);
-    sq_ctx* c = ctx_locked();
     sq_bvh* bvh = lookup_locked(hierarchy);
     if (!bvh) {
         check(sq_bvh_import_node1(c, reinterpret_cast<const sq_node1*>(hierarchy.node_base), hierarchy.node_count,
@@ -176,6 +177,14 @@ uint8_t* trace(Hierarchy& hierarchy, uint32_t w, uint32_t h, vec3f1 origin)
               "sq_bvh_import_node1");
         remember_locked(hierarchy, bvh);
     }
+    return bvh;
+}
+
+uint8_t* camera_trace(Hierarchy& hierarchy, uint32_t w, uint32_t h, vec3f1 origin, uint32_t mode)
+{
+    std::lock_guard<std::mutex> lock(g_mu);
+    sq_ctx* c = ctx_locked();
+    sq_bvh* bvh = tree_locked(c, hierarchy);
     sq_ray_source rs;
     memset(&rs, 0, sizeof(rs));
     rs.kind = SQ_RAYS_REFERENCE_CAMERA;
@@ -185,12 +194,24 @@ uint8_t* trace(Hierarchy& hierarchy, uint32_t w, uint32_t h, vec3f1 origin)
     rs.origin[1] = origin.y;
     rs.origin[2] = origin.z;
     uint8_t* image = new uint8_t[3ull * w * h];
-    const sq_status s = sq_trace(c, bvh, &rs, SQ_TRACE_REF, nullptr, image);
+    const sq_status s = sq_trace(c, bvh, &rs, mode, nullptr, image);
     if (s != SQ_OK) {
         delete[] image;
         check(s, "sq_trace");
     }
     return image;
+}
+
+}  // namespace
+
+uint8_t* trace(Hierarchy& hierarchy, uint32_t w, uint32_t h, vec3f1 origin)
+{
+    return camera_trace(hierarchy, w, h, origin, SQ_TRACE_REF);
+}
+
+uint8_t* trace_coherent(Hierarchy& hierarchy, uint32_t w, uint32_t h, vec3f1 origin, bool bundle, uint32_t k)
+{
+    return camera_trace(hierarchy, w, h, origin, (bundle ? SQ_TRACE_BUNDLE : SQ_TRACE_PACKET) | SQ_TRACE_WIDTH(k));
 }
 
 std::vector<Triangle> loadOBJFromFile(std::string filename)

@@ -92,18 +92,20 @@ public:
 // per-ray box-test count as a grey heatmap (new[]'d, w*h*3 bytes).
 uint8_t* trace(Hierarchy& hierarchy, uint32_t w, uint32_t h, vec3f1 origin);
 
-// src/tracer.h:131-135.  The reference's packet and bundle tracers count box
-// tests per packet, so their heatmaps differ from trace()'s; on the GPU every
-// warp is already a 32-ray packet, and these return trace()'s image.
+// src/tracer.h:131-135: the packet (K = 1, 2, 4, 8) and bundle (K = 16, 64)
+// tracers, whose heatmaps count box tests per packet / bundle exactly as the
+// reference's do (the same bytes).  w and h must be multiples of the packet
+// block (the reference writes outside the image otherwise).
+uint8_t* trace_coherent(Hierarchy& hierarchy, uint32_t w, uint32_t h, vec3f1 origin, bool bundle, uint32_t k);
 template <size_t K>
 uint8_t* trace_packet(Hierarchy& hierarchy, uint32_t w, uint32_t h, vec3f1 origin)
 {
-    return trace(hierarchy, w, h, origin);
+    return trace_coherent(hierarchy, w, h, origin, false, (uint32_t)K);
 }
 template <size_t K>
 uint8_t* trace_bundle(Hierarchy& hierarchy, uint32_t w, uint32_t h, vec3f1 origin)
 {
-    return trace(hierarchy, w, h, origin);
+    return trace_coherent(hierarchy, w, h, origin, true, (uint32_t)K);
 }
 
 // src/main.cpp:108-179, with the same parse (sq_obj_load); prints the same

@@ -65,7 +65,7 @@ void usage()
     printf("                recursive, horizontal : binned SAH (GPU breadth-first)\n");
     printf("                grid, grid_sse, grid_avx : 4x4x4 grid of per-cell SAH builds\n");
     printf("                morton         : 30-bit Morton codes, radix sort, LBVH\n");
-    printf("            -tracer  <type> : basic | packet <n> | bundle <n> (all run the GPU tracer)\n");
+    printf("            -tracer  <type> : basic | packet <n> (1, 2, 4, 8) | bundle <n> (16, 64)\n");
     printf("            -threads <n>    : threads of the OBJ parse\n");
     printf("            -res <x> <y>    : output resolution\n");
     printf("            -benchmark      : time every builder and tracer\n");
@@ -116,9 +116,8 @@ Arguments parse_arguments(int argc, char** argv)
             } else if (v == "packet") {
                 a.tracer = TracerType::packet;
                 a.packet_width = (uint32_t)atoi(need(i, argc, argv));
-                if (a.packet_width != 1 && a.packet_width != 2 && a.packet_width != 4 && a.packet_width != 8 &&
-                    a.packet_width != 16)
-                    bad("packet width must be 1, 2, 4, 8 or 16");
+                if (a.packet_width != 1 && a.packet_width != 2 && a.packet_width != 4 && a.packet_width != 8)
+                    bad("packet width must be 1, 2, 4 or 8");
             } else if (v == "bundle") {
                 a.tracer = TracerType::bundle;
                 a.bundle_width = (uint32_t)atoi(need(i, argc, argv));
@@ -191,7 +190,23 @@ vec3f1 reference_camera(const std::vector<Triangle>& prims)
 
 uint8_t* run_tracer(const Arguments& a, Hierarchy& h, vec3f1 camera)
 {
-    if (a.mode == SQ_TRACE_REF) return trace(h, a.w, a.h, camera);
+    if (a.mode == SQ_TRACE_REF) {
+        // src/main.cpp:279-300
+        switch (a.tracer) {
+        case TracerType::basic: return trace(h, a.w, a.h, camera);
+        case TracerType::packet:
+            switch (a.packet_width) {
+            case 1: return trace_packet<1>(h, a.w, a.h, camera);
+            case 2: return trace_packet<2>(h, a.w, a.h, camera);
+            case 4: return trace_packet<4>(h, a.w, a.h, camera);
+            case 8: return trace_packet<8>(h, a.w, a.h, camera);
+            default: throw Error(SQ_ERR_INVALID, "invalid packet width (1, 2, 4 or 8)");
+            }
+        case TracerType::bundle:
+            if (a.bundle_width == 16) return trace_bundle<16>(h, a.w, a.h, camera);
+            return trace_bundle<64>(h, a.w, a.h, camera);
+        }
+    }
     sq_bvh* bvh = device_tree(h);
     if (!bvh) throw Error(SQ_ERR_INVALID, "no device tree for this hierarchy");
     sq_ray_source rs;
@@ -277,7 +292,12 @@ void benchmark(const Arguments& a)
     ta.h = hh;
     double twall[3], tdev[3];
     uint8_t* img[3];
+    // basic, packet<8>, bundle<64> (src/main.cpp:368-373)
+    const TracerType kinds[3] = {TracerType::basic, TracerType::packet, TracerType::bundle};
+    ta.packet_width = 8;
+    ta.bundle_width = 64;
     for (int k = 0; k < 3; ++k) {
+        ta.tracer = kinds[k];
         const double t = now_ms();
         img[k] = run_tracer(ta, sah, camera);
         twall[k] = now_ms() - t;

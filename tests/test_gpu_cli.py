@@ -77,3 +77,16 @@ def test_cli_benchmark_mode(lib_built, tmp_path):
     assert "build time" in out and "mrps" in out
     for k in (1, 2, 3):
         assert (tmp_path / ("benchmark%d.bmp" % k)).stat().st_size == 54 + 1920 * 3 * 1080
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tracer,k", [("packet", 8), ("packet", 4), ("bundle", 64), ("bundle", 16)])
+def test_cli_packet_bundle_render_matches_reference(lib_built, tmp_path, tracer, k):
+    """-tracer packet <k> / bundle <k>: the reference's images of the same
+    scene, byte for byte."""
+    import sequoia_gb300 as sq
+    g = load_golden("ico4")
+    w, h = int(g["w"]), int(g["h"])
+    _run(tmp_path, _obj(tmp_path, g["tris"]), "-builder", "recursive", "-tracer", tracer, str(k), "-res", str(w),
+         str(h))
+    assert (tmp_path / "render.bmp").read_bytes() == sq.encode_bmp(g["%s%d_heat" % (tracer, k)], w, h)

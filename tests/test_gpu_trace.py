@@ -101,3 +101,48 @@ def test_closest_t_vs_fp64(ctx, oracle):
     rel = np.abs(hits["t"][m].astype(np.float64) - t64[m]) / np.abs(t64[m])
     print("t error vs FP64 re-intersection: max %.3g, mean %.3g relative over %d hits" % (rel.max(), rel.mean(), m.sum()))
     assert rel.max() < 1e-5
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["ico3", "ico4", "soup3k", "dups2k"])
+@pytest.mark.parametrize("mode,k", [("packet", 1), ("packet", 2), ("packet", 4), ("packet", 8),
+                                    ("bundle", 16), ("bundle", 64)])
+def test_packet_bundle_heatmap_golden(ctx, name, mode, k):
+    """trace_packet<k> / trace_bundle<k> on the reference's own SAH tree: the
+    reference's heatmap bytes (tests/golden)."""
+    from conftest import load_golden
+    g = load_golden(name)
+    w, h = int(g["w"]), int(g["h"])
+    bvh = ctx.import_node1(g["sah8_nodes"], int(g["sah8_root"]), g["tris"])
+    _, heat = ctx.trace(bvh, mode, k=k, camera="reference", width=w, height=h, origin=g["cam"])
+    assert np.array_equal(heat, g["%s%d_heat" % (mode, k)])
+    assert ctx.sync() == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode,k", [("packet", 8), ("bundle", 64), ("bundle", 16), ("packet", 2)])
+def test_packet_bundle_matches_oracle_large(ctx, oracle, mode, k):
+    """A GPU-built SAH tree of the level-6 icosphere at 640x480, against the
+    oracle's restatement of the reference's packet / bundle tracers."""
+    from sequoia_gb300 import scenes
+    tris = scenes.displaced_icosphere(6, seed=1)
+    bvh = ctx.build(tris, "sah", bins=8, leaf=8)
+    nodes, root = bvh.export_node1()
+    lo, hi = scenes.scene_box(tris)
+    c = (lo + hi) * np.float32(0.5)
+    cam = np.array([c[0], c[1], np.float32(2) * lo[2] - c[2]], np.float32)
+    w, h = 640, 480
+    _, heat = ctx.trace(bvh, mode, k=k, camera="reference", width=w, height=h, origin=cam)
+    want = oracle.trace_coherent(nodes, root, w, h, cam, mode == "bundle", k)
+    assert np.array_equal(heat, want)
+
+
+@pytest.mark.gpu
+def test_packet_bundle_argument_checks(ctx):
+    import sequoia_gb300 as sq
+    from sequoia_gb300 import scenes
+    tris = scenes.displaced_icosphere(3, seed=1)
+    bvh = ctx.build(tris, "sah")
+    for mode, k, w, h in (("packet", 3, 64, 64), ("packet", 8, 63, 64), ("bundle", 64, 64, 60), ("bundle", 8, 64, 64)):
+        with pytest.raises(sq.SequoiaError):
+            ctx.trace(bvh, mode, k=k, camera="reference", width=w, height=h, origin=(0, 0, -3))
