@@ -51,6 +51,11 @@ def _declare(L):
         "sqo_bit_interleave_32": (u32, [u32, u32, u32]),
         "sqo_sort_pairs": (None, [vp, vp, u32, u32, u32]),
         "sqo_find_split_morton": (u32, [vp, u32]),
+        "sqo_bit_interleave_64": (C.c_uint64, [C.c_uint64, C.c_uint64, C.c_uint64]),
+        "sqo_morton_codes64": (None, [vp, u32, i32, vp, vp]),
+        "sqo_sort_pairs64": (None, [vp, vp, u32]),
+        "sqo_find_split_morton64": (u32, [vp, u32]),
+        "sqo_build_morton64": (u32, [vp, u32, i32, vp, vp, vp]),
         "sqo_node_capacity": (u32, [u32, i32]),
         "sqo_build_morton": (u32, [vp, u32, i32, vp, vp, vp]),
         "sqo_build_sah": (u32, [vp, u32, u32, u32, vp, vp]),
@@ -108,6 +113,36 @@ def sort_pairs(keys, values, key_bits=32, digit_bits=8):
 def find_split_morton(codes):
     codes = np.ascontiguousarray(codes, np.uint32)
     return int(lib().sqo_find_split_morton(_p(codes), len(codes)))
+
+
+def morton_codes64(tris, bounds_mode=0):
+    tris = _tris(tris)
+    codes = np.empty(len(tris), np.uint64)
+    box = np.empty(6, np.float32)
+    lib().sqo_morton_codes64(_p(tris), len(tris), bounds_mode, _p(codes), _p(box))
+    return codes, box
+
+
+def sort_pairs64(keys, values):
+    k = np.array(keys, np.uint64, copy=True)
+    v = np.array(values, np.uint32, copy=True)
+    lib().sqo_sort_pairs64(_p(k), _p(v), len(k))
+    return k, v
+
+
+def find_split_morton64(codes):
+    codes = np.ascontiguousarray(codes, np.uint64)
+    return int(lib().sqo_find_split_morton64(_p(codes), len(codes)))
+
+
+def build_morton64(tris, bounds_mode=0):
+    tris = _tris(tris)
+    n = len(tris)
+    nodes = np.zeros(node_capacity(n, 0), NODE1)
+    codes = np.empty(n, np.uint64)
+    perm = np.empty(n, np.uint32)
+    root = lib().sqo_build_morton64(_p(tris), n, bounds_mode, _p(nodes), _p(codes), _p(perm))
+    return nodes, int(root), codes, perm
 
 
 def node_capacity(n, kind):
@@ -233,7 +268,8 @@ def leaf_reach(nodes, root, n):
 
 # ---------------------------------------------------------------- reference
 
-REF_BUILDERS = {"recursive": 0, "horizontal": 1, "grid": 2, "grid_sse": 3, "grid_avx": 4, "morton": 5}
+REF_BUILDERS = {"recursive": 0, "horizontal": 1, "grid": 2, "grid_sse": 3, "grid_avx": 4, "morton": 5,
+                "morton2": 6}
 _refs = {}
 
 
@@ -259,6 +295,10 @@ def ref(variant="b8"):
         L.ref_load_obj.restype = u32
         L.ref_write_bmp.argtypes = [C.c_char_p, u32, u32, vp]
         L.ref_write_bmp.restype = i32
+        L.ref_setup_morton2.argtypes = [vp, u32, vp, vp, vp]
+        L.ref_radix_sort64.argtypes = [vp, vp, u32]
+        L.ref_find_split_morton2.argtypes = [vp, u32]
+        L.ref_find_split_morton2.restype = u32
         _refs[variant] = L
     return _refs[variant]
 
@@ -271,6 +311,28 @@ def ref_setup_morton(tris, variant="b8"):
     box = np.empty(6, np.float32)
     ref(variant).ref_setup_morton(_p(tris), n, _p(codes), _p(index), _p(box))
     return codes, index, box
+
+
+def ref_setup_morton2(tris, variant="b8"):
+    tris = _tris(tris)
+    n = len(tris)
+    codes = np.empty(n, np.uint64)
+    index = np.empty(n, np.uint32)
+    box = np.empty(6, np.float32)
+    ref(variant).ref_setup_morton2(_p(tris), n, _p(codes), _p(index), _p(box))
+    return codes, index, box
+
+
+def ref_radix_sort64(codes, index, variant="b8"):
+    c = np.array(codes, np.uint64, copy=True)
+    i = np.array(index, np.uint32, copy=True)
+    ref(variant).ref_radix_sort64(_p(c), _p(i), len(c))
+    return c, i
+
+
+def ref_find_split_morton2(codes, variant="b8"):
+    codes = np.ascontiguousarray(codes, np.uint64)
+    return int(ref(variant).ref_find_split_morton2(_p(codes), len(codes)))
 
 
 def ref_radix_sort(codes, index, variant="b8"):

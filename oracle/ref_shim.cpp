@@ -28,8 +28,18 @@ typedef struct alignas(8) RadixInput32 {
     __forceinline bool operator<(const RadixInput32& m) const { return code < m.code; }
 } RadixInput32;
 
+// Same layout and name as the 64-bit record of src/builder.cpp:2239-2245.
+typedef struct alignas(16) RadixInput64 {
+    uint64_t code;
+    unsigned index;
+    __forceinline operator uint64_t() const { return code; }
+    __forceinline bool operator<(const RadixInput64& m) const { return code < m.code; }
+} RadixInput64;
+
 void setup_morton(std::vector<Triangle>& primitives, std::vector<RadixInput32>& morton_codes, AABB1& scene_aabb);
 unsigned find_split_morton(std::vector<RadixInput32>::iterator begin, std::vector<RadixInput32>::iterator end);
+void setup_morton2(std::vector<Triangle>& primitives, std::vector<RadixInput64>& morton_codes, AABB1& scene_aabb);
+unsigned find_split_morton2(std::vector<RadixInput64>::iterator begin, std::vector<RadixInput64>::iterator end);
 std::vector<Triangle> loadOBJFromFile(std::string filename);
 // stb_image_write v1.14 as compiled into the reference's main.cpp
 extern "C" int stbi_write_bmp(char const* filename, int w, int h, int comp, const void* data);
@@ -78,8 +88,38 @@ uint32_t ref_find_split_morton(const uint32_t* codes, uint32_t count)
     return find_split_morton(mc.begin(), mc.end());
 }
 
+// setup_morton2 (src/builder.cpp:2247-2279): 60-bit codes and the scene box
+void ref_setup_morton2(const float* tris, uint32_t n, uint64_t* codes, uint32_t* index, float* scene)
+{
+    std::vector<Triangle> v = to_tris(tris, n);
+    std::vector<RadixInput64> mc(n);
+    AABB1 box;
+    setup_morton2(v, mc, box);
+    for (uint32_t i = 0; i < n; ++i) { codes[i] = mc[i].code; index[i] = mc[i].index; }
+    scene[0] = box.min.x; scene[1] = box.min.y; scene[2] = box.min.z;
+    scene[3] = box.max.x; scene[4] = box.max.y; scene[5] = box.max.z;
+}
+
+// radix_sort<uint64_t, RadixInput64>(..., 8) as build_hierarchy_morton2 calls it
+void ref_radix_sort64(uint64_t* codes, uint32_t* index, uint32_t n)
+{
+    std::vector<RadixInput64> mc(n), scratch(n);
+    for (uint32_t i = 0; i < n; ++i) { mc[i].code = codes[i]; mc[i].index = index[i]; }
+    radix_sort<uint64_t, RadixInput64>(mc.begin(), mc.end(), scratch.begin(), scratch.end(), 8);
+    for (uint32_t i = 0; i < n; ++i) { codes[i] = mc[i].code; index[i] = mc[i].index; }
+}
+
+// find_split_morton2 over codes[0..count)
+uint32_t ref_find_split_morton2(const uint64_t* codes, uint32_t count)
+{
+    std::vector<RadixInput64> mc(count);
+    for (uint32_t i = 0; i < count; ++i) { mc[i].code = codes[i]; mc[i].index = i; }
+    return find_split_morton2(mc.begin(), mc.end());
+}
+
 // Builders.  kind: 0 recursive, 1 horizontal, 2 grid, 3 grid_sse,
-// 4 grid_m128 ("grid_avx"), 5 morton.  Copies min(cap, node_count) records.
+// 4 grid_m128 ("grid_avx"), 5 morton, 6 morton2.  Copies min(cap, node_count)
+// records.
 int ref_build(int kind, const float* tris, uint32_t n, Node1* out, uint32_t cap,
               uint32_t* node_count, uint32_t* root)
 {
@@ -93,6 +133,7 @@ int ref_build(int kind, const float* tris, uint32_t n, Node1* out, uint32_t cap,
     case 3: h = Builder::build_hierarchy_grid_sse(v); count += 128; break;
     case 4: h = Builder::build_hierarchy_grid_m128(v); count += 128; break;
     case 5: h = Builder::build_hierarchy_morton(v); break;
+    case 6: h = Builder::build_hierarchy_morton2(v); break;
     default: return 1;
     }
     uint32_t m = count < cap ? count : cap;

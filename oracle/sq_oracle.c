@@ -194,6 +194,60 @@ void sqo_morton_codes(const float* tris, uint32_t n, int bounds_mode,
     }
 }
 
+/* 64-bit codes (build_hierarchy_morton2): _pdep_u64 with masks
+ * 0x9249249249249249 / 0x2492492492492492 / 0x4924924924924924
+ * (src/algorithms.cpp:16-22) on 20-bit inputs.                             */
+static inline uint64_t spread3_64(uint64_t v, int first)
+{
+    uint64_t r = 0;
+    for (int i = 0; i < 22; ++i)
+        if ((v >> i) & 1u) {
+            int pos = first + 3 * i;
+            if (pos < 64) r |= (uint64_t)1 << pos;
+        }
+    return r;
+}
+
+uint64_t sqo_bit_interleave_64(uint64_t x, uint64_t y, uint64_t z)
+{
+    return spread3_64(x, 0) | spread3_64(y, 1) | spread3_64(z, 2);
+}
+
+/* setup_morton2 (src/builder.cpp:2247-2279): as sqo_morton_codes with
+ * 0xFFFFF steps per axis */
+void sqo_morton_codes64(const float* tris, uint32_t n, int bounds_mode, uint64_t* codes, float* scene_box)
+{
+    box s;
+    box_reset(&s);
+    for (uint32_t i = 0; i < n; ++i) {
+        box b;
+        tri_box(tris + 9 * (size_t)i, &b);
+        if (bounds_mode == 1) {
+            float c[3];
+            box_centre(&b, c);
+            box_grow_pt(&s, c);
+        } else {
+            box_grow_box(&s, &b);
+        }
+    }
+    if (scene_box) { memcpy(scene_box, s.mn, 12); memcpy(scene_box + 3, s.mx, 12); }
+    float ext[3];
+    for (int k = 0; k < 3; ++k) ext[k] = s.mx[k] - s.mn[k];
+#pragma omp parallel for schedule(static) num_threads(sqo_get_threads())
+    for (long long i = 0; i < (long long)n; ++i) {
+        box b;
+        tri_box(tris + 9 * (size_t)i, &b);
+        float c[3];
+        box_centre(&b, c);
+        uint64_t q[3];
+        for (int k = 0; k < 3; ++k) {
+            float u = (c[k] - s.mn[k]) / ext[k];
+            q[k] = f2u(u * 1048575.0f);
+        }
+        codes[i] = sqo_bit_interleave_64(q[0], q[1], q[2]);
+    }
+}
+
 /* ------------------------------------------------------------------------- */
 /* stable LSD radix sort (src/algorithms.h:41-113)                           */
 
@@ -232,6 +286,33 @@ void sqo_sort_pairs(uint32_t* keys, uint32_t* values, uint32_t n,
     free(cnt);
 }
 
+/* radix_sort<uint64_t, RadixInput64>(..., 8): stable LSD over 64-bit keys */
+void sqo_sort_pairs64(uint64_t* keys, uint32_t* values, uint32_t n)
+{
+    if (n < 2) return;
+    uint64_t* k2 = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)n);
+    uint32_t* v2 = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)n);
+    uint32_t cnt[256];
+    uint64_t *ks = keys, *kd = k2;
+    uint32_t *vs = values, *vd = v2;
+    for (uint32_t shift = 0; shift < 64; shift += 8) {
+        memset(cnt, 0, sizeof cnt);
+        for (uint32_t i = 0; i < n; ++i) cnt[(ks[i] >> shift) & 255u]++;
+        uint32_t sum = 0;
+        for (uint32_t d = 0; d < 256; ++d) { uint32_t c = cnt[d]; cnt[d] = sum; sum += c; }
+        for (uint32_t i = 0; i < n; ++i) {
+            uint32_t p = cnt[(ks[i] >> shift) & 255u]++;
+            kd[p] = ks[i];
+            vd[p] = vs[i];
+        }
+        uint64_t* tk = ks; ks = kd; kd = tk;
+        uint32_t* tv = vs; vs = vd; vd = tv;
+    }
+    /* eight passes: the result is back in the caller's arrays */
+    free(k2);
+    free(v2);
+}
+
 /* ------------------------------------------------------------------------- */
 /* Morton topology                                                           */
 
@@ -251,6 +332,29 @@ uint32_t sqo_find_split_morton(const uint32_t* codes, uint32_t count)
         int ns = split + step;
         if (ns < last) {
             int sp = lzcnt32(first ^ codes[ns]);
+            if (sp > common) split = ns;
+        }
+    } while (step > 1);
+    return (uint32_t)split;
+}
+
+static inline int lzcnt64(uint64_t x) { return x ? __builtin_clzll(x) : 64; }
+
+/* find_split_morton2 (src/builder.cpp:2316-2349) */
+uint32_t sqo_find_split_morton64(const uint64_t* codes, uint32_t count)
+{
+    uint64_t first = codes[0];
+    uint64_t last_code = codes[count - 1];
+    if (first == last_code) return count >> 1;
+    int common = lzcnt64(first ^ last_code);
+    int split = 0;
+    int last = (int)count - 1;
+    int step = last;
+    do {
+        step = (step + 1) >> 1;
+        int ns = split + step;
+        if (ns < last) {
+            int sp = lzcnt64(first ^ codes[ns]);
             if (sp > common) split = ns;
         }
     } while (step > 1);
@@ -294,7 +398,8 @@ static inline void range_box(const box* tb, const uint32_t* perm, uint32_t b, ui
 }
 
 typedef struct morton_job {
-    const uint32_t* codes;
+    const uint32_t* codes;    /* 30-bit codes, or NULL when codes64 is used */
+    const uint64_t* codes64;  /* 60-bit codes (build_hierarchy_morton2)     */
     const uint32_t* perm;
     const box* tb;
     sqo_node1* nodes;
@@ -317,7 +422,7 @@ static void morton_range(const morton_job* j, uint32_t b, uint32_t e, uint32_t s
         write_inner(&j->nodes[slot], out, j->leaf0 + b, c);
         return;
     }
-    uint32_t s = sqo_find_split_morton(j->codes + b, c);
+    uint32_t s = j->codes64 ? sqo_find_split_morton64(j->codes64 + b, c) : sqo_find_split_morton(j->codes + b, c);
     uint32_t q = b + s + 1u;
     box bl, br;
     if (c > 4096) {
@@ -347,7 +452,7 @@ uint32_t sqo_build_morton(const float* tris, uint32_t n, int bounds_mode,
         tri_box(tris + 9 * (size_t)i, &tb[i]);
     }
     sqo_sort_pairs(codes, perm, n, 32, 8);
-    morton_job j = {codes, perm, tb, nodes, 2u * n + 2u};
+    morton_job j = {codes, NULL, perm, tb, nodes, 2u * n + 2u};
     emit_leaves(tb, perm, 0, n, nodes);
     box root;
     if (n < 8) {
@@ -360,6 +465,39 @@ uint32_t sqo_build_morton(const float* tris, uint32_t n, int bounds_mode,
         morton_range(&j, 0, n, 0, &root);
     }
     if (codes_out) memcpy(codes_out, codes, sizeof(uint32_t) * (size_t)n);
+    if (perm_out) memcpy(perm_out, perm, sizeof(uint32_t) * (size_t)n);
+    free(codes);
+    free(perm);
+    free(tb);
+    return 0;
+}
+
+/* build_hierarchy_morton2 (src/builder.cpp:2510-2544): the same range tree
+ * over 60-bit codes (recurse_morton2, src/builder.cpp:2413-2472) */
+uint32_t sqo_build_morton64(const float* tris, uint32_t n, int bounds_mode, sqo_node1* nodes, uint64_t* codes_out,
+                            uint32_t* perm_out)
+{
+    uint64_t* codes = (uint64_t*)malloc(sizeof(uint64_t) * ((size_t)n + 1));
+    uint32_t* perm = (uint32_t*)malloc(sizeof(uint32_t) * ((size_t)n + 1));
+    box* tb = (box*)malloc(sizeof(box) * ((size_t)n + 1));
+    sqo_morton_codes64(tris, n, bounds_mode, codes, NULL);
+    for (uint32_t i = 0; i < n; ++i) {
+        perm[i] = i;
+        tri_box(tris + 9 * (size_t)i, &tb[i]);
+    }
+    sqo_sort_pairs64(codes, perm, n);
+    morton_job j = {NULL, codes, perm, tb, nodes, 2u * n + 2u};
+    emit_leaves(tb, perm, 0, n, nodes);
+    box root;
+    if (n < 8) {
+        range_box(tb, perm, 0, n, &root);
+        write_inner(&nodes[0], &root, j.leaf0, n);
+    } else {
+#pragma omp parallel num_threads(sqo_get_threads())
+#pragma omp single
+        morton_range(&j, 0, n, 0, &root);
+    }
+    if (codes_out) memcpy(codes_out, codes, sizeof(uint64_t) * (size_t)n);
     if (perm_out) memcpy(perm_out, perm, sizeof(uint32_t) * (size_t)n);
     free(codes);
     free(perm);

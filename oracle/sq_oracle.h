@@ -62,6 +62,14 @@ void sqo_sort_pairs(uint32_t* keys, uint32_t* values, uint32_t n,
 
 /* find_split_morton (src/builder.cpp:2281-2314) over codes[0..count) */
 uint32_t sqo_find_split_morton(const uint32_t* codes, uint32_t count);
+/* 60-bit codes of build_hierarchy_morton2 (src/builder.cpp:2247-2279,
+ * 2316-2349, 2413-2472, 2510-2544) */
+uint64_t sqo_bit_interleave_64(uint64_t x, uint64_t y, uint64_t z);
+void sqo_morton_codes64(const float* tris, uint32_t n, int bounds_mode, uint64_t* codes, float* scene_box);
+void sqo_sort_pairs64(uint64_t* keys, uint32_t* values, uint32_t n);
+uint32_t sqo_find_split_morton64(const uint64_t* codes, uint32_t count);
+uint32_t sqo_build_morton64(const float* tris, uint32_t n, int bounds_mode, sqo_node1* nodes, uint64_t* codes_out,
+                            uint32_t* perm_out);
 
 /* Node capacity of a range-tree layout for n triangles */
 uint32_t sqo_node_capacity(uint32_t n, int kind);

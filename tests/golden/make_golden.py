@@ -21,6 +21,9 @@ reference's own functions return for them:
                                 the reference-camera rays (regenerated by the
                                 oracle; trace()'s heatmap pins that generation)
   splits_*                      find_split_morton on sub-ranges
+  codes64, sorted_codes64,      setup_morton2 / radix_sort<uint64_t> /
+  sorted_index64, splits64      find_split_morton2 (src/builder.cpp:2247-2349)
+                                on the same sub-ranges
 """
 import os
 import sys
@@ -58,6 +61,11 @@ def make(name, tris, w=160, h=120):
         starts.append(a); ends.append(b); splits.append(O.ref_find_split_morton(sc[a:b]))
     out.update(splits_begin=np.array(starts, np.uint32), splits_end=np.array(ends, np.uint32),
                splits=np.array(splits, np.uint32))
+    # the 60-bit path of build_hierarchy_morton2
+    codes64, index64, _ = O.ref_setup_morton2(tris)
+    sc64, si64 = O.ref_radix_sort64(codes64, index64)
+    out.update(codes64=codes64, sorted_codes64=sc64, sorted_index64=si64,
+               splits64=np.array([O.ref_find_split_morton2(sc64[a:b]) for a, b in zip(starts, ends)], np.uint32))
     for bins, variant in ((8, "b8"), (16, "b16"), (32, "b32")):
         nodes, root = O.ref_build("recursive", tris, variant)
         if valid(nodes, root, n):

@@ -110,3 +110,24 @@ def test_packet_and_bundle_heatmaps(oracle, golden, bundle, k):
     key = ("bundle%d_heat" if bundle else "packet%d_heat") % k
     got = oracle.trace_coherent(golden["sah8_nodes"], int(golden["sah8_root"]), w, h, golden["cam"], bundle, k)
     assert np.array_equal(got, golden[key])
+
+
+def test_morton64_codes_sort_split(oracle, golden):
+    """The 60-bit path of build_hierarchy_morton2: codes, stable sort and
+    find_split_morton2, against the reference's own functions."""
+    codes, box = oracle.morton_codes64(golden["tris"])
+    assert np.array_equal(codes, golden["codes64"])
+    assert np.array_equal(box, golden["scene"])
+    k, v = oracle.sort_pairs64(golden["codes64"], np.arange(len(codes), dtype=np.uint32))
+    assert np.array_equal(k, golden["sorted_codes64"])
+    assert np.array_equal(v, golden["sorted_index64"])
+    sc = golden["sorted_codes64"]
+    for a, b, s in zip(golden["splits_begin"], golden["splits_end"], golden["splits64"]):
+        assert oracle.find_split_morton64(sc[a:b]) == s
+
+
+def test_morton64_tree_valid(oracle, golden):
+    n = len(golden["tris"])
+    nodes, root, codes, perm = oracle.build_morton64(golden["tris"])
+    assert np.array_equal(codes, golden["sorted_codes64"]) and np.array_equal(perm, golden["sorted_index64"])
+    assert (oracle.leaf_reach(nodes, root, n) == 1).all()
