@@ -116,6 +116,10 @@ typedef enum sq_builder_kind {
 #define SQ_BUILD_GRID_SCENE_BOUNDS 0x1u /* grid: give cell nodes the scene box,
                                            as the plain reference grid builder
                                            does (src/builder.cpp:2173-2174)      */
+#define SQ_BUILD_MORTON64 0x4u          /* Morton builder over 60-bit codes (20
+                                           bits per axis, 8 sort passes) as
+                                           Builder::build_hierarchy_morton2
+                                           (src/builder.cpp:2510)               */
 #define SQ_BUILD_WIDE8 0x2u             /* also collapse the binary tree into an
                                            8-wide BVH with 8-bit quantised child
                                            boxes (rounded outward); closest and
@@ -238,6 +242,9 @@ sq_status sq_radix_sort_pairs(sq_ctx* ctx, const uint32_t* keys_in,
 /* The sorted Morton codes and triangle permutation of the last Morton build
  * of this BVH (n entries each).                                              */
 sq_status sq_bvh_export_sorted(sq_bvh* bvh, uint32_t* codes, uint32_t* perm);
+/* The same for a SQ_BUILD_MORTON64 build: the sorted 60-bit codes of
+ * setup_morton2 + radix_sort<uint64_t> (src/builder.cpp:2247-2279, 2521). */
+sq_status sq_bvh_export_sorted64(sq_bvh* bvh, uint64_t* codes, uint32_t* perm);
 
 /* Radix sort that allocates nothing.  No counterpart in the reference: it is
  * for callers that cannot call cudaMalloc / cudaFree (for example a host

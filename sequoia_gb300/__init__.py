@@ -110,6 +110,7 @@ def load_library():
         "sq_morton_codes": (i32, [vp, vp, u32, u32, vp, vp]),
         "sq_radix_sort_pairs": (i32, [vp, vp, vp, u32, u32, u32, vp, vp]),
         "sq_bvh_export_sorted": (i32, [vp, vp, vp]),
+        "sq_bvh_export_sorted64": (i32, [vp, vp, vp]),
         "sq_trace": (i32, [vp, vp, C.POINTER(_RaySource), u32, vp, vp]),
         "sq_last_timings": (i32, [vp, C.POINTER(C.c_float * 8)]),
         "sq_last_trace_stats": (i32, [vp, C.POINTER(C.c_uint64 * 4)]),
@@ -200,6 +201,13 @@ class Bvh:
         self.ctx._check(load_library().sq_bvh_export_sorted(self.handle, codes.ctypes.data, perm.ctypes.data))
         return codes, perm
 
+    def export_sorted64(self):
+        n = self.info().tri_count
+        codes = np.empty(n, np.uint64)
+        perm = np.empty(n, np.uint32)
+        self.ctx._check(load_library().sq_bvh_export_sorted64(self.handle, codes.ctypes.data, perm.ctypes.data))
+        return codes, perm
+
     def free(self):
         if self.handle:
             load_library().sq_bvh_free(self.handle)
@@ -288,10 +296,13 @@ class Context:
         self._check(load_library().sq_sync(self.handle, C.byref(bits)))
         return bits.value
 
-    def build(self, tris, builder="morton", bins=8, leaf=8, digit_bits=8, morton_bounds=0, flags=0, wide=False):
+    def build(self, tris, builder="morton", bins=8, leaf=8, digit_bits=8, morton_bounds=0, flags=0, wide=False,
+              morton64=False):
         n = _len(tris, 9)
         if wide:
             flags |= 2
+        if morton64:
+            flags |= 4  # 60-bit codes (build_hierarchy_morton2)
         p = _BuildParams(BUILDERS[builder] if isinstance(builder, str) else int(builder), bins, leaf,
                          digit_bits, morton_bounds, flags)
         h = C.c_void_p()

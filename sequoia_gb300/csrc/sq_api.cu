@@ -178,6 +178,59 @@ sq_status build_morton(sq_ctx* c, sq_bvh* b, const sq_build_params& p)
     return SQ_OK;
 }
 
+// Morton build over 60-bit codes (Builder::build_hierarchy_morton2,
+// src/builder.cpp:2510-2544).  The 64-bit keys are sorted by two stable
+// 32-bit sorts, the low words first (with the triangle index) and then the
+// high words in that order (with the position): LSD order, so the result
+// is the reference's stable 64-bit sort.  The climb then runs on the
+// combined 64-bit codes.
+sq_status build_morton64(sq_ctx* c, sq_bvh* b, const sq_build_params& p)
+{
+    const uint32_t n = b->n;
+    if (p.sort_digit_bits && p.sort_digit_bits != 8)
+        return fail(c, SQ_ERR_UNSUPPORTED, "60-bit Morton builds sort with 8-bit digits");
+    const uint32_t db = 8, passes = 4;
+    const size_t radix = 256;
+    const size_t lb_words = sqk::sort_lookback_words(n, db, passes);
+    // zeroed: box_ord[8] | hist[8 * 256] | counters[16] | look-back (2 stages) | flags[n]
+    const size_t z_box = 0, z_hist = 8, z_ctr = z_hist + 8 * radix, z_lb = z_ctr + 16, z_flags = z_lb + 2 * lb_words;
+    const size_t z_words = z_flags + n;
+    uint32_t* zero = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * z_words));
+    uint32_t* work = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * 9ull * n));
+    float4* info = static_cast<float4*>(dalloc(c, sizeof(float4) * 6ull * n));
+    b->codes64 = static_cast<uint64_t*>(dalloc(c, sizeof(uint64_t) * (size_t)n));
+    b->perm = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * (size_t)n));
+    if (!zero || !work || !info || !b->codes64 || !b->perm) {
+        dfree(c, zero); dfree(c, work); dfree(c, info);
+        return fail(c, SQ_ERR_OOM, "device workspace allocation failed (n=%u)", n);
+    }
+    uint32_t *lo = work, *hi = work + n, *vals = work + 2ull * n, *alt = work + 3ull * n;  // alt: 2n
+    uint32_t *hi1 = work + 5ull * n, *pos = work + 6ull * n, *alt2 = work + 7ull * n;     // alt2: 2n
+    uint32_t* err = c->ctrl;
+    cudaStream_t s = c->stream;
+    SQ_CUDA(c, cudaEventRecord(c->ev[0], s));
+    SQ_CUDA(c, cudaMemsetAsync(zero, 0, sizeof(uint32_t) * z_words, s));
+    sqk::scene_bounds(b->tris, n, p.morton_bounds, zero + z_box, s);
+    sqk::morton_codes64(b->tris, n, zero + z_box, lo, hi, vals, zero + z_hist, s);
+    SQ_CUDA(c, cudaEventRecord(c->ev[1], s));
+    // an even number of passes leaves each stage's result in its input buffers
+    sqk::sort_passes(lo, vals, alt, alt + n, n, zero + z_hist, zero + z_lb, zero + z_ctr, db, passes, err, s);
+    sqk::gather_high(hi, vals, n, hi1, pos, s);
+    sqk::sort_passes(hi1, pos, alt2, alt2 + n, n, zero + z_hist + 4 * radix, zero + z_lb + lb_words, zero + z_ctr + 8,
+                     db, passes, err, s);
+    sqk::combine64(hi1, pos, lo, vals, n, b->codes64, b->perm, s);
+    SQ_CUDA(c, cudaEventRecord(c->ev[2], s));
+    sqk::lbvh_climb64(b->codes64, b->perm, b->tris, n, b->nodes, zero + z_flags, info, err, s);
+    SQ_CUDA(c, cudaEventRecord(c->ev[3], s));
+    SQ_CUDA(c, cudaGetLastError());
+    c->build_timed = true;
+    dfree(c, zero);
+    dfree(c, work);
+    dfree(c, info);
+    b->root = 0;
+    return SQ_OK;
+}
+
 // Binned SAH or grid build into b.
 sq_status build_sah(sq_ctx* c, sq_bvh* b, const sq_build_params& p, int grid)
 {
@@ -345,7 +398,7 @@ sq_status sq_build(sq_ctx* c, const sq_triangle* tris, uint32_t n, const sq_buil
         return SQ_OK;
     }
     b->leaf0 = (p.kind == SQ_BUILDER_GRID ? 128u : 0u) + 2u * n + 2u;
-    if (p.kind == SQ_BUILDER_MORTON) st = build_morton(c, b, p);
+    if (p.kind == SQ_BUILDER_MORTON) st = (p.flags & SQ_BUILD_MORTON64) ? build_morton64(c, b, p) : build_morton(c, b, p);
     else st = build_sah(c, b, p, p.kind == SQ_BUILDER_GRID);
     if (st != SQ_OK) { sq_bvh_free(b); return st; }
     if (p.flags & SQ_BUILD_WIDE8) {
@@ -365,6 +418,7 @@ sq_status sq_bvh_free(sq_bvh* b)
     dfree(c, b->nodes);
     dfree(c, b->tris_own);
     dfree(c, b->codes);
+    dfree(c, b->codes64);
     dfree(c, b->perm);
     dfree(c, b->nodes8);
     dfree(c, b->tris8);
@@ -406,8 +460,20 @@ sq_status sq_bvh_export_sorted(sq_bvh* b, uint32_t* codes, uint32_t* perm)
     if (!b) return SQ_ERR_INVALID;
     sq_ctx* c = b->ctx;
     Guard g(c->device);
-    if (!b->codes) return fail(c, SQ_ERR_INVALID, "export_sorted: not a Morton build");
+    if (!b->codes) return fail(c, SQ_ERR_INVALID, "export_sorted: not a 30-bit Morton build");
     if (codes) SQ_CUDA(c, cudaMemcpyAsync(codes, b->codes, sizeof(uint32_t) * (size_t)b->n, cudaMemcpyDefault, c->stream));
+    if (perm) SQ_CUDA(c, cudaMemcpyAsync(perm, b->perm, sizeof(uint32_t) * (size_t)b->n, cudaMemcpyDefault, c->stream));
+    return check_device_error(c, nullptr);
+}
+
+sq_status sq_bvh_export_sorted64(sq_bvh* b, uint64_t* codes, uint32_t* perm)
+{
+    if (!b) return SQ_ERR_INVALID;
+    sq_ctx* c = b->ctx;
+    Guard g(c->device);
+    if (!b->codes64) return fail(c, SQ_ERR_INVALID, "export_sorted64: not a 60-bit Morton build");
+    if (codes) SQ_CUDA(c, cudaMemcpyAsync(codes, b->codes64, sizeof(uint64_t) * (size_t)b->n, cudaMemcpyDefault,
+                                          c->stream));
     if (perm) SQ_CUDA(c, cudaMemcpyAsync(perm, b->perm, sizeof(uint32_t) * (size_t)b->n, cudaMemcpyDefault, c->stream));
     return check_device_error(c, nullptr);
 }

@@ -34,6 +34,7 @@ struct sq_bvh {
     uint32_t kind = 0;
     float scene[6] = {0, 0, 0, 0, 0, 0};
     uint32_t* codes = nullptr;  // sorted codes (Morton builds)
+    uint64_t* codes64 = nullptr;  // sorted 60-bit codes (SQ_BUILD_MORTON64)
     uint32_t* perm = nullptr;   // sorted permutation
     void* nodes8 = nullptr;     // 8-wide quantised nodes (SQ_BUILD_WIDE8)
     void* tris8 = nullptr;      // their 48-byte triangles

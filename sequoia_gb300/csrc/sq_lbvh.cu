@@ -166,10 +166,98 @@ __global__ void __launch_bounds__(256) k_morton(const float* __restrict__ tris, 
     }
 }
 
+// Spread the low 21 bits of v to every third bit (bit i -> bit 3i).
+__device__ __forceinline__ uint64_t spread21(uint64_t v)
+{
+    v &= 0x1FFFFFull;
+    v = (v | (v << 32)) & 0x001F00000000FFFFull;
+    v = (v | (v << 16)) & 0x001F0000FF0000FFull;
+    v = (v | (v << 8)) & 0x100F00F00F00F00Full;
+    v = (v | (v << 4)) & 0x10C30C30C30C30C3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+
+// 60-bit codes of build_hierarchy_morton2 (setup_morton2,
+// src/builder.cpp:2247-2279: 0xFFFFF steps per axis, x at bit 0), split into
+// low and high words, plus the 8-bit digit histograms of both words (four
+// passes each: hist[0..4) the low word, hist[4..8) the high word).
+__global__ void __launch_bounds__(256) k_morton64(const float* __restrict__ tris, uint32_t n,
+                                                  const uint32_t* __restrict__ box_ord, uint32_t* __restrict__ lo,
+                                                  uint32_t* __restrict__ hi, uint32_t* __restrict__ vals,
+                                                  uint32_t* __restrict__ hist, bool aligned)
+{
+    __shared__ __align__(16) float s_tri[kTileTris * 9];
+    __shared__ uint32_t s_hist[8 * 256];
+    for (int j = threadIdx.x; j < 8 * 256; j += blockDim.x) s_hist[j] = 0;
+    float smin[3], ext[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        smin[k] = -ordered_to_float(box_ord[k]);
+        ext[k] = ordered_to_float(box_ord[3 + k]) - smin[k];
+    }
+    for (uint32_t first = blockIdx.x * kTileTris; first < n; first += gridDim.x * kTileTris) {
+        const uint32_t count = min((uint32_t)kTileTris, n - first);
+        __syncthreads();
+        stage_tris(tris, first, count, s_tri, aligned);
+        __syncthreads();
+        if (threadIdx.x < count) {
+            const Box b = tri_box(s_tri + 9 * threadIdx.x);
+            uint64_t q[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float c = (b.mn[k] + b.mx[k]) * 0.5f;
+                const float u = (c - smin[k]) / ext[k];
+                q[k] = f2u(u * 1048575.0f);
+            }
+            const uint64_t code = spread21(q[0]) | (spread21(q[1]) << 1) | (spread21(q[2]) << 2);
+            const uint32_t i = first + threadIdx.x;
+            const uint32_t l = (uint32_t)code, h = (uint32_t)(code >> 32);
+            lo[i] = l;
+            hi[i] = h;
+            vals[i] = i;
+#pragma unroll
+            for (int p = 0; p < 4; ++p) {
+                atomicAdd(&s_hist[p * 256 + ((l >> (8 * p)) & 255u)], 1u);
+                atomicAdd(&s_hist[(4 + p) * 256 + ((h >> (8 * p)) & 255u)], 1u);
+            }
+        }
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < 8 * 256; j += blockDim.x) {
+        const uint32_t c = s_hist[j];
+        if (c) atomicAdd(hist + j, c);
+    }
+}
+
+// Second sort stage of the 60-bit codes: the high words in the order of the
+// first stage, keyed by position.
+__global__ void k_gather_high(const uint32_t* __restrict__ hi, const uint32_t* __restrict__ perm1, uint32_t n,
+                              uint32_t* __restrict__ hi1, uint32_t* __restrict__ pos)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        hi1[i] = hi[perm1[i]];
+        pos[i] = i;
+    }
+}
+
+// codes64[i] = hi_sorted[i] : lo_sorted[perm2[i]], perm[i] = perm1[perm2[i]]
+__global__ void k_combine64(const uint32_t* __restrict__ hi_sorted, const uint32_t* __restrict__ perm2,
+                            const uint32_t* __restrict__ lo_sorted, const uint32_t* __restrict__ perm1, uint32_t n,
+                            uint64_t* __restrict__ codes64, uint32_t* __restrict__ perm)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t j = perm2[i];
+        codes64[i] = ((uint64_t)hi_sorted[i] << 32) | lo_sorted[j];
+        perm[i] = perm1[j];
+    }
+}
+
 // ---------------------------------------------------------------------------
 // climb
 
-__global__ void __launch_bounds__(256) k_lbvh_climb(const uint32_t* __restrict__ codes, const uint32_t* __restrict__ perm,
+template <class Code>
+__global__ void __launch_bounds__(256) k_lbvh_climb(const Code* __restrict__ codes, const uint32_t* __restrict__ perm,
                                                     const float* __restrict__ tris, uint32_t n, Node* __restrict__ nodes,
                                                     uint32_t* __restrict__ flags, float4* __restrict__ info, uint32_t* err)
 {
@@ -180,19 +268,19 @@ __global__ void __launch_bounds__(256) k_lbvh_climb(const uint32_t* __restrict__
     // this lane's node: [l, r) with its box and split, while `active`
     bool active = false;
     uint32_t l = 0, r = 0, split = 0;
-    uint32_t dl = 0, dr = 0;  // code XOR at boundaries l and r (where they are inside (0, n))
+    Code dl = 0, dr = 0;  // code XOR at boundaries l and r (where they are inside (0, n))
     Box box;
     box_reset(box);
     // codes of this position and its neighbours (shuffled within the warp)
     const uint32_t W = i - (uint32_t)lane;  // the warp's first position
-    const uint32_t code = i < n ? codes[i] : 0u;
-    uint32_t prev = __shfl_up_sync(FULL, code, 1), next = __shfl_down_sync(FULL, code, 1);
+    const Code code = i < n ? codes[i] : Code(0);
+    Code prev = __shfl_up_sync(FULL, code, 1), next = __shfl_down_sync(FULL, code, 1);
     if (lane == 0 && i > 0 && i < n) prev = codes[i - 1];
     if (lane == 31 && i + 1 < n) next = codes[i + 1];
     // d_own = code XOR at boundary i (between positions i - 1 and i); d_end =
     // the XOR at boundary W + 32, just past the warp
-    const uint32_t d_own = prev ^ code;
-    const uint32_t d_end = __shfl_sync(FULL, code ^ next, 31);
+    const Code d_own = prev ^ code;
+    const Code d_end = __shfl_sync(FULL, code ^ next, 31);
     if (i < n) {
         if (i == 0 || prev != code) {  // a run head
             uint32_t e = i + 1;
@@ -227,7 +315,7 @@ __global__ void __launch_bounds__(256) k_lbvh_climb(const uint32_t* __restrict__
         // the XOR at the run's end comes from the lane that owns it when it is
         // inside the warp
         const bool r_in = active && r - W < 32u;
-        const uint32_t dr_in = __shfl_sync(FULL, d_own, r_in ? (int)(r - W) : lane);
+        const Code dr_in = __shfl_sync(FULL, d_own, r_in ? (int)(r - W) : lane);
         if (active) {
             dl = d_own;
             if (r_in) dr = dr_in;
@@ -252,7 +340,7 @@ __global__ void __launch_bounds__(256) k_lbvh_climb(const uint32_t* __restrict__
     // Merge this node with its sibling (ending or starting at s_end, with the
     // code XOR s_d at that far boundary): write both children's records when
     // the parent is an inner node, and continue with the parent.
-    auto merge = [&](uint32_t p, bool left, uint32_t s_end, const Box& sb, uint32_t s_split, uint32_t s_d) {
+    auto merge = [&](uint32_t p, bool left, uint32_t s_end, const Box& sb, uint32_t s_split, Code s_d) {
         uint32_t ll, rr, lsplit, rsplit;
         Box lb, rb;
         if (left) { ll = l; rr = s_end; lb = box; rb = sb; lsplit = split; rsplit = s_split; dr = s_d; }
@@ -286,7 +374,7 @@ __global__ void __launch_bounds__(256) k_lbvh_climb(const uint32_t* __restrict__
             if (__popc(grp) == 2) {
                 const int other = __ffs(grp & ~(1u << lane)) - 1;
                 const uint32_t o_r = __shfl_sync(grp, r, other);
-                const uint32_t o_dr = __shfl_sync(grp, dr, other);
+                const Code o_dr = __shfl_sync(grp, dr, other);
                 const uint32_t o_split = __shfl_sync(grp, split, other);
                 Box ob;
 #pragma unroll
@@ -319,7 +407,8 @@ __global__ void __launch_bounds__(256) k_lbvh_climb(const uint32_t* __restrict__
         float4* mine = info + 3ull * (2ull * p + (left ? 0u : 1u));
         mine[0] = make_float4(box.mn[0], box.mn[1], box.mn[2], __uint_as_float(left ? l : r));
         mine[1] = make_float4(box.mx[0], box.mx[1], box.mx[2], __uint_as_float(split));
-        mine[2] = make_float4(__uint_as_float(left ? dl : dr), 0.0f, 0.0f, 0.0f);
+        const uint64_t dfar = (uint64_t)(left ? dl : dr);
+        mine[2] = make_float4(__uint_as_float((uint32_t)dfar), __uint_as_float((uint32_t)(dfar >> 32)), 0.0f, 0.0f);
         // release my record, acquire the sibling's (the first arrival stops)
         const uint32_t old = atomic_add_acq_rel_u32(flags + p, 1u);
         if (old == 0) return;
@@ -329,7 +418,8 @@ __global__ void __launch_bounds__(256) k_lbvh_climb(const uint32_t* __restrict__
         Box sb;
         sb.mn[0] = s0.x; sb.mn[1] = s0.y; sb.mn[2] = s0.z;
         sb.mx[0] = s1.x; sb.mx[1] = s1.y; sb.mx[2] = s1.z;
-        merge(p, left, __float_as_uint(s0.w), sb, __float_as_uint(s1.w), __float_as_uint(s2.x));
+        const uint64_t s_d = (uint64_t)__float_as_uint(s2.x) | ((uint64_t)__float_as_uint(s2.y) << 32);
+        merge(p, left, __float_as_uint(s0.w), sb, __float_as_uint(s1.w), (Code)s_d);
     }
 }
 
@@ -370,11 +460,42 @@ void morton_codes(const float* tris, uint32_t n, uint32_t mode, const uint32_t* 
     else if (digit_bits == 6 && passes == 5) k_morton<6, 5><<<grid, 256, 0, s>>>(tris, n, mode, box_ord, keys, vals, hist, aligned);
 }
 
+void morton_codes64(const float* tris, uint32_t n, const uint32_t* box_ord, uint32_t* lo, uint32_t* hi,
+                    uint32_t* vals, uint32_t* hist, cudaStream_t s)
+{
+    if (n == 0) return;
+    const bool aligned = (reinterpret_cast<uintptr_t>(tris) & 15u) == 0;
+    const uint32_t tiles = (n + kTileTris - 1) / kTileTris;
+    const uint32_t grid = min(tiles, (uint32_t)sms() * 4u);
+    k_morton64<<<grid, 256, 0, s>>>(tris, n, box_ord, lo, hi, vals, hist, aligned);
+}
+
+void gather_high(const uint32_t* hi, const uint32_t* perm1, uint32_t n, uint32_t* hi1, uint32_t* pos, cudaStream_t s)
+{
+    if (n == 0) return;
+    k_gather_high<<<min((n + 255) / 256, (uint32_t)sms() * 8u), 256, 0, s>>>(hi, perm1, n, hi1, pos);
+}
+
+void combine64(const uint32_t* hi_sorted, const uint32_t* perm2, const uint32_t* lo_sorted, const uint32_t* perm1,
+               uint32_t n, uint64_t* codes64, uint32_t* perm, cudaStream_t s)
+{
+    if (n == 0) return;
+    k_combine64<<<min((n + 255) / 256, (uint32_t)sms() * 8u), 256, 0, s>>>(hi_sorted, perm2, lo_sorted, perm1, n,
+                                                                            codes64, perm);
+}
+
 void lbvh_climb(const uint32_t* codes, const uint32_t* perm, const float* tris, uint32_t n, sq::Node* nodes,
                 uint32_t* flags, float4* info, uint32_t* err, cudaStream_t s)
 {
     if (n == 0) return;
-    k_lbvh_climb<<<(n + 255) / 256, 256, 0, s>>>(codes, perm, tris, n, nodes, flags, info, err);
+    k_lbvh_climb<uint32_t><<<(n + 255) / 256, 256, 0, s>>>(codes, perm, tris, n, nodes, flags, info, err);
+}
+
+void lbvh_climb64(const uint64_t* codes, const uint32_t* perm, const float* tris, uint32_t n, sq::Node* nodes,
+                  uint32_t* flags, float4* info, uint32_t* err, cudaStream_t s)
+{
+    if (n == 0) return;
+    k_lbvh_climb<uint64_t><<<(n + 255) / 256, 256, 0, s>>>(codes, perm, tris, n, nodes, flags, info, err);
 }
 
 }  // namespace sqk

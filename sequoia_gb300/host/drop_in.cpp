@@ -159,9 +159,9 @@ Hierarchy Builder::build_hierarchy_grid_m128(std::vector<Triangle>& p)
 {
     return build(p, SQ_BUILDER_GRID, 0, SQ_BUILD_GRID_SCENE_BOUNDS);
 }
-Hierarchy Builder::build_hierarchy_morton2(std::vector<Triangle>&)
+Hierarchy Builder::build_hierarchy_morton2(std::vector<Triangle>& p)
 {
-    throw Error(SQ_ERR_UNSUPPORTED, "sequoia: 64-bit Morton codes (build_hierarchy_morton2) are not implemented");
+    return build(p, SQ_BUILDER_MORTON, SQ_BUILD_MORTON64, 0);
 }
 
 namespace {

@@ -81,7 +81,7 @@ class Builder {
 public:
     static Hierarchy build_hierarchy(std::vector<Triangle>& primitives);
     static Hierarchy build_hierarchy_morton(std::vector<Triangle>& primitives);
-    static Hierarchy build_hierarchy_morton2(std::vector<Triangle>& primitives);  // throws: 64-bit codes unsupported
+    static Hierarchy build_hierarchy_morton2(std::vector<Triangle>& primitives);  // 60-bit codes
     static Hierarchy build_hierarchy_grid(std::vector<Triangle>& primitives);
     static Hierarchy build_hierarchy_grid_sse(std::vector<Triangle>& primitives);
     static Hierarchy build_hierarchy_grid_m128(std::vector<Triangle>& primitives);

@@ -149,3 +149,38 @@ def test_invalid_arguments(ctx):
         ctx.build(np.zeros((4, 9), np.float32), "morton", digit_bits=7)
     with pytest.raises(sq.SequoiaError):
         ctx.radix_sort_pairs(np.zeros(4, np.uint32), np.zeros(4, np.uint32), 0, 8)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["ico3", "ico4", "soup3k", "dups2k"])
+def test_morton64_golden(ctx, oracle, name):
+    """build_hierarchy_morton2's 60-bit path: sorted codes and permutation
+    equal the reference's setup_morton2 + radix_sort<uint64_t>, and the tree
+    the oracle's record for record."""
+    g = load_golden(name)
+    bvh = ctx.build(g["tris"], "morton", morton64=True)
+    codes, perm = bvh.export_sorted64()
+    assert np.array_equal(codes, g["sorted_codes64"])
+    assert np.array_equal(perm, g["sorted_index64"])
+    nodes, root = bvh.export_node1()
+    onodes, oroot, _, _ = oracle.build_morton64(g["tris"])
+    assert_same_tree(oracle, nodes, root, onodes, oroot)
+    assert (oracle.leaf_reach(nodes, root, len(g["tris"])) == 1).all()
+    assert ctx.sync() == 0
+
+
+@pytest.mark.gpu
+def test_morton64_soup_2m(ctx, oracle):
+    """The 2M-triangle soup at full size: 60-bit codes, permutation and every
+    record equal the oracle's; the 60-bit tree separates what the 30-bit one
+    leaves in runs of equal codes."""
+    from sequoia_gb300 import scenes
+    tris = scenes.gaussian_soup(2_000_000, 64, seed=2)
+    bvh = ctx.build(tris, "morton", morton64=True)
+    codes, perm = bvh.export_sorted64()
+    onodes, oroot, ocodes, operm = oracle.build_morton64(tris)
+    assert np.array_equal(codes, ocodes) and np.array_equal(perm, operm)
+    nodes, root = bvh.export_node1()
+    assert_same_tree(oracle, nodes, root, onodes, oroot)
+    c32, _ = ctx.build(tris, "morton").export_sorted()
+    assert len(np.unique(codes)) >= len(np.unique(c32))
