@@ -379,7 +379,7 @@ def main():
             lbvh_stage[k].append(tm[k])
         trace_ms.append(tm["trace"])
         stats.append(st)
-        launches += LBVH_KERNELS + bvh.info().wide_levels + 1
+        launches += LBVH_KERNELS + bvh.info().wide_launches + 1
         bvh.free()
     torch.cuda.synchronize()
     if dist:

@@ -142,7 +142,8 @@ typedef struct sq_bvh_info {
     float scene_min[3];
     float scene_max[3];
     uint32_t wide_nodes;      /* 8-wide quantised nodes (0 if none)               */
-    uint32_t wide_levels;     /* levels of the 8-wide collapse (kernel launches)  */
+    uint32_t wide_levels;     /* levels of the 8-wide tree                        */
+    uint32_t wide_launches;   /* kernel launches of the 8-wide collapse           */
 } sq_bvh_info;
 
 typedef enum sq_trace_mode {

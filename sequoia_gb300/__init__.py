@@ -53,7 +53,7 @@ class _BuildParams(C.Structure):
 class _BvhInfo(C.Structure):
     _fields_ = [("node_capacity", C.c_uint32), ("root", C.c_uint32), ("tri_count", C.c_uint32),
                 ("kind", C.c_uint32), ("scene_min", C.c_float * 3), ("scene_max", C.c_float * 3),
-                ("wide_nodes", C.c_uint32), ("wide_levels", C.c_uint32)]
+                ("wide_nodes", C.c_uint32), ("wide_levels", C.c_uint32), ("wide_launches", C.c_uint32)]
 
 
 class _RaySource(C.Structure):

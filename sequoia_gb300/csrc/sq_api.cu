@@ -287,6 +287,7 @@ sq_status build_wide(sq_ctx* c, sq_bvh* b)
     if (rc != 0) return fail(c, SQ_ERR_CUDA, "8-wide collapse: %s", cudaGetErrorString((cudaError_t)rc));
     b->n8 = c->host_ctl[0];
     b->levels8 = c->host_ctl[3];
+    b->launches8 = c->host_ctl[4];
     dfree(c, b->ws8);
     b->ws8 = nullptr;
     return SQ_OK;
@@ -438,6 +439,7 @@ sq_status sq_bvh_get_info(const sq_bvh* b_const, sq_bvh_info* info)
     for (int k = 0; k < 3; ++k) { info->scene_min[k] = b->scene[k]; info->scene_max[k] = b->scene[3 + k]; }
     info->wide_nodes = b->n8;
     info->wide_levels = b->levels8;
+    info->wide_launches = b->launches8;
     return SQ_OK;
 }
 

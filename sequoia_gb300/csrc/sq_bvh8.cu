@@ -1541,6 +1541,7 @@ static int build_bvh8_levels(const Node* rec, uint32_t root, uint32_t leaf0, con
         std::swap(na, nb);
     }
     host_ctl[3] = levels;
+    host_ctl[4] = levels;  // one launch per level
     return (int)cudaGetLastError();
 }
 
@@ -1570,6 +1571,7 @@ int build_bvh8(const Node* rec, uint32_t root, uint32_t leaf0, const float* tris
     if ((e = cudaMemcpyAsync(host_ctl, ws, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return (int)e;
     if ((e = cudaMemcpyAsync(host_ctl + 3, ws + 4, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return (int)e;
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return (int)e;
+    host_ctl[4] = 2;  // the seed and the cooperative kernel
     return (int)cudaGetLastError();
 }
 

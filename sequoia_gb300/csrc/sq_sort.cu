@@ -83,7 +83,7 @@ struct Smem {
 };
 
 template <int DB>
-__global__ void __launch_bounds__(kBlock) k_onesweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+__global__ void __launch_bounds__(kBlock, 4) k_onesweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
                                                      uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n,
                                                      uint32_t shift, const uint32_t* __restrict__ hist,
                                                      uint32_t* __restrict__ lookback, uint32_t* __restrict__ counter,
