@@ -163,7 +163,7 @@ __global__ void k_gather_codes(const uint32_t* __restrict__ perm, uint32_t n, co
 }
 
 // The climb of k_lbvh_climb (sq_lbvh.cu) within mesh segments.
-__global__ void __launch_bounds__(256) k_seg_climb(const uint32_t* __restrict__ codes, const uint32_t* __restrict__ perm,
+__global__ void __launch_bounds__(256, 6) k_seg_climb(const uint32_t* __restrict__ codes, const uint32_t* __restrict__ perm,
                                                    const float* __restrict__ tris, uint32_t n,
                                                    const uint32_t* __restrict__ off, uint32_t M, Node* __restrict__ nodes,
                                                    uint32_t* __restrict__ flags, float4* __restrict__ info, uint32_t root0,

@@ -107,19 +107,24 @@ __device__ __forceinline__ uint8_t quant_hi(float v, float origin, int e)
 // the first child of largest surface area that still fits, until none does.
 // All 32 lanes must call this; a group whose `active` is false only takes
 // part in the warp-wide shuffles.  Inner children become nodes
-// [child_base, child_base + n) where child_base comes from reserve(n)
-// (called by the group's first lane); publish(node, record) is called by the
-// child's lane.  sm: this warp's staging area (kGroupSmem per warp).
+// [child_base, child_base + n) and leaf triangles slots [tri_base, ...).
+// The warp's four groups allocate together: lane 0 calls
+// alloc(nodes, tris, node_base, tri_base, task_base) once with the warp's
+// totals (one atomic per warp instead of one per node and one per child:
+// same-address atomics serialise in L2), and each group takes its share in
+// group order.  publish(task, node, record) is called by the child's lane
+// with task = task_base + the child's rank in the warp.  sm: this warp's
+// staging area (kGroupSmem per warp).
 struct GroupSmem {
     Node8 node[4];
     uint32_t off[4][8], cnt[4][8], child[4][8];
 };
 
-template <class Reserve, class Publish>
+template <class Alloc, class Publish>
 __device__ void collapse_node_group(const Node* __restrict__ rec, uint32_t leaf0, const float* __restrict__ tris,
                                     bool active, uint32_t rec_i, uint32_t node_i, Node8* __restrict__ nodes8,
-                                    float4* __restrict__ tris8, uint32_t* __restrict__ tri_counter, uint32_t* err,
-                                    GroupSmem& sm, Reserve reserve, Publish publish)
+                                    float4* __restrict__ tris8, uint32_t* err, GroupSmem& sm, Alloc alloc,
+                                    Publish publish)
 {
     constexpr uint32_t FULL = 0xFFFFFFFFu;
     const int lane = (int)(threadIdx.x & 31u);
@@ -224,14 +229,21 @@ __device__ void collapse_node_group(const Node* __restrict__ rec, uint32_t leaf0
     }
     const uint32_t n_tris = __shfl_sync(FULL, incl, 7, 8);
     const uint32_t tri_off = incl - cntk;
-    const uint32_t n_inner = __popc(imask);
-    uint32_t child_base = 0, tri_base = 0;
-    if (active && k == 0) {
-        child_base = n_inner ? reserve(n_inner) : 0u;
-        tri_base = n_tris ? atomicAdd(tri_counter, n_tris) : 0u;
+    const uint32_t n_inner = active ? __popc(imask) : 0u, n_place = active ? n_tris : 0u;
+    // the warp's totals and this group's offsets (groups in lane order)
+    uint32_t pre_i = 0, pre_t = 0, sum_i = 0, sum_t = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const uint32_t a = __shfl_sync(FULL, n_inner, 8 * q), b = __shfl_sync(FULL, n_place, 8 * q);
+        if (q < g) { pre_i += a; pre_t += b; }
+        sum_i += a;
+        sum_t += b;
     }
-    child_base = __shfl_sync(FULL, child_base, 0, 8);
-    tri_base = __shfl_sync(FULL, tri_base, 0, 8);
+    uint32_t node_base = 0, tri_base = 0, task_base = 0;
+    if (lane == 0 && (sum_i | sum_t)) alloc(sum_i, sum_t, node_base, tri_base, task_base);
+    const uint32_t child_base = __shfl_sync(FULL, node_base, 0) + pre_i;
+    tri_base = __shfl_sync(FULL, tri_base, 0) + pre_t;
+    task_base = __shfl_sync(FULL, task_base, 0) + pre_i;
     // quantised child planes, one slot per lane, staged in shared memory
     Node8& sn = sm.node[g];
     int e[3] = {0, 0, 0};
@@ -253,7 +265,10 @@ __device__ void collapse_node_group(const Node* __restrict__ rec, uint32_t leaf0
         sm.off[g][k] = tri_off;
         sm.cnt[g][k] = cntk;
         sm.child[g][k] = e_node.child;
-        if (inner) publish(child_base + __popc(imask & ((1u << k) - 1u)), e_rec);
+        if (inner) {
+            const uint32_t r = __popc(imask & ((1u << k) - 1u));
+            publish(task_base + r, child_base + r, e_rec);
+        }
     }
     __syncwarp();
     if (active && k == 0) {
@@ -293,6 +308,23 @@ __device__ void collapse_node_group(const Node* __restrict__ rec, uint32_t leaf0
     __syncwarp();  // the staging area is reused by the warp's next nodes
 }
 
+// Nodes and triangle slots of one warp from the counter pair at ctr (nodes
+// in word 0, triangles in word 1: one 64-bit atomic).  On overflow of the
+// node capacity the error word is set and the nodes land at `capacity`, where
+// nothing is written.
+__device__ __forceinline__ void alloc_nodes_tris(uint32_t* ctr, uint32_t kn, uint32_t kt, uint32_t capacity,
+                                                 uint32_t* err, uint32_t& nb, uint32_t& tb)
+{
+    const unsigned long long v =
+        atomicAdd(reinterpret_cast<unsigned long long*>(ctr), ((unsigned long long)kt << 32) | kn);
+    nb = (uint32_t)v;
+    tb = (uint32_t)(v >> 32);
+    if ((unsigned long long)nb + kn > capacity) {
+        raise_error(err, SQ_DEVERR_SAH_QUEUE);
+        nb = capacity;
+    }
+}
+
 // One level of the collapse: group i (four per warp) builds node
 // task_node[i] from binary record tasks[i]; inner children are allocated
 // contiguously from the node counter and appended to the next level's list.
@@ -309,19 +341,17 @@ __global__ void __launch_bounds__(kCollapseBlock) k_collapse_level(
     if (4u * w >= ntasks) return;  // whole warps
     const uint32_t i = 4u * w + ((threadIdx.x & 31u) >> 3);
     const bool active = i < ntasks;
-    auto reserve = [&](uint32_t k) -> uint32_t {
-        const uint32_t b0 = atomicAdd(counters + 0, k);
-        if ((unsigned long long)b0 + k > capacity) { raise_error(err, SQ_DEVERR_SAH_QUEUE); return 0u; }
-        return b0;
+    auto alloc = [&](uint32_t kn, uint32_t kt, uint32_t& nb, uint32_t& tb, uint32_t& jb) {
+        alloc_nodes_tris(counters, kn, kt, capacity, err, nb, tb);
+        jb = kn ? atomicAdd(counters + 2, kn) : 0u;
     };
-    auto publish = [&](uint32_t node, uint32_t record) {
+    auto publish = [&](uint32_t j, uint32_t node, uint32_t record) {
         if (node >= capacity) return;
-        const uint32_t j = atomicAdd(counters + 2, 1u);
         next_tasks[j] = record;
         next_node[j] = node;
     };
     collapse_node_group(rec, leaf0, tris, active, active ? tasks[i] : 0u, active ? task_node[i] : 0u, nodes8, tris8,
-                        counters + 1, err, s_group[threadIdx.x >> 5], reserve, publish);
+                        err, s_group[threadIdx.x >> 5], alloc, publish);
 }
 
 // Collapse without host synchronisation (so it can be captured in a CUDA
@@ -336,8 +366,7 @@ __global__ void __launch_bounds__(128) k_collapse_fixed(const Node* __restrict__
                                                         uint32_t* __restrict__ counts, const uint32_t* __restrict__ tasks,
                                                         const uint32_t* __restrict__ task_node,
                                                         uint32_t* __restrict__ next_tasks, uint32_t* __restrict__ next_node,
-                                                        uint32_t* __restrict__ node_counter,
-                                                        uint32_t* __restrict__ tri_counter, Node8* __restrict__ nodes8,
+                                                        uint32_t* __restrict__ counters2, Node8* __restrict__ nodes8,
                                                         float4* __restrict__ tris8, uint32_t capacity, uint32_t* err)
 {
     const uint32_t ntasks = counts[level];
@@ -352,19 +381,17 @@ __global__ void __launch_bounds__(128) k_collapse_fixed(const Node* __restrict__
     for (uint32_t base = 4u * ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); base < ntasks; base += 4u * warps) {
         const uint32_t i = base + ((threadIdx.x & 31u) >> 3);
         const bool active = i < ntasks;
-        auto reserve = [&](uint32_t k) -> uint32_t {
-            const uint32_t b0 = atomicAdd(node_counter, k);
-            if ((unsigned long long)b0 + k > capacity) { raise_error(err, SQ_DEVERR_SAH_QUEUE); return 0u; }
-            return b0;
+        auto alloc = [&](uint32_t kn, uint32_t kt, uint32_t& nb, uint32_t& tb, uint32_t& jb) {
+            alloc_nodes_tris(counters2, kn, kt, capacity, err, nb, tb);
+            jb = kn ? atomicAdd(next_count, kn) : 0u;
         };
-        auto publish = [&](uint32_t node, uint32_t record) {
+        auto publish = [&](uint32_t j, uint32_t node, uint32_t record) {
             if (node >= capacity) return;
-            const uint32_t j = atomicAdd(next_count, 1u);
             next_tasks[j] = record;
             next_node[j] = node;
         };
         collapse_node_group(rec, leaf0, tris, active, active ? tasks[i] : 0u, active ? task_node[i] : 0u, nodes8,
-                            tris8, tri_counter, err, s_group[threadIdx.x >> 5], reserve, publish);
+                            tris8, err, s_group[threadIdx.x >> 5], alloc, publish);
     }
 }
 
@@ -377,7 +404,11 @@ __global__ void __launch_bounds__(128) k_collapse_fixed(const Node* __restrict__
 // level, so an SM's L1 may hold stale lines of them.
 constexpr uint32_t kBarrierSpins = 1u << 24;
 
-__device__ bool grid_barrier(uint32_t* bar, uint32_t nblocks, uint32_t* err)
+// Grid barrier; the last block to arrive runs on_last() (thread 0 only)
+// after every other block's writes before the barrier are visible to it and
+// before any block leaves.
+template <class OnLast>
+__device__ bool grid_barrier(uint32_t* bar, uint32_t nblocks, uint32_t* err, OnLast on_last)
 {
     __shared__ int s_ok;
     __syncthreads();
@@ -387,6 +418,8 @@ __device__ bool grid_barrier(uint32_t* bar, uint32_t nblocks, uint32_t* err)
         __threadfence();
         if (atomicAdd(bar, 1u) + 1u == nblocks) {
             // last arrival: reset the count, then open the next generation
+            __threadfence();
+            on_last();
             atomicExch(bar, 0u);
             __threadfence();
             atomicAdd(bar + 1, 1u);
@@ -407,27 +440,30 @@ __device__ bool grid_barrier(uint32_t* bar, uint32_t nblocks, uint32_t* err)
     return s_ok != 0;
 }
 
+// The tasks of a level are the nodes [lo, hi) that the previous level
+// allocated, in allocation order: task j builds node lo + j from the binary
+// record in the level's task list at j.  A warp's allocation at node base b
+// therefore also places its children's tasks at b - hi in the next list, and
+// the next level's end is the node counter once the level is done (read by
+// the barrier's last block).
 __global__ void __launch_bounds__(256) k_collapse_coop(const Node* __restrict__ rec, uint32_t leaf0,
                                                        const float* __restrict__ tris, uint32_t* __restrict__ ws,
                                                        uint32_t capacity, Node8* __restrict__ nodes8,
                                                        float4* __restrict__ tris8, uint32_t* err)
 {
-    // ws: [0] node counter, [1] triangle counter, [2..3] barrier, [4] levels
-    // done, [8 .. 8 + kFixedLevels) level task counts, then the two (record,
-    // node) task lists of `capacity` entries each
-    uint32_t* node_counter = ws;
-    uint32_t* tri_counter = ws + 1;
+    // ws: [0] node counter, [1] triangle counter (one 64-bit pair), [2..3]
+    // barrier, [4] levels done, [5] end of the next level's nodes, then the
+    // task lists of even and odd levels (`capacity` records each, at the
+    // offsets the seed uses)
     uint32_t* bar = ws + 2;
-    uint32_t* counts = ws + 8;
-    uint32_t* ta = counts + kFixedLevels + 8;
-    uint32_t* na = ta + capacity;
-    uint32_t* tb = na + capacity;
-    uint32_t* nb = tb + capacity;
+    uint32_t* ta = ws + 8 + kFixedLevels + 8;
+    uint32_t* tb = ta + 2ull * capacity;
     __shared__ GroupSmem s_group[8];
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t lo = 0, hi = 1;  // the root task
     for (uint32_t level = 0;; ++level) {
-        const uint32_t ntasks = ld_acquire_u32(counts + level);
+        const uint32_t ntasks = hi - lo;
         if (ntasks == 0) {
             if (blockIdx.x == 0 && threadIdx.x == 0) ws[4] = level;
             return;
@@ -437,41 +473,36 @@ __global__ void __launch_bounds__(256) k_collapse_coop(const Node* __restrict__ 
             return;
         }
         const uint32_t* tasks = (level & 1) ? tb : ta;
-        const uint32_t* task_node = (level & 1) ? nb : na;
         uint32_t* next_tasks = (level & 1) ? ta : tb;
-        uint32_t* next_node = (level & 1) ? na : nb;
-        uint32_t* next_count = counts + level + 1;
         for (uint32_t base = 4u * wid; base < ntasks; base += 4u * warps) {
             const uint32_t i = base + ((threadIdx.x & 31u) >> 3);
             const bool active = i < ntasks;
-            auto reserve = [&](uint32_t k) -> uint32_t {
-                const uint32_t b0 = atomicAdd(node_counter, k);
-                if ((unsigned long long)b0 + k > capacity) { raise_error(err, SQ_DEVERR_SAH_QUEUE); return 0u; }
-                return b0;
+            auto alloc = [&](uint32_t kn, uint32_t kt, uint32_t& nb, uint32_t& tb_, uint32_t& jb) {
+                alloc_nodes_tris(ws, kn, kt, capacity, err, nb, tb_);
+                jb = nb - hi;
             };
-            auto publish = [&](uint32_t node, uint32_t record) {
+            auto publish = [&](uint32_t j, uint32_t node, uint32_t record) {
                 if (node >= capacity) return;
-                const uint32_t j = atomicAdd(next_count, 1u);
                 next_tasks[j] = record;
-                next_node[j] = node;
             };
-            collapse_node_group(rec, leaf0, tris, active, active ? __ldcg(tasks + i) : 0u,
-                                active ? __ldcg(task_node + i) : 0u, nodes8, tris8, tri_counter, err,
-                                s_group[threadIdx.x >> 5], reserve, publish);
+            collapse_node_group(rec, leaf0, tris, active, active ? __ldcg(tasks + i) : 0u, lo + i, nodes8, tris8, err,
+                                s_group[threadIdx.x >> 5], alloc, publish);
         }
-        if (!grid_barrier(bar, gridDim.x, err)) return;
+        const bool ok = grid_barrier(bar, gridDim.x, err, [&]() {
+            const uint32_t end = ld_acquire_u32(ws);
+            st_relaxed_u32(ws + 5, end < capacity ? end : capacity);
+        });
+        if (!ok) return;
+        lo = hi;
+        hi = ld_acquire_u32(ws + 5);
     }
 }
 
 // Seed of the cooperative collapse: one root task (record `root`, node 0).
-__global__ void k_coop_seed(uint32_t* __restrict__ ws, uint32_t root, uint32_t capacity)
+__global__ void k_coop_seed(uint32_t* __restrict__ ws, uint32_t root)
 {
-    uint32_t* counts = ws + 8;
-    uint32_t* ta = counts + kFixedLevels + 8;
-    ws[0] = 1u;       // node 0 is the root
-    ta[0] = root;
-    ta[capacity] = 0u;  // its node index (na[0])
-    counts[0] = 1u;
+    ws[0] = 1u;  // node 0 is the root
+    ws[8 + kFixedLevels + 8] = root;  // the first task list
 }
 
 __global__ void k_fixed_seed(const uint32_t* __restrict__ roots, uint32_t nroots, uint32_t* __restrict__ tasks,
@@ -1469,7 +1500,6 @@ int build_bvh8_queue(const Node* rec, const uint32_t* roots_dev, uint32_t nroots
     // counts, then two (record, node) task lists of `capacity` entries
     const uint32_t capacity = bvh8_capacity(n) + nroots;
     uint32_t* node_counter = ws;
-    uint32_t* tri_counter = ws + 1;
     uint32_t* counts = ws + 8;
     uint32_t* ta = counts + kFixedLevels + 8;
     uint32_t* na = ta + capacity;
@@ -1491,8 +1521,8 @@ int build_bvh8_queue(const Node* rec, const uint32_t* roots_dev, uint32_t nroots
         uint32_t* in_n = (level & 1) ? nb : na;
         uint32_t* out_t = (level & 1) ? ta : tb;
         uint32_t* out_n = (level & 1) ? na : nb;
-        k_collapse_fixed<<<grid, 128, 0, s>>>(rec, leaf0, tris, level, counts, in_t, in_n, out_t, out_n, node_counter,
-                                              tri_counter, static_cast<Node8*>(nodes8), static_cast<float4*>(tris8),
+        k_collapse_fixed<<<grid, 128, 0, s>>>(rec, leaf0, tris, level, counts, in_t, in_n, out_t, out_n, ws,
+                                              static_cast<Node8*>(nodes8), static_cast<float4*>(tris8),
                                               capacity, err);
     }
     return (int)cudaGetLastError();
@@ -1561,7 +1591,7 @@ int build_bvh8(const Node* rec, uint32_t root, uint32_t leaf0, const float* tris
     const uint32_t capacity = bvh8_capacity(n);
     cudaError_t e;
     if ((e = cudaMemsetAsync(ws, 0, sizeof(uint32_t) * (16 + kFixedLevels), s)) != cudaSuccess) return (int)e;
-    k_coop_seed<<<1, 1, 0, s>>>(ws, root, capacity);
+    k_coop_seed<<<1, 1, 0, s>>>(ws, root);
     void* args[] = {(void*)&rec, (void*)&leaf0, (void*)&tris, (void*)&ws, (void*)&capacity, (void*)&nodes8,
                     (void*)&tris8, (void*)&err};
     if ((e = cudaLaunchCooperativeKernel((const void*)k_collapse_coop, dim3(grid), dim3(256), args, 0, s)) !=

@@ -256,8 +256,10 @@ __global__ void k_combine64(const uint32_t* __restrict__ hi_sorted, const uint32
 // ---------------------------------------------------------------------------
 // climb
 
+// 256 threads and at most 40 registers: six blocks per SM, so more blocks
+// overlap their leaf gathers and global-phase round trips.
 template <class Code>
-__global__ void __launch_bounds__(256) k_lbvh_climb(const Code* __restrict__ codes, const uint32_t* __restrict__ perm,
+__global__ void __launch_bounds__(256, 6) k_lbvh_climb(const Code* __restrict__ codes, const uint32_t* __restrict__ perm,
                                                     const float* __restrict__ tris, uint32_t n, Node* __restrict__ nodes,
                                                     uint32_t* __restrict__ flags, float4* __restrict__ info, uint32_t* err)
 {
