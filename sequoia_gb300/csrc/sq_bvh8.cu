@@ -1041,11 +1041,14 @@ __global__ void __launch_bounds__(128) k_trace8_tiles(const sqk::Trace8Args a, u
     const uint32_t lane = threadIdx.x & 31u;
     const bool camera = a.ray_kind != SQ_RAYS_EXPLICIT;
     const uint32_t tiles_x = (a.width + 7u) >> 3;
+    __shared__ WarpStats s_stats[4];
+    WarpStats& ws = s_stats[threadIdx.x >> 5];
+    ws.reset(lane);
     for (;;) {
         uint32_t b = 0;
         if (lane == 0) b = atomicAdd(a.work, 1u);
         b = __shfl_sync(0xFFFFFFFFu, b, 0);
-        if (b >= batches) return;
+        if (b >= batches) break;
         Ray8 r;
         uint32_t rid = 0;
         bool active;
@@ -1120,14 +1123,7 @@ __global__ void __launch_bounds__(128) k_trace8_tiles(const sqk::Trace8Args a, u
             unsigned long long by = active ? (unsigned long long)(camera ? 0u : 32u) + (a.hits ? 12u : 0u) +
                                                  (a.heat ? 3u : 0u) + 80ull * res.nodes + 48ull * res.tri_tests
                                            : 0ull;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                bt += __shfl_xor_sync(0xFFFFFFFFu, bt, o);
-                tt += __shfl_xor_sync(0xFFFFFFFFu, tt, o);
-                by += __shfl_xor_sync(0xFFFFFFFFu, by, o);
-                nv += __shfl_xor_sync(0xFFFFFFFFu, nv, o);
-            }
-            if (lane == 0) { atomicAdd(a.stats, bt); atomicAdd(a.stats + 1, tt); atomicAdd(a.stats + 2, by); atomicAdd(a.stats + 3, nv); }
+            ws.add(lane, bt, tt, by, nv);
         }
         if (!active) continue;
         if (a.hits) {
@@ -1144,6 +1140,7 @@ __global__ void __launch_bounds__(128) k_trace8_tiles(const sqk::Trace8Args a, u
             hp[0] = v; hp[1] = v; hp[2] = v;
         }
     }
+    if (a.stats) ws.flush(lane, a.stats);
 }
 
 template <int MODE>
@@ -1279,11 +1276,14 @@ __global__ void __launch_bounds__(256) k_trace8_batch_tiles(const sqk::BatchTrac
 {
     const uint32_t lane = threadIdx.x & 31u;
     const Node8* nodes = static_cast<const Node8*>(a.nodes8);
+    __shared__ WarpStats s_stats[8];
+    WarpStats& ws = s_stats[threadIdx.x >> 5];
+    ws.reset(lane);
     for (;;) {
         uint32_t b = 0;
         if (lane == 0) b = atomicAdd(a.work, 1u);
         b = __shfl_sync(0xFFFFFFFFu, b, 0);
-        if (b >= a.total_batches) return;
+        if (b >= a.total_batches) break;
         const uint32_t j = find_job(a.jobs, a.njobs, b);
         const sqk::BatchJob& job = a.jobs[j];
         const uint32_t lb = b - job.batch_begin;
@@ -1322,14 +1322,7 @@ __global__ void __launch_bounds__(256) k_trace8_batch_tiles(const sqk::BatchTrac
                                                  (a.hits ? 12u : 0u) + (a.heat ? 3u : 0u) + 80ull * res.nodes +
                                                  48ull * res.tri_tests
                                            : 0ull;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                bt += __shfl_xor_sync(0xFFFFFFFFu, bt, o);
-                tt += __shfl_xor_sync(0xFFFFFFFFu, tt, o);
-                by += __shfl_xor_sync(0xFFFFFFFFu, by, o);
-                nv += __shfl_xor_sync(0xFFFFFFFFu, nv, o);
-            }
-            if (lane == 0) { atomicAdd(a.stats, bt); atomicAdd(a.stats + 1, tt); atomicAdd(a.stats + 2, by); atomicAdd(a.stats + 3, nv); }
+            ws.add(lane, bt, tt, by, nv);
         }
         if (!active) continue;
         const uint64_t out = (uint64_t)job.out_offset + rid;
@@ -1347,6 +1340,7 @@ __global__ void __launch_bounds__(256) k_trace8_batch_tiles(const sqk::BatchTrac
             hp[0] = v; hp[1] = v; hp[2] = v;
         }
     }
+    if (a.stats) ws.flush(lane, a.stats);
 }
 
 template <int MODE>

@@ -146,6 +146,39 @@ __device__ __forceinline__ void raise_error(uint32_t* err, uint32_t bit)
 
 constexpr int kNumSMs = 152;
 
+// Trace statistics of one warp (box tests, triangle tests, requested bytes,
+// node visits), summed over the warp's tiles in shared memory by lane 0 and
+// added to the four global counters once, when the warp finishes: one atomic
+// per counter per warp instead of one per tile, since same-address atomics
+// serialise in L2.
+struct WarpStats {
+    unsigned long long v[4];
+    __device__ __forceinline__ void reset(uint32_t lane)
+    {
+        if (lane == 0) v[0] = v[1] = v[2] = v[3] = 0ull;
+    }
+    __device__ __forceinline__ void add(uint32_t lane, unsigned long long a, unsigned long long b,
+                                        unsigned long long c, unsigned long long d)
+    {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_xor_sync(0xFFFFFFFFu, a, o);
+            b += __shfl_xor_sync(0xFFFFFFFFu, b, o);
+            c += __shfl_xor_sync(0xFFFFFFFFu, c, o);
+            d += __shfl_xor_sync(0xFFFFFFFFu, d, o);
+        }
+        if (lane == 0) { v[0] += a; v[1] += b; v[2] += c; v[3] += d; }
+    }
+    __device__ __forceinline__ void flush(uint32_t lane, unsigned long long* g)
+    {
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (v[k]) atomicAdd(g + k, v[k]);
+        }
+    }
+};
+
 }  // namespace sq
 
 // ---------------------------------------------------------------------------

@@ -20,11 +20,11 @@
 //
 // Schedule:
 //   large nodes (> kSmall triangles): level by level.  Chunks of kChunk
-//     triangles bin into per-warp shared bins (warp-aggregated with
-//     __match_any_sync + __reduce_max_sync on order-preserving integer
-//     encodings), then one atomic per bin value and block; one warp per node
-//     sweeps the planes; a count / scan / scatter triple partitions stably
-//     into the other id buffer.
+//     triangles bin into per-warp shared bins (shared-memory atomics on
+//     order-preserving integer encodings, or full-warp reductions when a
+//     warp's 32 triangles share one bin), then one atomic per bin value and
+//     block; one warp per node sweeps the planes; a count / scan / scatter
+//     triple partitions stably into the other id buffer.
 //   small nodes: one warp per subtree, smaller child first (stack depth
 //     O(log n)), binning and partitioning with warp intrinsics only.
 #include "sq_common.cuh"
@@ -300,8 +300,6 @@ __global__ void k_grid_heap(Node* __restrict__ nodes)
 __device__ __forceinline__ void warp_bin_add(uint32_t* __restrict__ wb, int bin, int nb, const float* mn, const float* mx,
                                              const float* c)
 {
-    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, (uint32_t)bin);
-    const int leader = __ffs(peers) - 1;
     const int lane = threadIdx.x & 31;
     uint32_t e[12];
 #pragma unroll
@@ -311,13 +309,26 @@ __device__ __forceinline__ void warp_bin_add(uint32_t* __restrict__ wb, int bin,
         e[6 + a] = float_to_ordered(-c[a]);
         e[9 + a] = float_to_ordered(c[a]);
     }
+    const int b0 = __shfl_sync(0xFFFFFFFFu, bin, 0);
+    if (__all_sync(0xFFFFFFFFu, bin == b0)) {
+        // the whole warp in one bin: full-warp reductions and one writer
+        if (b0 < nb) {
 #pragma unroll
-    for (int k = 0; k < 12; ++k) e[k] = __reduce_max_sync(peers, e[k]);
-    if (lane == leader && bin < nb) {
+            for (int k = 0; k < 12; ++k) e[k] = __reduce_max_sync(0xFFFFFFFFu, e[k]);
+            if (lane == 0) {
+                uint32_t* b = wb + b0 * kBinWords;
+#pragma unroll
+                for (int k = 0; k < 12; ++k) b[k] = max(b[k], e[k]);
+                b[12] += 32u;
+            }
+        }
+    } else if (bin < nb) {
+        // lanes spread over bins: shared-memory atomics per lane (reductions
+        // with per-bin masks would run once per distinct bin)
         uint32_t* b = wb + bin * kBinWords;
 #pragma unroll
-        for (int k = 0; k < 12; ++k) b[k] = max(b[k], e[k]);
-        b[12] += __popc(peers);
+        for (int k = 0; k < 12; ++k) atomicMax(b + k, e[k]);
+        atomicAdd(b + 12, 1u);
     }
     __syncwarp();
 }

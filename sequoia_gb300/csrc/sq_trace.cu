@@ -354,11 +354,14 @@ __global__ void __launch_bounds__(128) k_trace(const sqk::TraceArgs a, uint32_t 
     const uint32_t lane = threadIdx.x & 31u;
     const bool camera = a.ray_kind != SQ_RAYS_EXPLICIT;
     const uint32_t tiles_x = (a.width + 7u) >> 3;
+    __shared__ WarpStats s_stats[4];
+    WarpStats& ws = s_stats[threadIdx.x >> 5];
+    ws.reset(lane);
     for (;;) {
         uint32_t b = 0;
         if (lane == 0) b = atomicAdd(a.work, 1u);
         b = __shfl_sync(0xFFFFFFFFu, b, 0);
-        if (b >= batches) return;
+        if (b >= batches) break;
         Ray r;
         uint32_t rid = 0;
         bool active;
@@ -397,13 +400,7 @@ __global__ void __launch_bounds__(128) k_trace(const sqk::TraceArgs a, uint32_t 
             unsigned long long by = active ? (unsigned long long)(camera ? 0u : 32u) + (a.hits ? 12u : 0u) +
                                                  (a.heat ? 3u : 0u) + 32ull * res.tests + 36ull * res.tri_tests
                                            : 0ull;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                bt += __shfl_xor_sync(0xFFFFFFFFu, bt, o);
-                tt += __shfl_xor_sync(0xFFFFFFFFu, tt, o);
-                by += __shfl_xor_sync(0xFFFFFFFFu, by, o);
-            }
-            if (lane == 0) { atomicAdd(a.stats, bt); atomicAdd(a.stats + 1, tt); atomicAdd(a.stats + 2, by); atomicAdd(a.stats + 3, bt); }
+            ws.add(lane, bt, tt, by, bt);
         }
         if (!active) continue;
         if (a.hits) {
@@ -420,6 +417,7 @@ __global__ void __launch_bounds__(128) k_trace(const sqk::TraceArgs a, uint32_t 
             hp[0] = v; hp[1] = v; hp[2] = v;
         }
     }
+    if (a.stats) ws.flush(lane, a.stats);
 }
 
 template <int MODE>
@@ -450,11 +448,14 @@ template <int MODE>
 __global__ void __launch_bounds__(256) k_trace_batch(const sqk::BatchTraceArgs a)
 {
     const uint32_t lane = threadIdx.x & 31u;
+    __shared__ WarpStats s_stats[8];
+    WarpStats& ws = s_stats[threadIdx.x >> 5];
+    ws.reset(lane);
     for (;;) {
         uint32_t b = 0;
         if (lane == 0) b = atomicAdd(a.work, 1u);
         b = __shfl_sync(0xFFFFFFFFu, b, 0);
-        if (b >= a.total_batches) return;
+        if (b >= a.total_batches) break;
         const uint32_t j = find_job(a.jobs, a.njobs, b);
         const sqk::BatchJob& job = a.jobs[j];
         const uint32_t lb = b - job.batch_begin;
@@ -497,13 +498,7 @@ __global__ void __launch_bounds__(256) k_trace_batch(const sqk::BatchTraceArgs a
                                                  (a.hits ? 12u : 0u) + (a.heat ? 3u : 0u) + 32ull * res.tests +
                                                  36ull * res.tri_tests
                                            : 0ull;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                bt += __shfl_xor_sync(0xFFFFFFFFu, bt, o);
-                tt += __shfl_xor_sync(0xFFFFFFFFu, tt, o);
-                by += __shfl_xor_sync(0xFFFFFFFFu, by, o);
-            }
-            if (lane == 0) { atomicAdd(a.stats, bt); atomicAdd(a.stats + 1, tt); atomicAdd(a.stats + 2, by); atomicAdd(a.stats + 3, bt); }
+            ws.add(lane, bt, tt, by, bt);
         }
         if (!active) continue;
         const uint64_t out = (uint64_t)job.out_offset + rid;
@@ -521,6 +516,7 @@ __global__ void __launch_bounds__(256) k_trace_batch(const sqk::BatchTraceArgs a
             hp[0] = v; hp[1] = v; hp[2] = v;
         }
     }
+    if (a.stats) ws.flush(lane, a.stats);
 }
 
 template <int MODE>
