@@ -673,24 +673,89 @@ __device__ __forceinline__ bool no_nan_slabs(const Pre8& r)
 // 8 * 2^-24 * M (plus subnormal absolute errors well under 2^-125), so the
 // affine near distance is never above, and the far never below, what the
 // exact form computes for the same quantised box, which in turn is never
-// tighter than the FP32 box.  The test therefore passes for every child the
-// exact test passes (it may pass a few more), and the hits are unchanged.
-// A node whose M is not finite (coordinates near FLT_MAX) uses the exact form.
+// tighter than the FP32 box.
+//
+// Two more terms are folded into the per-node constants:
+//   - the byte enters as the float x = 1 + q * 2^-15 (one byte permute into
+//     the mantissa), so t = x * A' + (C - A') with A' = 2^15 * A (exact).
+//     C - A' is rounded down for the near constant and up for the far one,
+//     which only widens the box (by at most 2^-8 of a quantisation step);
+//   - the traversal's robust factor on the far distance (f * (1 + 2^-21))
+//     becomes D = 2^-20 * (M + E) added to the far constant: every far
+//     distance is at most M + E plus roundings, so D covers f * 2^-21 and
+//     the rounding of the product with room to spare.
+// The test therefore passes for every child the exact test passes (it may
+// pass a few more), and the hits are unchanged.  A node whose constants are
+// not all finite (coordinates near FLT_MAX) uses the exact form.
 __device__ __forceinline__ bool node_affine(const float* org, const float* sc, const Pre8& rp, float* A, float* Cn,
                                             float* Cf)
 {
     float msum = 0.0f;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        A[a] = sc[a] * rp.inv[a];
+        const float A1 = sc[a] * rp.inv[a];
         const float C = (org[a] - rp.o[a]) * rp.inv[a];
         const float M = (fmaf(255.0f, sc[a], fabsf(org[a]) + fabsf(rp.o[a])) + 0x1p-126f) * fabsf(rp.inv[a]);
         const float E = fmaf(M, 0x1p-19f, 0x1p-125f);
-        Cn[a] = C - E;
-        Cf[a] = C + E;
-        msum += M;
+        const float D = fmaf(M + E, 0x1p-20f, 0x1p-125f);
+        A[a] = A1 * 32768.0f;
+        Cn[a] = __fsub_rd(C - E, A[a]);
+        Cf[a] = __fsub_ru(__fadd_ru(C + E, D), A[a]);
+        msum += M + fabsf(A[a]) + fabsf(Cn[a]) + fabsf(Cf[a]);
     }
     return isfinite(msum);
+}
+
+// x = 1 + q * 2^-15 for byte j of a word of quantised planes
+__device__ __forceinline__ float qunit(uint32_t word, uint32_t j)
+{
+    return __uint_as_float(__byte_perm(word, 0x3F800000u, 0x7604u | (j << 4)));
+}
+
+__device__ __forceinline__ float max3f(float a, float b, float c)
+{
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c)
+{
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+// Entry and exit distances of child slot k (word w = k / 4, byte j = k % 4).
+// The affine form's exit already carries the robust factor; the exact forms
+// apply it here.
+template <bool AFF, bool SIGNED>
+__device__ __forceinline__ void child_span(const uint32_t* qa, const uint32_t* qb, int w, uint32_t j, const float* A,
+                                           const float* Cn, const float* Cf, const float* sc, const float* org,
+                                           const Pre8& rp, float& n, float& f)
+{
+    float ta[3], tb[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (AFF) {
+            ta[a] = fmaf(qunit(qa[a * 2 + w], j), A[a], Cn[a]);
+            tb[a] = fmaf(qunit(qb[a * 2 + w], j), A[a], Cf[a]);
+        } else {
+            const float ba = fmaf(qbyte(qa[a * 2 + w], j), sc[a], org[a]);
+            const float bb = fmaf(qbyte(qb[a * 2 + w], j), sc[a], org[a]);
+            ta[a] = (ba - rp.o[a]) * rp.inv[a];
+            tb[a] = (bb - rp.o[a]) * rp.inv[a];
+        }
+    }
+    if (AFF) {
+        n = fmaxf(max3f(ta[0], ta[1], ta[2]), rp.tmin);
+        f = min3f(tb[0], tb[1], tb[2]);
+    } else if (SIGNED) {
+        n = fmaxf(fmaxf(fmaxf(ta[0], ta[1]), ta[2]), rp.tmin);
+        f = fminf(fminf(tb[0], tb[1]), tb[2]) * kRobust;
+    } else {
+        n = fmaxf(fmaxf(fmaxf(fminf(ta[0], tb[0]), fminf(ta[1], tb[1])), fminf(ta[2], tb[2])), rp.tmin);
+        f = fminf(fminf(fmaxf(ta[0], tb[0]), fmaxf(ta[1], tb[1])), fmaxf(ta[2], tb[2])) * kRobust;
+    }
 }
 
 struct Res8 {
@@ -758,31 +823,9 @@ __device__ Res8 trace8_impl(const Node8* __restrict__ nodes, uint32_t root, cons
                 const uint32_t cnt = (counts >> (4 * k)) & 0xFu;
                 const bool is_inner = (imask >> k) & 1u;
                 if ((valid >> k) & 1u) {
-                    const int w = k >> 2;
-                    const uint32_t j = (uint32_t)(k & 3);
-                    float ta[3], tb[3];
-#pragma unroll
-                    for (int a = 0; a < 3; ++a) {
-                        if (AFF) {
-                            ta[a] = fmaf(qbyte(qa[a * 2 + w], j), A[a], Cn[a]);
-                            tb[a] = fmaf(qbyte(qb[a * 2 + w], j), A[a], Cf[a]);
-                        } else {
-                            const float ba = fmaf(qbyte(qa[a * 2 + w], j), sc[a], org[a]);
-                            const float bb = fmaf(qbyte(qb[a * 2 + w], j), sc[a], org[a]);
-                            ta[a] = (ba - rp.o[a]) * rp.inv[a];
-                            tb[a] = (bb - rp.o[a]) * rp.inv[a];
-                        }
-                    }
-                    tests++;
                     float n, f;
-                    if (SIGNED) {
-                        n = fmaxf(fmaxf(fmaxf(ta[0], ta[1]), ta[2]), rp.tmin);
-                        f = fminf(fminf(tb[0], tb[1]), tb[2]);
-                    } else {
-                        n = fmaxf(fmaxf(fmaxf(fminf(ta[0], tb[0]), fminf(ta[1], tb[1])), fminf(ta[2], tb[2])), rp.tmin);
-                        f = fminf(fminf(fmaxf(ta[0], tb[0]), fmaxf(ta[1], tb[1])), fmaxf(ta[2], tb[2]));
-                    }
-                    f = f * kRobust;
+                    child_span<AFF, SIGNED>(qa, qb, k >> 2, (uint32_t)(k & 3), A, Cn, Cf, sc, org, rp, n, f);
+                    tests++;
                     if (n <= f && n <= best_t * kRobust) {
                         const uint32_t ent = is_inner ? (child_base + inner_rank)
                                                       : (0x80000000u | (cnt << 27) | (tri_base + tri_off));
@@ -949,31 +992,9 @@ __device__ __forceinline__ void visit8(Lane8& L, const Node8* __restrict__ nodes
             const uint32_t cnt = (counts >> (4 * k)) & 0xFu;
             const bool is_inner = (imask >> k) & 1u;
             if ((valid >> k) & 1u) {
-                const int w = k >> 2;
-                const uint32_t j = (uint32_t)(k & 3);
-                float ta[3], tb[3];
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    if (AFF) {
-                        ta[a] = fmaf(qbyte(qa[a * 2 + w], j), A[a], Cn[a]);
-                        tb[a] = fmaf(qbyte(qb[a * 2 + w], j), A[a], Cf[a]);
-                    } else {
-                        const float ba = fmaf(qbyte(qa[a * 2 + w], j), sc[a], org[a]);
-                        const float bb = fmaf(qbyte(qb[a * 2 + w], j), sc[a], org[a]);
-                        ta[a] = (ba - rp.o[a]) * rp.inv[a];
-                        tb[a] = (bb - rp.o[a]) * rp.inv[a];
-                    }
-                }
-                L.tests++;
                 float n, f;
-                if (SIGNED) {
-                    n = fmaxf(fmaxf(fmaxf(ta[0], ta[1]), ta[2]), rp.tmin);
-                    f = fminf(fminf(tb[0], tb[1]), tb[2]);
-                } else {
-                    n = fmaxf(fmaxf(fmaxf(fminf(ta[0], tb[0]), fminf(ta[1], tb[1])), fminf(ta[2], tb[2])), rp.tmin);
-                    f = fminf(fminf(fmaxf(ta[0], tb[0]), fmaxf(ta[1], tb[1])), fmaxf(ta[2], tb[2]));
-                }
-                f = f * kRobust;
+                child_span<AFF, SIGNED>(qa, qb, k >> 2, (uint32_t)(k & 3), A, Cn, Cf, sc, org, rp, n, f);
+                L.tests++;
                 if (n <= f && n <= lim) {
                     uint32_t ent = is_inner ? (child_base + inner_rank) : (0x80000000u | (cnt << 27) | (tri_base + tri_off));
                     float et = n;
