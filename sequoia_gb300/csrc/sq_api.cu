@@ -78,6 +78,21 @@ bool is_device_ptr(const void* p)
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// The device address of page-locked host memory (cudaHostAlloc /
+// cudaHostRegister), or null for any other pointer.  Kernels write results
+// there directly: the transfer to the host overlaps the kernel instead of
+// following it as a copy.
+void* pinned_device_alias(const void* p)
+{
+    if (!p) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 sq_status check_device_error(sq_ctx* c, uint32_t* bits_out)
 {
     uint32_t bits = 0;
@@ -668,18 +683,21 @@ sq_status sq_trace(sq_ctx* c, const sq_bvh* b, const sq_ray_source* rays, uint32
     if (count > 0xFFFFFFFFull / 3) return fail(c, SQ_ERR_INVALID, "sq_trace: too many rays");
     const bool hits_dev = hits && is_device_ptr(hits);
     const bool heat_dev = heatmap_rgb && is_device_ptr(heatmap_rgb);
+    // page-locked host outputs are written by the kernel in place
+    sq_hit* hits_map = (hits && !hits_dev) ? static_cast<sq_hit*>(pinned_device_alias(hits)) : nullptr;
+    uint8_t* heat_map = (heatmap_rgb && !heat_dev) ? static_cast<uint8_t*>(pinned_device_alias(heatmap_rgb)) : nullptr;
     sq_hit* hits_tmp = nullptr;
     uint8_t* heat_tmp = nullptr;
-    if (hits && !hits_dev) {
+    if (hits && !hits_dev && !hits_map) {
         hits_tmp = static_cast<sq_hit*>(dalloc(c, sizeof(sq_hit) * count));
         if (!hits_tmp) { dfree(c, rays_own); return fail(c, SQ_ERR_OOM, "hit buffer allocation failed"); }
     }
-    if (heatmap_rgb && !heat_dev) {
+    if (heatmap_rgb && !heat_dev && !heat_map) {
         heat_tmp = static_cast<uint8_t*>(dalloc(c, 3ull * count));
         if (!heat_tmp) { dfree(c, rays_own); dfree(c, hits_tmp); return fail(c, SQ_ERR_OOM, "heatmap allocation failed"); }
     }
-    a.hits = hits_dev ? hits : hits_tmp;
-    a.heat = heat_dev ? heatmap_rgb : heat_tmp;
+    a.hits = hits_dev ? hits : (hits_map ? hits_map : hits_tmp);
+    a.heat = heat_dev ? heatmap_rgb : (heat_map ? heat_map : heat_tmp);
     a.work = c->ctrl + 1;
     a.err = c->ctrl;
     a.stats = reinterpret_cast<unsigned long long*>(c->ctrl + 4);
@@ -718,7 +736,7 @@ sq_status sq_trace(sq_ctx* c, const sq_bvh* b, const sq_ray_source* rays, uint32
     if (hits_tmp) SQ_CUDA(c, cudaMemcpyAsync(hits, hits_tmp, sizeof(sq_hit) * count, cudaMemcpyDeviceToHost, s));
     if (heat_tmp) SQ_CUDA(c, cudaMemcpyAsync(heatmap_rgb, heat_tmp, 3ull * count, cudaMemcpyDeviceToHost, s));
     sq_status st = SQ_OK;
-    if (hits_tmp || heat_tmp) st = check_device_error(c, nullptr);
+    if (hits_tmp || heat_tmp || hits_map || heat_map) st = check_device_error(c, nullptr);
     dfree(c, rays_own);
     dfree(c, hits_tmp);
     dfree(c, heat_tmp);

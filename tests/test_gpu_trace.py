@@ -79,6 +79,26 @@ def test_trace_explicit_random_rays(ctx, oracle):
     assert np.array_equal(hits["t"], bts)
 
 
+def test_trace_into_pinned_host_buffers(ctx):
+    """Page-locked host outputs are written by the kernel in place; the
+    results equal those written to pageable host arrays (through a copy)."""
+    torch = pytest.importorskip("torch")
+    from sequoia_gb300 import scenes
+    tris = scenes.gaussian_soup(200_000, 16, seed=33)
+    lo, hi = scenes.scene_box(tris)
+    rays = scenes.random_rays(60_000, lo, hi, seed=34)
+    for wide in (False, True):
+        bvh = ctx.build(tris, "morton", wide=wide)
+        for kw in (dict(rays=rays), dict(camera="pinhole", width=320, height=200, origin=(0, 0, -40), target=(0, 0, 0))):
+            ref_hits, ref_heat = ctx.trace(bvh, "closest", heatmap=True, **kw)
+            count = len(ref_hits)
+            p_hits = torch.zeros(count * 3, dtype=torch.int32).pin_memory()
+            p_heat = torch.zeros(count * 3, dtype=torch.uint8).pin_memory()
+            ctx.trace(bvh, "closest", hits=p_hits, heatmap=p_heat, **kw)
+            assert np.array_equal(p_hits.numpy().view(np.uint8), ref_hits.view(np.uint8))
+            assert np.array_equal(p_heat.numpy(), ref_heat)
+
+
 def test_closest_t_vs_fp64(ctx, oracle):
     """Closest-hit t is bit-identical to the oracle (so within any relative
     tolerance of it, 1e-6 included); its error against an FP64 re-intersection
