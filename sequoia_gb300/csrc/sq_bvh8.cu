@@ -683,7 +683,8 @@ __device__ __forceinline__ bool no_nan_slabs(const Pre8& r)
 //   - the traversal's robust factor on the far distance (f * (1 + 2^-21))
 //     becomes D = 2^-20 * (M + E) added to the far constant: every far
 //     distance is at most M + E plus roundings, so D covers f * 2^-21 and
-//     the rounding of the product with room to spare.
+//     the rounding of the product with room to spare.  The far constant
+//     takes E + D <= 1.5625 * 2^-19 * M + 2^-123 in one term.
 // The test therefore passes for every child the exact test passes (it may
 // pass a few more), and the hits are unchanged.  A node whose constants are
 // not all finite (coordinates near FLT_MAX) uses the exact form.
@@ -697,11 +698,12 @@ __device__ __forceinline__ bool node_affine(const float* org, const float* sc, c
         const float C = (org[a] - rp.o[a]) * rp.inv[a];
         const float M = (fmaf(255.0f, sc[a], fabsf(org[a]) + fabsf(rp.o[a])) + 0x1p-126f) * fabsf(rp.inv[a]);
         const float E = fmaf(M, 0x1p-19f, 0x1p-125f);
-        const float D = fmaf(M + E, 0x1p-20f, 0x1p-125f);
+        const float ED = fmaf(M, 0x1.9p-19f, 0x1p-123f);
         A[a] = A1 * 32768.0f;
         Cn[a] = __fsub_rd(C - E, A[a]);
-        Cf[a] = __fsub_ru(__fadd_ru(C + E, D), A[a]);
-        msum += M + fabsf(A[a]) + fabsf(Cn[a]) + fabsf(Cf[a]);
+        Cf[a] = __fsub_ru(__fadd_ru(C, ED), A[a]);
+        // an infinite or NaN M, A or C reaches one of these two
+        msum += fabsf(Cn[a]) + fabsf(Cf[a]);
     }
     return isfinite(msum);
 }
@@ -815,18 +817,19 @@ __device__ Res8 trace8_impl(const Node8* __restrict__ nodes, uint32_t root, cons
         float A[3], Cn[3], Cf[3];
         const bool aff = SIGNED && node_affine(org, sc, rp, A, Cn, Cf);
         // the child loop, compiled once per distance form (branching per node,
-        // not per child, keeps one form's registers live at a time)
+        // not per child, keeps one form's registers live at a time).  Every
+        // slot is tested without a branch (lanes at different nodes have
+        // different valid masks); the valid bit joins the hit condition.
         auto scan = [&](auto form) {
             constexpr bool AFF = decltype(form)::value;
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
                 const uint32_t cnt = (counts >> (4 * k)) & 0xFu;
                 const bool is_inner = (imask >> k) & 1u;
-                if ((valid >> k) & 1u) {
+                {
                     float n, f;
                     child_span<AFF, SIGNED>(qa, qb, k >> 2, (uint32_t)(k & 3), A, Cn, Cf, sc, org, rp, n, f);
-                    tests++;
-                    if (n <= f && n <= best_t * kRobust) {
+                    if (((valid >> k) & 1u) && n <= f && n <= best_t * kRobust) {
                         const uint32_t ent = is_inner ? (child_base + inner_rank)
                                                       : (0x80000000u | (cnt << 27) | (tri_base + tri_off));
                         int b = nh - 1;
@@ -840,6 +843,7 @@ __device__ Res8 trace8_impl(const Node8* __restrict__ nodes, uint32_t root, cons
                 tri_off += cnt;
             }
         };
+        tests += __popc(valid);
         if (aff) scan(std::true_type{});
         else scan(std::false_type{});
         if (sp + nh > kStack8) { overflow = true; break; }
@@ -991,11 +995,10 @@ __device__ __forceinline__ void visit8(Lane8& L, const Node8* __restrict__ nodes
         for (int k = 0; k < 8; ++k) {
             const uint32_t cnt = (counts >> (4 * k)) & 0xFu;
             const bool is_inner = (imask >> k) & 1u;
-            if ((valid >> k) & 1u) {
+            {
                 float n, f;
                 child_span<AFF, SIGNED>(qa, qb, k >> 2, (uint32_t)(k & 3), A, Cn, Cf, sc, org, rp, n, f);
-                L.tests++;
-                if (n <= f && n <= lim) {
+                if (((valid >> k) & 1u) && n <= f && n <= lim) {
                     uint32_t ent = is_inner ? (child_base + inner_rank) : (0x80000000u | (cnt << 27) | (tri_base + tri_off));
                     float et = n;
                     if (near_e == kNoHit) {
@@ -1032,6 +1035,7 @@ __device__ __forceinline__ void visit8(Lane8& L, const Node8* __restrict__ nodes
             tri_off += cnt;
         }
     };
+    L.tests += __popc(valid);
     if (aff) scan(std::true_type{});
     else scan(std::false_type{});
     if (L.overflow) { L.cur = kNoHit; return; }
