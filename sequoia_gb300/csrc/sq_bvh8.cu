@@ -727,6 +727,24 @@ __device__ __forceinline__ float min3f(float a, float b, float c)
     return r;
 }
 
+// Sum of the 4-bit triangle counts of slots [0, k) of a node's count word.
+__device__ __forceinline__ uint32_t slots_below(uint32_t counts, int k)
+{
+    const uint32_t x = k >= 8 ? counts : counts & ((1u << (4 * k)) - 1u);
+    const uint32_t s = (x & 0x0F0F0F0Fu) + ((x >> 4) & 0x0F0F0F0Fu);
+    return (s * 0x01010101u) >> 24;
+}
+
+// Stack entry of child slot k: an inner child's node index, or a leaf
+// child's triangle range (bit 31, count in bits 27-30, first triangle).
+// Computed only for children that pass their box test.
+__device__ __forceinline__ uint32_t child_entry(uint32_t imask, uint32_t child_base, uint32_t counts, uint32_t tri_base,
+                                                int k)
+{
+    if ((imask >> k) & 1u) return child_base + __popc(imask & ((1u << k) - 1u));
+    return 0x80000000u | (((counts >> (4 * k)) & 0xFu) << 27) | (tri_base + slots_below(counts, k));
+}
+
 // Entry and exit distances of child slot k (word w = k / 4, byte j = k % 4).
 // The affine form's exit already carries the robust factor; the exact forms
 // apply it here.
@@ -813,7 +831,6 @@ __device__ Res8 trace8_impl(const Node8* __restrict__ nodes, uint32_t root, cons
         uint32_t hn[8];
         float ht[8];
         int nh = 0;
-        uint32_t inner_rank = 0, tri_off = 0;
         float A[3], Cn[3], Cf[3];
         const bool aff = SIGNED && node_affine(org, sc, rp, A, Cn, Cf);
         // the child loop, compiled once per distance form (branching per node,
@@ -824,14 +841,11 @@ __device__ Res8 trace8_impl(const Node8* __restrict__ nodes, uint32_t root, cons
             constexpr bool AFF = decltype(form)::value;
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
-                const uint32_t cnt = (counts >> (4 * k)) & 0xFu;
-                const bool is_inner = (imask >> k) & 1u;
                 {
                     float n, f;
                     child_span<AFF, SIGNED>(qa, qb, k >> 2, (uint32_t)(k & 3), A, Cn, Cf, sc, org, rp, n, f);
                     if (((valid >> k) & 1u) && n <= f && n <= best_t * kRobust) {
-                        const uint32_t ent = is_inner ? (child_base + inner_rank)
-                                                      : (0x80000000u | (cnt << 27) | (tri_base + tri_off));
+                        const uint32_t ent = child_entry(imask, child_base, counts, tri_base, k);
                         int b = nh - 1;
                         while (b >= 0 && ht[b] > n) { hn[b + 1] = hn[b]; ht[b + 1] = ht[b]; --b; }
                         hn[b + 1] = ent;
@@ -839,8 +853,6 @@ __device__ Res8 trace8_impl(const Node8* __restrict__ nodes, uint32_t root, cons
                         nh++;
                     }
                 }
-                inner_rank += is_inner;
-                tri_off += cnt;
             }
         };
         tests += __popc(valid);
@@ -985,7 +997,6 @@ __device__ __forceinline__ void visit8(Lane8& L, const Node8* __restrict__ nodes
     uint32_t near_e = kNoHit;
     float near_t = 0.0f;
     const int seg = L.sp;
-    uint32_t inner_rank = 0, tri_off = 0;
     float A[3], Cn[3], Cf[3];
     const bool aff = SIGNED && node_affine(org, sc, rp, A, Cn, Cf);
     // the child loop, compiled once per distance form (see the tiles path)
@@ -993,13 +1004,11 @@ __device__ __forceinline__ void visit8(Lane8& L, const Node8* __restrict__ nodes
         constexpr bool AFF = decltype(form)::value;
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-            const uint32_t cnt = (counts >> (4 * k)) & 0xFu;
-            const bool is_inner = (imask >> k) & 1u;
             {
                 float n, f;
                 child_span<AFF, SIGNED>(qa, qb, k >> 2, (uint32_t)(k & 3), A, Cn, Cf, sc, org, rp, n, f);
                 if (((valid >> k) & 1u) && n <= f && n <= lim) {
-                    uint32_t ent = is_inner ? (child_base + inner_rank) : (0x80000000u | (cnt << 27) | (tri_base + tri_off));
+                    uint32_t ent = child_entry(imask, child_base, counts, tri_base, k);
                     float et = n;
                     if (near_e == kNoHit) {
                         near_e = ent;
@@ -1031,8 +1040,6 @@ __device__ __forceinline__ void visit8(Lane8& L, const Node8* __restrict__ nodes
                     }
                 }
             }
-            inner_rank += is_inner;
-            tri_off += cnt;
         }
     };
     L.tests += __popc(valid);
