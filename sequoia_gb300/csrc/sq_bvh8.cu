@@ -747,8 +747,11 @@ __device__ __forceinline__ uint32_t child_entry(uint32_t imask, uint32_t child_b
 
 // Entry and exit distances of child slot k (word w = k / 4, byte j = k % 4).
 // The affine form's exit already carries the robust factor; the exact forms
-// apply it here.
-template <bool AFF, bool SIGNED>
+// apply it here.  PAIR: the near and far planes of an axis in one paired
+// fp32 fma (fma.rn.f32x2: two independent IEEE fmas, one issue slot), which
+// pays in the per-ray tiles loop; the refill loop keeps scalar fmas (the
+// pairs raise its register count past its occupancy step).
+template <bool AFF, bool SIGNED, bool PAIR = false>
 __device__ __forceinline__ void child_span(const uint32_t* qa, const uint32_t* qb, int w, uint32_t j, const float* A,
                                            const float* Cn, const float* Cf, const float* sc, const float* org,
                                            const Pre8& rp, float& n, float& f)
@@ -756,7 +759,14 @@ __device__ __forceinline__ void child_span(const uint32_t* qa, const uint32_t* q
     float ta[3], tb[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        if (AFF) {
+        if (AFF && PAIR) {
+            unsigned long long X, AA, CC, R;
+            asm("mov.b64 %0, {%1, %2};" : "=l"(X) : "f"(qunit(qa[a * 2 + w], j)), "f"(qunit(qb[a * 2 + w], j)));
+            asm("mov.b64 %0, {%1, %2};" : "=l"(AA) : "f"(A[a]), "f"(A[a]));
+            asm("mov.b64 %0, {%1, %2};" : "=l"(CC) : "f"(Cn[a]), "f"(Cf[a]));
+            asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(R) : "l"(X), "l"(AA), "l"(CC));
+            asm("mov.b64 {%0, %1}, %2;" : "=f"(ta[a]), "=f"(tb[a]) : "l"(R));
+        } else if (AFF) {
             ta[a] = fmaf(qunit(qa[a * 2 + w], j), A[a], Cn[a]);
             tb[a] = fmaf(qunit(qb[a * 2 + w], j), A[a], Cf[a]);
         } else {
@@ -843,7 +853,7 @@ __device__ Res8 trace8_impl(const Node8* __restrict__ nodes, uint32_t root, cons
             for (int k = 0; k < 8; ++k) {
                 {
                     float n, f;
-                    child_span<AFF, SIGNED>(qa, qb, k >> 2, (uint32_t)(k & 3), A, Cn, Cf, sc, org, rp, n, f);
+                    child_span<AFF, SIGNED, true>(qa, qb, k >> 2, (uint32_t)(k & 3), A, Cn, Cf, sc, org, rp, n, f);
                     if (((valid >> k) & 1u) && n <= f && n <= best_t * kRobust) {
                         const uint32_t ent = child_entry(imask, child_base, counts, tri_base, k);
                         int b = nh - 1;
