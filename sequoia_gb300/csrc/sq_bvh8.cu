@@ -156,6 +156,9 @@ __device__ void collapse_node_group(const Node* __restrict__ rec, uint32_t leaf0
         e_cnt = node_count(e_node.count_flags);
         if (node_is_leaf(e_node.count_flags)) e_kind = 2;
         else e_kind = (e_node.child < leaf0 && e_cnt > 0) ? 0u : 1u;
+        // the records an opening of this entry would load, towards L2 now:
+        // the collapse is a chain of dependent record loads
+        if (e_kind != 2 && e_cnt > 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(rec + e_node.child));
     };
     if (active && k < (int)cn) load_entry(c0 + (uint32_t)k);
     // the start set is a binary record's two children or a cluster's leaves;
@@ -1185,8 +1188,11 @@ __global__ void __launch_bounds__(128) k_trace8_tiles(const sqk::Trace8Args a, u
     if (a.stats) ws.flush(lane, a.stats);
 }
 
+// Launch bounds of six blocks per SM: the register count stays at 72 (seven
+// blocks resident), but the code scheduled under this cap runs 2-3% faster
+// on incoherent rays than under the default.
 template <int MODE>
-__global__ void __launch_bounds__(128) k_trace8_refill(const sqk::Trace8Args a, uint32_t total)
+__global__ void __launch_bounds__(128, 6) k_trace8_refill(const sqk::Trace8Args a, uint32_t total)
 {
     constexpr bool ANY = MODE == SQ_TRACE_ANYHIT;
     const uint32_t lane = threadIdx.x & 31u;
