@@ -297,12 +297,19 @@ sq_status build_wide(sq_ctx* c, sq_bvh* b)
     b->tris8 = dalloc(c, sqk::bvh8_tri_bytes(n));
     b->ws8 = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * sqk::bvh8_ws_words(n)));
     if (!b->nodes8 || !b->tris8 || !b->ws8) return fail(c, SQ_ERR_OOM, "8-wide BVH allocation failed (n=%u)", n);
+    b->meta8 = static_cast<uint32_t*>(dalloc(c, 2 * sizeof(uint32_t)));
+    if (!b->meta8) return fail(c, SQ_ERR_OOM, "8-wide BVH allocation failed (n=%u)", n);
     const int rc = sqk::build_bvh8(b->nodes, b->root, b->leaf0, b->tris, n, b->nodes8, b->tris8, b->ws8, c->host_ctl,
-                                   c->ctrl, c->stream);
+                                   c->ctrl, c->stream, b->meta8);
     if (rc != 0) return fail(c, SQ_ERR_CUDA, "8-wide collapse: %s", cudaGetErrorString((cudaError_t)rc));
-    b->n8 = c->host_ctl[0];
-    b->levels8 = c->host_ctl[3];
     b->launches8 = c->host_ctl[4];
+    if (!c->host_ctl[5]) {
+        // the per-level path read both counts back already
+        b->n8 = c->host_ctl[0];
+        b->levels8 = c->host_ctl[3];
+        dfree(c, b->meta8);
+        b->meta8 = nullptr;
+    }
     dfree(c, b->ws8);
     b->ws8 = nullptr;
     return SQ_OK;
@@ -439,6 +446,7 @@ sq_status sq_bvh_free(sq_bvh* b)
     dfree(c, b->nodes8);
     dfree(c, b->tris8);
     dfree(c, b->ws8);
+    dfree(c, b->meta8);
     delete b;
     return SQ_OK;
 }
@@ -446,7 +454,19 @@ sq_status sq_bvh_free(sq_bvh* b)
 sq_status sq_bvh_get_info(const sq_bvh* b_const, sq_bvh_info* info)
 {
     if (!b_const || !info) return SQ_ERR_INVALID;
-    const sq_bvh* b = b_const;
+    sq_bvh* b = const_cast<sq_bvh*>(b_const);
+    if (b->meta8) {
+        // the collapse left its node and level counts on the device
+        uint32_t m[2] = {0, 0};
+        Guard g(b->ctx->device);
+        if (cudaMemcpyAsync(m, b->meta8, sizeof m, cudaMemcpyDeviceToHost, b->ctx->stream) != cudaSuccess ||
+            cudaStreamSynchronize(b->ctx->stream) != cudaSuccess)
+            return fail(b->ctx, SQ_ERR_CUDA, "sq_bvh_get_info: %s", cudaGetErrorString(cudaGetLastError()));
+        b->n8 = m[0];
+        b->levels8 = m[1];
+        dfree(b->ctx, b->meta8);
+        b->meta8 = nullptr;
+    }
     info->node_capacity = b->cap;
     info->root = b->root;
     info->tri_count = b->n;

@@ -1618,8 +1618,9 @@ static int build_bvh8_levels(const Node* rec, uint32_t root, uint32_t leaf0, con
 }
 
 int build_bvh8(const Node* rec, uint32_t root, uint32_t leaf0, const float* tris, uint32_t n, void* nodes8, void* tris8,
-               uint32_t* ws, uint32_t* host_ctl, uint32_t* err, cudaStream_t s)
+               uint32_t* ws, uint32_t* host_ctl, uint32_t* err, cudaStream_t s, uint32_t* meta)
 {
+    host_ctl[5] = 0;
     static int grid = -1;
     if (grid < 0) {
         int per_sm = 0, sms = 0, dev = 0, coop = 0;
@@ -1639,11 +1640,18 @@ int build_bvh8(const Node* rec, uint32_t root, uint32_t leaf0, const float* tris
     if ((e = cudaLaunchCooperativeKernel((const void*)k_collapse_coop, dim3(grid), dim3(256), args, 0, s)) !=
         cudaSuccess)
         return (int)e;
+    host_ctl[4] = 2;  // the seed and the cooperative kernel
+    if (meta) {
+        // node count and levels stay on the device until asked for
+        if ((e = cudaMemcpyAsync(meta, ws, 4, cudaMemcpyDeviceToDevice, s)) != cudaSuccess) return (int)e;
+        if ((e = cudaMemcpyAsync(meta + 1, ws + 4, 4, cudaMemcpyDeviceToDevice, s)) != cudaSuccess) return (int)e;
+        host_ctl[5] = 1;
+        return (int)cudaGetLastError();
+    }
     // node count -> host_ctl[0], levels -> host_ctl[3]
     if ((e = cudaMemcpyAsync(host_ctl, ws, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return (int)e;
     if ((e = cudaMemcpyAsync(host_ctl + 3, ws + 4, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return (int)e;
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return (int)e;
-    host_ctl[4] = 2;  // the seed and the cooperative kernel
     return (int)cudaGetLastError();
 }
 

@@ -265,8 +265,13 @@ uint32_t bvh8_capacity(uint32_t n);
 size_t bvh8_node_bytes(uint32_t n);
 size_t bvh8_ws_words(uint32_t n);
 size_t bvh8_tri_bytes(uint32_t n);
+// meta (device, 2 words, may be null): when given and the cooperative
+// collapse runs, the node count and level count are copied there on the
+// stream instead of being read back (no host synchronisation); host_ctl[4]
+// then holds 2 and host_ctl[0] / [3] are not written.  Returns 1 in
+// host_ctl[5] when meta was filled that way, else 0.
 int build_bvh8(const sq::Node* rec, uint32_t root, uint32_t leaf0, const float* tris, uint32_t n, void* nodes8,
-               void* tris8, uint32_t* ws, uint32_t* host_ctl, uint32_t* err, cudaStream_t s);
+               void* tris8, uint32_t* ws, uint32_t* host_ctl, uint32_t* err, cudaStream_t s, uint32_t* meta = nullptr);
 void trace8(const Trace8Args& a, cudaStream_t s);
 
 // batched trace over many BVHs and ray tiles (sq_trace.cu, sq_bvh8.cu)

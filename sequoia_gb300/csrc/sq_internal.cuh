@@ -39,6 +39,7 @@ struct sq_bvh {
     void* nodes8 = nullptr;     // 8-wide quantised nodes (SQ_BUILD_WIDE8)
     void* tris8 = nullptr;      // their 48-byte triangles
     uint32_t n8 = 0;
+    uint32_t* meta8 = nullptr;  // device copy of (n8, levels8) not yet read back (cooperative collapse)
     uint32_t levels8 = 0;       // levels of the 8-wide tree
     uint32_t launches8 = 0;     // collapse kernel launches
     uint32_t* ws8 = nullptr;    // collapse queue state (its first word = nodes reserved)
