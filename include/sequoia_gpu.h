@@ -203,10 +203,14 @@ sq_status sq_sync(sq_ctx* ctx, uint32_t* device_error);
  * 2133).  tris: n triangles, host or device.  A device tris pointer is
  * referenced, not copied, exactly as Hierarchy::tri_base references the
  * caller's vector (src/builder.cpp:1613): it must outlive the BVH.  The BVH
- * lives on the device until sq_bvh_free.                                      */
+ * lives on the device until sq_bvh_free.  Morton builds return without
+ * waiting for the device; the next call on the context (a trace) is ordered
+ * after the build on the context's stream.                                   */
 sq_status sq_build(sq_ctx* ctx, const sq_triangle* tris, uint32_t n,
                    const sq_build_params* params, sq_bvh** out);
 sq_status sq_bvh_free(sq_bvh* bvh);
+/* Sizes of a built BVH.  The first call after an 8-wide build waits for the
+ * build to finish (its node count is read back then).                        */
 sq_status sq_bvh_get_info(const sq_bvh* bvh, sq_bvh_info* info);
 
 /* Copy the node array out in Sequoia's Node1 layout so that the reference's
@@ -272,7 +276,12 @@ sq_status sq_radix_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* v
  * src/tracer.cpp:47-65, 195-230).  hits: one sq_hit per ray (may be NULL);
  * heatmap_rgb: width*height*3 bytes, byte = (uint8)(min(1, tests/200)*255)
  * in all three channels as in src/tracer.cpp:222-225 (may be NULL; for
- * explicit rays it holds ray_count*3 bytes).  Outputs host or device.        */
+ * explicit rays it holds ray_count*3 bytes).  Outputs host or device:
+ * device outputs are written on the context's stream and the call returns
+ * without waiting; host outputs are complete when the call returns.
+ * Page-locked host outputs (cudaHostAlloc / cudaHostRegister) are written by
+ * the kernel in place, so their transfer overlaps the trace; pageable host
+ * outputs go through a device buffer and one copy.                           */
 sq_status sq_trace(sq_ctx* ctx, const sq_bvh* bvh, const sq_ray_source* rays,
                    uint32_t mode, sq_hit* hits, uint8_t* heatmap_rgb);
 
