@@ -456,7 +456,7 @@ void morton_codes(const float* tris, uint32_t n, uint32_t mode, const uint32_t* 
     if (n == 0) return;
     const bool aligned = (reinterpret_cast<uintptr_t>(tris) & 15u) == 0;
     const uint32_t tiles = (n + kTileTris - 1) / kTileTris;
-    const uint32_t grid = min(tiles, (uint32_t)sms() * 4u);
+    const uint32_t grid = min(tiles, (uint32_t)sms() * 8u);
     if (digit_bits == 8 && passes == 4) k_morton<8, 4><<<grid, 256, 0, s>>>(tris, n, mode, box_ord, keys, vals, hist, aligned);
     else if (digit_bits == 10 && passes == 3) k_morton<10, 3><<<grid, 256, 0, s>>>(tris, n, mode, box_ord, keys, vals, hist, aligned);
     else if (digit_bits == 6 && passes == 5) k_morton<6, 5><<<grid, 256, 0, s>>>(tris, n, mode, box_ord, keys, vals, hist, aligned);
@@ -468,7 +468,7 @@ void morton_codes64(const float* tris, uint32_t n, const uint32_t* box_ord, uint
     if (n == 0) return;
     const bool aligned = (reinterpret_cast<uintptr_t>(tris) & 15u) == 0;
     const uint32_t tiles = (n + kTileTris - 1) / kTileTris;
-    const uint32_t grid = min(tiles, (uint32_t)sms() * 4u);
+    const uint32_t grid = min(tiles, (uint32_t)sms() * 8u);
     k_morton64<<<grid, 256, 0, s>>>(tris, n, box_ord, lo, hi, vals, hist, aligned);
 }
 
