@@ -51,7 +51,7 @@ METRIC = "Mrays/s traced & Mtris/s built on 1 GB300: quantized+batched vs plain 
 WORKLOAD = dict(name="soup_2m", tris=2_000_000, clusters=64, seed=2, width=3840, height=2160,
                 eye=(0.0, 0.0, -40.0), target=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0), vfov=60.0)
 STRESS = dict(tris=8_000_000, clusters=256, seed=5, rays=1 << 24, batches=64)
-LBVH_KERNELS = 7  # scene bounds, Morton codes, 4 onesweep passes, climb
+LBVH_KERNELS = 8  # scene bounds, Morton codes, 4 onesweep passes, climb (local + global phase)
 # DRAM bytes (read + write) of one k_trace8_tiles<closest> launch on this
 # workload, from the ncu capture summarised in profiles/k_trace8_tiles_soup2m.md
 TRACE8_DRAM_BYTES = 115.8e6 + 106.1e6

@@ -182,7 +182,9 @@ sq_status build_morton(sq_ctx* c, sq_bvh* b, const sq_build_params& p)
     SQ_CUDA(c, cudaEventRecord(c->ev[1], s));
     sqk::sort_passes(ka, va, kb, vb, n, zero + z_hist, zero + z_lb, zero + z_ctr, db, passes, err, s);
     SQ_CUDA(c, cudaEventRecord(c->ev[2], s));
-    sqk::lbvh_climb(b->codes, b->perm, b->tris, n, b->nodes, zero + z_flags, info, err, s);
+    // the sort's second buffer is free now: it lists the climb's open nodes;
+    // box_ord leaves words 6 and 7 of the zeroed region for their count
+    sqk::lbvh_climb(b->codes, b->perm, b->tris, n, b->nodes, zero + z_flags, info, alt, zero + z_box + 6, err, s);
     SQ_CUDA(c, cudaEventRecord(c->ev[3], s));
     SQ_CUDA(c, cudaGetLastError());
     c->build_timed = true;
@@ -235,7 +237,7 @@ sq_status build_morton64(sq_ctx* c, sq_bvh* b, const sq_build_params& p)
                      db, passes, err, s);
     sqk::combine64(hi1, pos, lo, vals, n, b->codes64, b->perm, s);
     SQ_CUDA(c, cudaEventRecord(c->ev[2], s));
-    sqk::lbvh_climb64(b->codes64, b->perm, b->tris, n, b->nodes, zero + z_flags, info, err, s);
+    sqk::lbvh_climb64(b->codes64, b->perm, b->tris, n, b->nodes, zero + z_flags, info, alt, zero + z_box + 6, err, s);
     SQ_CUDA(c, cudaEventRecord(c->ev[3], s));
     SQ_CUDA(c, cudaGetLastError());
     c->build_timed = true;

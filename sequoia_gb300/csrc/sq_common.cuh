@@ -190,8 +190,10 @@ void scene_bounds(const float* tris, uint32_t n, uint32_t mode, uint32_t* box_or
 void morton_codes(const float* tris, uint32_t n, uint32_t mode, const uint32_t* box_ord, uint32_t* keys,
                   uint32_t* vals, uint32_t* hist, uint32_t digit_bits, uint32_t passes, cudaStream_t s);
 // flags: n zeroed words; info: 6n float4 (a 48-byte record per boundary side)
+// surv: n words of scratch for the nodes left to the global phase;
+// surv_count: one zeroed word.
 void lbvh_climb(const uint32_t* codes, const uint32_t* perm, const float* tris, uint32_t n, sq::Node* nodes,
-                uint32_t* flags, float4* info, uint32_t* err, cudaStream_t s);
+                uint32_t* flags, float4* info, uint32_t* surv, uint32_t* surv_count, uint32_t* err, cudaStream_t s);
 // 60-bit codes (build_hierarchy_morton2): codes as low / high words with the
 // histograms of 8 digit passes (4 per word); the high words re-ordered by
 // the first sort stage; the combined sorted codes and permutation; the
@@ -202,7 +204,8 @@ void gather_high(const uint32_t* hi, const uint32_t* perm1, uint32_t n, uint32_t
 void combine64(const uint32_t* hi_sorted, const uint32_t* perm2, const uint32_t* lo_sorted, const uint32_t* perm1,
                uint32_t n, uint64_t* codes64, uint32_t* perm, cudaStream_t s);
 void lbvh_climb64(const uint64_t* codes, const uint32_t* perm, const float* tris, uint32_t n, sq::Node* nodes,
-                  uint32_t* flags, float4* info, uint32_t* err, cudaStream_t s);
+                  uint32_t* flags, float4* info, uint32_t* surv, uint32_t* surv_count, uint32_t* err,
+                  cudaStream_t s);
 
 // onesweep radix sort (sq_sort.cu)
 size_t sort_lookback_words(uint32_t n, uint32_t digit_bits, uint32_t passes);

@@ -258,10 +258,28 @@ __global__ void k_combine64(const uint32_t* __restrict__ hi_sorted, const uint32
 
 // 256 threads and at most 40 registers: six blocks per SM, so more blocks
 // overlap their leaf gathers and global-phase round trips.
+// Sibling record of a node beside its parent boundary p: box, far end,
+// split and the code XOR at the far end (left child: slot 2p, right: 2p + 1).
+__device__ __forceinline__ void publish_record(float4* __restrict__ info, uint32_t p, bool left, const Box& box,
+                                               uint32_t far_end, uint32_t split, uint64_t dfar)
+{
+    float4* mine = info + 3ull * (2ull * p + (left ? 0u : 1u));
+    mine[0] = make_float4(box.mn[0], box.mn[1], box.mn[2], __uint_as_float(far_end));
+    mine[1] = make_float4(box.mx[0], box.mx[1], box.mx[2], __uint_as_float(split));
+    mine[2] = make_float4(__uint_as_float((uint32_t)dfar), __uint_as_float((uint32_t)(dfar >> 32)), 0.0f, 0.0f);
+}
+
+// Leaf and warp phases of the climb.  Nodes still open after the warp phase
+// (their sibling finishes in another warp) publish their record and are
+// listed as (parent boundary | left << 31) in surv for k_lbvh_global; a
+// block takes its slots with one atomic on surv_count.  Splitting the climb
+// this way lets these blocks retire at once: waiting out a global climb held
+// their SM slots from the blocks still to run.
 template <class Code>
 __global__ void __launch_bounds__(256, 6) k_lbvh_climb(const Code* __restrict__ codes, const uint32_t* __restrict__ perm,
                                                     const float* __restrict__ tris, uint32_t n, Node* __restrict__ nodes,
-                                                    uint32_t* __restrict__ flags, float4* __restrict__ info, uint32_t* err)
+                                                    float4* __restrict__ info, uint32_t* __restrict__ surv,
+                                                    uint32_t* __restrict__ surv_count, uint32_t* err)
 {
     constexpr uint32_t FULL = 0xFFFFFFFFu;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -392,36 +410,91 @@ __global__ void __launch_bounds__(256, 6) k_lbvh_climb(const Code* __restrict__ 
         if (!__any_sync(FULL, merged)) break;
     }
 
-    if (!active) return;
-
-    // Global protocol: publish this node's range end, box and split beside
-    // its parent boundary, count the arrival; the second arrival continues
-    // with the union of both children.
-    for (;;) {
-        if (l == 0 && r == n) {
-            write_root();
-            return;
-        }
-        uint32_t p;
-        bool left;
+    uint32_t p = 0;
+    bool left = false;
+    if (active) {
         parent_of(p, left);
-        // record: box, far end, split and the code XOR at the far end
-        float4* mine = info + 3ull * (2ull * p + (left ? 0u : 1u));
-        mine[0] = make_float4(box.mn[0], box.mn[1], box.mn[2], __uint_as_float(left ? l : r));
-        mine[1] = make_float4(box.mx[0], box.mx[1], box.mx[2], __uint_as_float(split));
-        const uint64_t dfar = (uint64_t)(left ? dl : dr);
-        mine[2] = make_float4(__uint_as_float((uint32_t)dfar), __uint_as_float((uint32_t)(dfar >> 32)), 0.0f, 0.0f);
-        // release my record, acquire the sibling's (the first arrival stops)
-        const uint32_t old = atomic_add_acq_rel_u32(flags + p, 1u);
-        if (old == 0) return;
-        if (old != 1) { raise_error(err, SQ_DEVERR_TOPOLOGY); return; }
-        const float4* sib = info + 3ull * (2ull * p + (left ? 1u : 0u));
-        const float4 s0 = __ldcg(sib), s1 = __ldcg(sib + 1), s2 = __ldcg(sib + 2);
-        Box sb;
-        sb.mn[0] = s0.x; sb.mn[1] = s0.y; sb.mn[2] = s0.z;
-        sb.mx[0] = s1.x; sb.mx[1] = s1.y; sb.mx[2] = s1.z;
-        const uint64_t s_d = (uint64_t)__float_as_uint(s2.x) | ((uint64_t)__float_as_uint(s2.y) << 32);
-        merge(p, left, __float_as_uint(s0.w), sb, __float_as_uint(s1.w), (Code)s_d);
+        publish_record(info, p, left, box, left ? l : r, split, (uint64_t)(left ? dl : dr));
+    }
+    __shared__ uint32_t s_count, s_base;
+    if (threadIdx.x == 0) s_count = 0;
+    __syncthreads();
+    const uint32_t am = __ballot_sync(FULL, active);
+    uint32_t woff = 0;
+    if (lane == 0 && am) woff = atomicAdd(&s_count, (uint32_t)__popc(am));
+    woff = __shfl_sync(FULL, woff, 0);
+    __syncthreads();
+    if (threadIdx.x == 0) s_base = s_count ? atomicAdd(surv_count, s_count) : 0u;
+    __syncthreads();
+    if (active) surv[s_base + woff + __popc(am & ((1u << lane) - 1u))] = p | (left ? 0x80000000u : 0u);
+}
+
+// Global phase of the climb (Apetrei's protocol): each listed node counts its
+// arrival at its parent boundary (release its record, acquire the sibling's);
+// the second arrival merges the two and continues with the parent, whose
+// record it publishes first.  Nothing waits: a first arrival stops.
+template <class Code>
+__global__ void __launch_bounds__(256) k_lbvh_global(const uint32_t* __restrict__ surv,
+                                                     const uint32_t* __restrict__ surv_count, uint32_t n,
+                                                     Node* __restrict__ nodes, uint32_t* __restrict__ flags,
+                                                     float4* __restrict__ info, uint32_t* err)
+{
+    const uint32_t leaf0 = 2u * n + 2u;
+    const uint32_t count = *surv_count;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
+        const uint32_t e = surv[t];
+        uint32_t p = e & 0x7FFFFFFFu;
+        bool left = (e >> 31) != 0u;
+        // this node from its own record; the XOR at its near end (boundary p)
+        // is not needed: the merge replaces it with the sibling's far XOR
+        const float4* mine = info + 3ull * (2ull * p + (left ? 0u : 1u));
+        const float4 m0 = __ldcg(mine), m1 = __ldcg(mine + 1), m2 = __ldcg(mine + 2);
+        Box box;
+        box.mn[0] = m0.x; box.mn[1] = m0.y; box.mn[2] = m0.z;
+        box.mx[0] = m1.x; box.mx[1] = m1.y; box.mx[2] = m1.z;
+        uint32_t split = __float_as_uint(m1.w);
+        const Code dfar = (Code)((uint64_t)__float_as_uint(m2.x) | ((uint64_t)__float_as_uint(m2.y) << 32));
+        uint32_t l, r;
+        Code dl = 0, dr = 0;
+        if (left) { l = __float_as_uint(m0.w); r = p; dl = dfar; }
+        else { l = p; r = __float_as_uint(m0.w); dr = dfar; }
+        for (bool first = true;; first = false) {
+            if (!first) {
+                if (l == 0 && r == n) {
+                    if (n >= 8) store_node(nodes, box, 2u * split, 2u, 0);
+                    else store_node(nodes, box, leaf0, n, 0);
+                    break;
+                }
+                if (l == 0) { p = r; left = true; }
+                else if (r == n) { p = l; left = false; }
+                else if (dr < dl) { p = r; left = true; }
+                else { p = l; left = false; }
+                publish_record(info, p, left, box, left ? l : r, split, (uint64_t)(left ? dl : dr));
+            }
+            const uint32_t old = atomic_add_acq_rel_u32(flags + p, 1u);
+            if (old == 0) break;
+            if (old != 1) { raise_error(err, SQ_DEVERR_TOPOLOGY); break; }
+            const float4* sib = info + 3ull * (2ull * p + (left ? 1u : 0u));
+            const float4 s0 = __ldcg(sib), s1 = __ldcg(sib + 1), s2 = __ldcg(sib + 2);
+            Box sb;
+            sb.mn[0] = s0.x; sb.mn[1] = s0.y; sb.mn[2] = s0.z;
+            sb.mx[0] = s1.x; sb.mx[1] = s1.y; sb.mx[2] = s1.z;
+            const Code s_d = (Code)((uint64_t)__float_as_uint(s2.x) | ((uint64_t)__float_as_uint(s2.y) << 32));
+            const uint32_t s_end = __float_as_uint(s0.w), s_split = __float_as_uint(s1.w);
+            uint32_t ll, rr, lsplit, rsplit;
+            Box lb, rb;
+            if (left) { ll = l; rr = s_end; lb = box; rb = sb; lsplit = split; rsplit = s_split; dr = s_d; }
+            else { ll = s_end; rr = r; lb = sb; rb = box; lsplit = s_split; rsplit = split; dl = s_d; }
+            if (rr - ll >= 8) {
+                write_child(nodes, 2u * p, ll, p, lb, lsplit, leaf0);
+                write_child(nodes, 2u * p + 1u, p, rr, rb, rsplit, leaf0);
+            }
+            box = lb;
+            box_grow(box, rb);
+            l = ll;
+            r = rr;
+            split = p;
+        }
     }
 }
 
@@ -486,18 +559,31 @@ void combine64(const uint32_t* hi_sorted, const uint32_t* perm2, const uint32_t*
                                                                             codes64, perm);
 }
 
-void lbvh_climb(const uint32_t* codes, const uint32_t* perm, const float* tris, uint32_t n, sq::Node* nodes,
-                uint32_t* flags, float4* info, uint32_t* err, cudaStream_t s)
+template <class Code>
+void climb_launch(const Code* codes, const uint32_t* perm, const float* tris, uint32_t n, sq::Node* nodes,
+                  uint32_t* flags, float4* info, uint32_t* surv, uint32_t* surv_count, uint32_t* err, cudaStream_t s)
 {
     if (n == 0) return;
-    k_lbvh_climb<uint32_t><<<(n + 255) / 256, 256, 0, s>>>(codes, perm, tris, n, nodes, flags, info, err);
+    k_lbvh_climb<Code><<<(n + 255) / 256, 256, 0, s>>>(codes, perm, tris, n, nodes, info, surv, surv_count, err);
+    static int per_sm = 0;
+    if (!per_sm) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lbvh_global<Code>, 256, 0);
+        if (per_sm <= 0) per_sm = 1;
+    }
+    const uint32_t grid = min((n + 255) / 256, (uint32_t)(per_sm * sms()));
+    k_lbvh_global<Code><<<grid, 256, 0, s>>>(surv, surv_count, n, nodes, flags, info, err);
+}
+
+void lbvh_climb(const uint32_t* codes, const uint32_t* perm, const float* tris, uint32_t n, sq::Node* nodes,
+                uint32_t* flags, float4* info, uint32_t* surv, uint32_t* surv_count, uint32_t* err, cudaStream_t s)
+{
+    climb_launch<uint32_t>(codes, perm, tris, n, nodes, flags, info, surv, surv_count, err, s);
 }
 
 void lbvh_climb64(const uint64_t* codes, const uint32_t* perm, const float* tris, uint32_t n, sq::Node* nodes,
-                  uint32_t* flags, float4* info, uint32_t* err, cudaStream_t s)
+                  uint32_t* flags, float4* info, uint32_t* surv, uint32_t* surv_count, uint32_t* err, cudaStream_t s)
 {
-    if (n == 0) return;
-    k_lbvh_climb<uint64_t><<<(n + 255) / 256, 256, 0, s>>>(codes, perm, tris, n, nodes, flags, info, err);
+    climb_launch<uint64_t>(codes, perm, tris, n, nodes, flags, info, surv, surv_count, err, s);
 }
 
 }  // namespace sqk
