@@ -565,13 +565,10 @@ void climb_launch(const Code* codes, const uint32_t* perm, const float* tris, ui
 {
     if (n == 0) return;
     k_lbvh_climb<Code><<<(n + 255) / 256, 256, 0, s>>>(codes, perm, tris, n, nodes, info, surv, surv_count, err);
-    static int per_sm = 0;
-    if (!per_sm) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lbvh_global<Code>, 256, 0);
-        if (per_sm <= 0) per_sm = 1;
-    }
-    const uint32_t grid = min((n + 255) / 256, (uint32_t)(per_sm * sms()));
-    k_lbvh_global<Code><<<grid, 256, 0, s>>>(surv, surv_count, n, nodes, flags, info, err);
+    // one thread per possible open node (their count is on the device): the
+    // climbs are chains of round trips, so running them all at once beats a
+    // grid-stride loop over fewer threads
+    k_lbvh_global<Code><<<(n + 255) / 256, 256, 0, s>>>(surv, surv_count, n, nodes, flags, info, err);
 }
 
 void lbvh_climb(const uint32_t* codes, const uint32_t* perm, const float* tris, uint32_t n, sq::Node* nodes,
