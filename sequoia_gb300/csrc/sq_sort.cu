@@ -8,8 +8,10 @@
 // Morton kernel for builds); then one kernel per digit:
 //   - a block takes the next tile from an atomic counter, so tiles are
 //     processed in order and a tile's predecessors are always running;
-//   - warps rank their keys with __match_any_sync (stable: items are ranked
-//     in index order within the warp, warps in index order within the tile);
+//   - warps rank their keys by digit (stable: items are ranked in index
+//     order within the warp, warps in index order within the tile); the lanes
+//     sharing a digit come from one ballot per digit bit, which costs the
+//     same for any number of distinct digits (a match does not);
 //   - the tile publishes its per-digit counts and walks back over earlier
 //     tiles' published counts (decoupled look-back) for its global offsets;
 //     every wait is bounded and raises SQ_DEVERR_LOOKBACK_TIMEOUT instead of
@@ -124,7 +126,16 @@ __global__ void __launch_bounds__(kBlock, 4) k_onesweep(const uint32_t* __restri
         const uint32_t idx = wbase + it * 32 + lane;
         const bool valid = idx < n;
         const uint32_t d = valid ? ((k[it] >> shift) & MASK) : (uint32_t)RADIX;
-        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+        // lanes with the same digit, from one ballot per digit bit (constant
+        // cost; a match over up to 32 distinct digits costs more)
+        uint32_t peers = __ballot_sync(0xFFFFFFFFu, valid);
+        if (!valid) peers = ~peers;
+#pragma unroll
+        for (int b = 0; b < DB; ++b) {
+            const bool bit = (d >> b) & 1u;
+            const uint32_t bal = __ballot_sync(0xFFFFFFFFu, bit);
+            peers &= bit ? bal : ~bal;
+        }
         const int leader = __ffs(peers) - 1;
         uint32_t old = 0;
         // a shared-memory atomic (not a load and a store) so that the
