@@ -54,7 +54,7 @@ STRESS = dict(tris=8_000_000, clusters=256, seed=5, rays=1 << 24, batches=64)
 LBVH_KERNELS = 8  # scene bounds, Morton codes, 4 onesweep passes, climb (local + global phase)
 # DRAM bytes (read + write) of one k_trace8_tiles<closest> launch on this
 # workload, from the ncu capture summarised in profiles/k_trace8_tiles_soup2m.md
-TRACE8_DRAM_BYTES = 114.8e6 + 106.3e6
+TRACE8_DRAM_BYTES = 115.0e6 + 106.3e6
 TRACE8_DRAM_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch (profiles/k_trace8_tiles_soup2m.md)"
 
 
