@@ -107,14 +107,15 @@ __device__ __forceinline__ uint8_t quant_hi(float v, float origin, int e)
 // the first child of largest surface area that still fits, until none does.
 // All 32 lanes must call this; a group whose `active` is false only takes
 // part in the warp-wide shuffles.  Inner children become nodes
-// [child_base, child_base + n) and leaf triangles slots [tri_base, ...).
+// [child_base, child_base + n) and leaf triangles take the triangle slots
+// [tri_base, ...).
 // The warp's four groups allocate together: lane 0 calls
 // alloc(nodes, tris, node_base, tri_base, task_base) once with the warp's
 // totals (one atomic per warp instead of one per node and one per child:
 // same-address atomics serialise in L2), and each group takes its share in
 // group order.  publish(task, node, record) is called by the child's lane
 // with task = task_base + the child's rank in the warp.  sm: this warp's
-// staging area (kGroupSmem per warp).
+// staging area (one GroupSmem per warp).
 struct GroupSmem {
     Node8 node[4];
     uint32_t off[4][8], cnt[4][8], child[4][8];

@@ -6,7 +6,10 @@
 //   k_morton        30-bit codes (src/builder.cpp:2217-2236) + the digit
 //                   histograms of every radix-sort pass, in one read
 //   onesweep sort   (sq_sort.cu)
-//   k_lbvh_climb    topology, bounds and node records in one bottom-up pass
+//   k_lbvh_climb    topology, bounds and node records bottom-up: leaf and
+//                   warp phases; lists the nodes whose sibling finishes in
+//                   another warp
+//   k_lbvh_global   the rest of the climb, one thread per listed node
 //
 // The climb builds the same logical tree as recurse_morton /
 // find_split_morton (src/builder.cpp:2281-2409): ranges of fewer than 8
