@@ -382,8 +382,8 @@ __global__ void __launch_bounds__(256, 6) k_lbvh_climb(const Code* __restrict__ 
     // Warp phase: nodes whose two children both finish inside this warp are
     // merged through shuffles (the lanes of the two children find each other
     // by their common parent), in rounds, until a round merges nothing; only
-    // the nodes left then take the global protocol below.  Most small
-    // subtrees never touch the sibling records or the flags.
+    // the nodes left then go to the global protocol (k_lbvh_global).  Most
+    // small subtrees never touch the sibling records or the flags.
     for (;;) {
         if (active && l == 0 && r == n) { write_root(); active = false; }
         const uint32_t A = __ballot_sync(FULL, active);
