@@ -123,7 +123,9 @@ typedef enum sq_builder_kind {
 #define SQ_BUILD_WIDE8 0x2u             /* also collapse the binary tree into an
                                            8-wide BVH with 8-bit quantised child
                                            boxes (rounded outward); closest and
-                                           any-hit traces then use it          */
+                                           any-hit traces then use it.  At most
+                                           2^27 triangles (SQ_ERR_UNSUPPORTED
+                                           above that)                         */
 
 typedef struct sq_build_params {
     uint32_t kind;            /* sq_builder_kind                                  */

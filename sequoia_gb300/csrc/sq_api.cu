@@ -394,6 +394,9 @@ sq_status sq_build(sq_ctx* c, const sq_triangle* tris, uint32_t n, const sq_buil
 {
     if (!c || !out || !params || (n > 0 && !tris)) return fail(c, SQ_ERR_INVALID, "sq_build: null argument");
     if (n > (1u << 29)) return fail(c, SQ_ERR_INVALID, "sq_build: n=%u exceeds 2^29", n);
+    // the 8-wide traversal's leaf entries hold a 27-bit first-triangle index
+    if ((params->flags & SQ_BUILD_WIDE8) && n > sqk::kWide8MaxTris)
+        return fail(c, SQ_ERR_UNSUPPORTED, "sq_build: the 8-wide BVH takes at most 2^27 triangles (n=%u)", n);
     *out = nullptr;
     Guard g(c->device);
     sq_build_params p = *params;

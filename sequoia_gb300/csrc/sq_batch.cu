@@ -359,6 +359,8 @@ sq_status prepare(sq_batch* b)
 {
     sq_ctx* c = b->ctx;
     const bool wide = b->params.wide != 0 && b->params.mode != SQ_TRACE_REF;
+    if (wide && b->tris > sqk::kWide8MaxTris)
+        return fail(c, SQ_ERR_UNSUPPORTED, "batch: the 8-wide BVH takes at most 2^27 triangles (%u)", b->tris);
     for (uint32_t m = 0; m < b->meshes; ++m) b->jobs[m].root = wide ? m : 3u * b->tris + 2u + m;
     SQ_CUDA(c, cudaMemcpyAsync(b->d_jobs, b->jobs.data(), sizeof(sqk::BatchJob) * b->meshes, cudaMemcpyHostToDevice,
                                c->stream));
@@ -621,6 +623,7 @@ sq_status sq_batch_autotune(sq_batch* b, const char* cache_path, sq_batch_params
     for (uint32_t d : digits)
         for (uint32_t w : widths)
             for (uint32_t bl : blocks) {
+                if (w && b->tris > sqk::kWide8MaxTris) continue;  // beyond the 8-wide form's reach
                 b->params = base;
                 b->params.sort_digit_bits = d;
                 b->params.wide = w;

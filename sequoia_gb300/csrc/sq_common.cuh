@@ -264,6 +264,9 @@ struct Trace8Args {
     unsigned long long* stats;
     uint32_t refill;       // 1: per-lane ray refill; 0: whole 32-ray batches per warp
 };
+// Triangles an 8-wide BVH can address: a traversal stack entry holds the
+// first triangle of a leaf range in 27 bits (and its count in 4).
+constexpr uint32_t kWide8MaxTris = 1u << 27;
 uint32_t bvh8_capacity(uint32_t n);
 size_t bvh8_node_bytes(uint32_t n);
 size_t bvh8_ws_words(uint32_t n);
