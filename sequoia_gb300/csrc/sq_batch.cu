@@ -255,17 +255,7 @@ __global__ void k_empty_roots(const uint32_t* __restrict__ off, uint32_t M, Node
     }
 }
 
-int g_sms = 0;
-int sms()
-{
-    if (!g_sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (g_sms <= 0) g_sms = kNumSMs;
-    }
-    return g_sms;
-}
+int sms() { return sm_count(); }
 
 uint32_t mesh_passes(uint32_t M) { return M <= 256 ? 1u : (M <= 65536 ? 2u : 3u); }
 

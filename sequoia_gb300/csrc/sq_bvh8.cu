@@ -1301,18 +1301,9 @@ void launch8(const sqk::Trace8Args& a, cudaStream_t s)
     if (a.ray_kind == SQ_RAYS_EXPLICIT) batches = (a.ray_count + 31u) / 32u;
     else batches = ((a.width + 7u) / 8u) * ((a.height + 3u) / 4u);
     if (batches == 0) return;
-    static int per_sm[2] = {0, 0}, sms = 0;
+    static const int per_sm[2] = {blocks_per_sm(k_trace8_tiles<MODE>, 128), blocks_per_sm(k_trace8_refill<MODE>, 128)};
     const int v = a.refill ? 1 : 0;
-    if (!per_sm[v]) {
-        if (v) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[v], k_trace8_refill<MODE>, 128, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[v], k_trace8_tiles<MODE>, 128, 0);
-        if (per_sm[v] <= 0) per_sm[v] = 1;
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = kNumSMs;
-    }
-    uint32_t grid = (uint32_t)(per_sm[v] * sms);
+    uint32_t grid = (uint32_t)(per_sm[v] * sm_count());
     const uint32_t need = (batches + 3u) / 4u;
     if (grid > need) grid = need;
     if (v) k_trace8_refill<MODE><<<grid, 128, 0, s>>>(a, a.ray_kind == SQ_RAYS_EXPLICIT ? a.ray_count : batches * 32u);
@@ -1506,19 +1497,14 @@ template <int MODE>
 void launch8_batch(const sqk::BatchTraceArgs& a, int block, cudaStream_t s)
 {
     if (a.total_batches == 0) return;
-    static int per_sm[2][3] = {{0, 0, 0}, {0, 0, 0}}, sms = 0;
+    static const int per_sm[2][3] = {
+        {blocks_per_sm(k_trace8_batch_tiles<MODE>, 64), blocks_per_sm(k_trace8_batch_tiles<MODE>, 128),
+         blocks_per_sm(k_trace8_batch_tiles<MODE>, 256)},
+        {blocks_per_sm(k_trace8_batch_refill<MODE>, 64), blocks_per_sm(k_trace8_batch_refill<MODE>, 128),
+         blocks_per_sm(k_trace8_batch_refill<MODE>, 256)}};
     const int bi = block <= 64 ? 0 : (block <= 128 ? 1 : 2);
     const int v = a.refill ? 1 : 0;
-    if (!per_sm[v][bi]) {
-        if (v) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[v][bi], k_trace8_batch_refill<MODE>, block, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[v][bi], k_trace8_batch_tiles<MODE>, block, 0);
-        if (per_sm[v][bi] <= 0) per_sm[v][bi] = 1;
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = kNumSMs;
-    }
-    uint32_t grid = (uint32_t)(per_sm[v][bi] * sms);
+    uint32_t grid = (uint32_t)(per_sm[v][bi] * sm_count());
     const uint32_t need = (a.total_batches + (uint32_t)(block / 32) - 1) / (uint32_t)(block / 32);
     if (grid > need) grid = need;
     if (v) k_trace8_batch_refill<MODE><<<grid, block, 0, s>>>(a);
@@ -1551,14 +1537,7 @@ int build_bvh8_queue(const Node* rec, const uint32_t* roots_dev, uint32_t nroots
     cudaError_t e;
     if ((e = cudaMemsetAsync(ws, 0, sizeof(uint32_t) * (16 + kFixedLevels), s)) != cudaSuccess) return (int)e;
     k_fixed_seed<<<(nroots + 255) / 256, 256, 0, s>>>(roots_dev, nroots, ta, na, counts, node_counter);
-    static int grid = 0;
-    if (!grid) {
-        int per_sm = 0, sms = 0, dev = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collapse_fixed, 128, 0);
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        grid = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : kNumSMs);
-    }
+    static const int grid = blocks_per_sm(k_collapse_fixed, 128) * sm_count();
     for (uint32_t level = 0; level < kFixedLevels; ++level) {
         uint32_t* in_t = (level & 1) ? tb : ta;
         uint32_t* in_n = (level & 1) ? nb : na;
@@ -1622,15 +1601,15 @@ int build_bvh8(const Node* rec, uint32_t root, uint32_t leaf0, const float* tris
                uint32_t* ws, uint32_t* host_ctl, uint32_t* err, cudaStream_t s, uint32_t* meta)
 {
     host_ctl[5] = 0;
-    static int grid = -1;
-    if (grid < 0) {
-        int per_sm = 0, sms = 0, dev = 0, coop = 0;
+    // every block of the cooperative collapse must be resident: the grid is
+    // the occupancy limit (0: no cooperative launch, use the per-level path)
+    static const int grid = [] {
+        int dev = 0, coop = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collapse_coop, 256, 0);
-        grid = (coop && per_sm > 0 && sms > 0) ? per_sm * sms : 0;
-    }
+        return (coop && per_sm > 0) ? per_sm * sm_count() : 0;
+    }();
     if (grid == 0) return build_bvh8_levels(rec, root, leaf0, tris, n, nodes8, tris8, ws, host_ctl, err, s);
     const uint32_t capacity = bvh8_capacity(n);
     cudaError_t e;

@@ -251,17 +251,7 @@ __global__ void __launch_bounds__(128) k_trace_bundle(const sqk::TraceArgs a)
     }
 }
 
-int g_sms = 0;
-int sms()
-{
-    if (!g_sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (g_sms <= 0) g_sms = kNumSMs;
-    }
-    return g_sms;
-}
+int sms() { return sm_count(); }
 
 }  // namespace
 

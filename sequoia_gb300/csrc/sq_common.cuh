@@ -146,6 +146,28 @@ __device__ __forceinline__ void raise_error(uint32_t* err, uint32_t bit)
 
 constexpr int kNumSMs = 152;
 
+// Multiprocessor count of the current device, queried once per process
+// (a function-local static: initialised once even under concurrent calls).
+inline int sm_count()
+{
+    static const int v = [] {
+        int dev = 0, n = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        return n > 0 ? n : kNumSMs;
+    }();
+    return v;
+}
+
+// Resident blocks per SM of a kernel at a block size (at least 1).
+template <class Kernel>
+inline int blocks_per_sm(Kernel kernel, int threads)
+{
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, 0);
+    return n > 0 ? n : 1;
+}
+
 // Trace statistics of one warp (box tests, triangle tests, requested bytes,
 // node visits), summed over the warp's tiles in shared memory by lane 0 and
 // added to the four global counters once, when the warp finishes: one atomic

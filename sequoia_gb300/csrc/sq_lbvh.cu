@@ -501,17 +501,7 @@ __global__ void __launch_bounds__(256) k_lbvh_global(const uint32_t* __restrict_
     }
 }
 
-int g_sms = 0;
-int sms()
-{
-    if (!g_sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (g_sms <= 0) g_sms = kNumSMs;
-    }
-    return g_sms;
-}
+int sms() { return sm_count(); }
 
 }  // namespace
 

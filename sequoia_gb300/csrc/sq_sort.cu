@@ -244,27 +244,17 @@ template <int DB>
 void launch_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, uint32_t n, uint32_t shift,
                  const uint32_t* hist, uint32_t* lookback, uint32_t* counter, uint32_t* err, cudaStream_t s)
 {
-    static bool configured = false;
     const size_t bytes = Smem<DB>::bytes;
-    if (!configured) {
-        cudaFuncSetAttribute(k_onesweep<DB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-        configured = true;
-    }
+    static const bool configured = [] {
+        cudaFuncSetAttribute(k_onesweep<DB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Smem<DB>::bytes);
+        return true;
+    }();
+    (void)configured;
     const uint32_t tiles = (n + kTile - 1) / kTile;
     k_onesweep<DB><<<tiles, kBlock, bytes, s>>>(kin, vin, kout, vout, n, shift, hist, lookback, counter, err);
 }
 
-int g_sms = 0;
-int sms()
-{
-    if (!g_sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (g_sms <= 0) g_sms = kNumSMs;
-    }
-    return g_sms;
-}
+int sms() { return sm_count(); }
 
 }  // namespace
 

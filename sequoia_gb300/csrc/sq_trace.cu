@@ -427,16 +427,8 @@ void launch(const sqk::TraceArgs& a, cudaStream_t s)
     if (a.ray_kind == SQ_RAYS_EXPLICIT) batches = (a.ray_count + 31u) / 32u;
     else batches = ((a.width + 7u) / 8u) * ((a.height + 3u) / 4u);
     if (batches == 0) return;
-    static int per_sm = 0, sms = 0;
-    if (!per_sm) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<MODE>, 128, 0);
-        if (per_sm <= 0) per_sm = 1;
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = kNumSMs;
-    }
-    uint32_t grid = (uint32_t)(per_sm * sms);
+    static const int per_sm = blocks_per_sm(k_trace<MODE>, 128);
+    uint32_t grid = (uint32_t)(per_sm * sm_count());
     const uint32_t need = (batches + 3u) / 4u;
     if (grid > need) grid = need;
     k_trace<MODE><<<grid, 128, 0, s>>>(a, batches);
@@ -523,17 +515,10 @@ template <int MODE>
 void launch_batch(const sqk::BatchTraceArgs& a, int block, cudaStream_t s)
 {
     if (a.total_batches == 0) return;
-    static int per_sm[3] = {0, 0, 0}, sms = 0;
+    static const int per_sm[3] = {blocks_per_sm(k_trace_batch<MODE>, 64), blocks_per_sm(k_trace_batch<MODE>, 128),
+                                  blocks_per_sm(k_trace_batch<MODE>, 256)};
     const int bi = block <= 64 ? 0 : (block <= 128 ? 1 : 2);
-    if (!per_sm[bi]) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[bi], k_trace_batch<MODE>, block, 0);
-        if (per_sm[bi] <= 0) per_sm[bi] = 1;
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = kNumSMs;
-    }
-    uint32_t grid = (uint32_t)(per_sm[bi] * sms);
+    uint32_t grid = (uint32_t)(per_sm[bi] * sm_count());
     const uint32_t need = (a.total_batches + (uint32_t)(block / 32) - 1) / (uint32_t)(block / 32);
     if (grid > need) grid = need;
     k_trace_batch<MODE><<<grid, block, 0, s>>>(a);
