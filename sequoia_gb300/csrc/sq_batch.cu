@@ -8,8 +8,9 @@
 //                    per mesh) + the code digit histograms
 //   onesweep         stable sort by code, then stable sort by mesh id: the
 //                    result is (mesh, code) order, each mesh contiguous
-//   k_seg_climb      the LBVH climb of sq_lbvh.cu that never merges across a
-//                    mesh boundary; mesh m's root record is slot 3N + 2 + m
+//   climb            the LBVH climb of sq_lbvh.cu (k_lbvh_climb and
+//                    k_lbvh_global over mesh segments): nothing merges across
+//                    a mesh boundary; mesh m's root record is slot 3N + 2 + m
 //   8-wide collapse  (optional) seeded with all mesh roots, a fixed number
 //                    of level kernels with device-side task counts: 8-wide
 //                    node m is mesh m's root
@@ -61,16 +62,6 @@ struct sq_batch {
 namespace {
 
 using namespace sq;
-
-__device__ __forceinline__ uint32_t mesh_of(const uint32_t* __restrict__ off, uint32_t M, uint32_t i)
-{
-    uint32_t lo = 0, hi = M;  // largest m < M with off[m] <= i
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (__ldg(off + mid) <= i) lo = mid; else hi = mid;
-    }
-    return lo;
-}
 
 __device__ __forceinline__ uint32_t spread10(uint32_t v)
 {
@@ -162,87 +153,6 @@ __global__ void k_gather_codes(const uint32_t* __restrict__ perm, uint32_t n, co
         codes[i] = code_by_tri[perm[i]];
 }
 
-// The climb of k_lbvh_climb (sq_lbvh.cu) within mesh segments.
-__global__ void __launch_bounds__(256, 6) k_seg_climb(const uint32_t* __restrict__ codes, const uint32_t* __restrict__ perm,
-                                                   const float* __restrict__ tris, uint32_t n,
-                                                   const uint32_t* __restrict__ off, uint32_t M, Node* __restrict__ nodes,
-                                                   uint32_t* __restrict__ flags, float4* __restrict__ info, uint32_t root0,
-                                                   uint32_t* err)
-{
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t m = mesh_of(off, M, i);
-    const uint32_t sb = off[m], se = off[m + 1];
-    const uint32_t code = codes[i];
-    if (i > sb && codes[i - 1] == code) return;  // not a run head
-    uint32_t e = i + 1;
-    while (e < se && e < i + 8 && codes[e] == code) ++e;
-    if (e == i + 8 && e < se && codes[e] == code) {
-        uint32_t lo = e, hi = se;
-        while (lo < hi) {
-            const uint32_t mid = lo + ((hi - lo) >> 1);
-            if (codes[mid] == code) lo = mid + 1; else hi = mid;
-        }
-        e = lo;
-    }
-    const uint32_t leaf0 = 2u * n + 2u;
-    Box box;
-    box_reset(box);
-    for (uint32_t p = i; p < e; ++p) {
-        const uint32_t t = perm[p];
-        float tv[9];
-        load_tri(tris, t, tv);
-        const Box b = tri_box(tv);
-        store_node(nodes + leaf0 + p, b, t, 1u, kLeafFlag);
-        box_grow(box, b);
-    }
-    uint32_t l = i, r = e, split = 0;
-    if (e - i >= 8) run_subtree(i, e, leaf0, nodes, box, split, err);
-    for (;;) {
-        if (l == sb && r == se) {
-            const uint32_t cnt = se - sb;
-            if (cnt >= 8) store_node(nodes + root0 + m, box, 2u * split, 2u, 0);
-            else store_node(nodes + root0 + m, box, leaf0 + sb, cnt, 0);
-            return;
-        }
-        uint32_t p;
-        bool left;
-        if (l == sb) { p = r; left = true; }
-        else if (r == se) { p = l; left = false; }
-        else {
-            const uint32_t dl = codes[l - 1] ^ codes[l];
-            const uint32_t dr = codes[r - 1] ^ codes[r];
-            if (dr < dl) { p = r; left = true; } else { p = l; left = false; }
-        }
-        float4* mine = info + 2ull * (2ull * p + (left ? 0u : 1u));
-        mine[0] = make_float4(box.mn[0], box.mn[1], box.mn[2], __uint_as_float(left ? l : r));
-        mine[1] = make_float4(box.mx[0], box.mx[1], box.mx[2], __uint_as_float(split));
-        // release my record, acquire the sibling's (the first arrival stops)
-        const uint32_t old = atomic_add_acq_rel_u32(flags + p, 1u);
-        if (old == 0) return;
-        if (old != 1) { raise_error(err, SQ_DEVERR_TOPOLOGY); return; }
-        const float4* sib = info + 2ull * (2ull * p + (left ? 1u : 0u));
-        const float4 s0 = __ldcg(sib), s1 = __ldcg(sib + 1);
-        Box sbx;
-        sbx.mn[0] = s0.x; sbx.mn[1] = s0.y; sbx.mn[2] = s0.z;
-        sbx.mx[0] = s1.x; sbx.mx[1] = s1.y; sbx.mx[2] = s1.z;
-        const uint32_t s_end = __float_as_uint(s0.w), s_split = __float_as_uint(s1.w);
-        uint32_t ll, rr, lsplit, rsplit;
-        Box lb, rb;
-        if (left) { ll = l; rr = s_end; lb = box; rb = sbx; lsplit = split; rsplit = s_split; }
-        else { ll = s_end; rr = r; lb = sbx; rb = box; lsplit = s_split; rsplit = split; }
-        if (rr - ll >= 8) {
-            write_child(nodes, 2u * p, ll, p, lb, lsplit, leaf0);
-            write_child(nodes, 2u * p + 1u, p, rr, rb, rsplit, leaf0);
-        }
-        box = lb;
-        box_grow(box, rb);
-        l = ll;
-        r = rr;
-        split = p;
-    }
-}
-
 // root records of meshes without triangles
 __global__ void k_empty_roots(const uint32_t* __restrict__ off, uint32_t M, Node* __restrict__ nodes, uint32_t root0,
                               uint32_t leaf0)
@@ -304,8 +214,10 @@ sq_status enqueue_run(sq_batch* b)
         const int w2 = sqk::sort_passes(mk, sv, ok, ov, N, hist_m, lb_m, ctr + 8, 8, mp, c->ctrl, s);
         uint32_t* perm = w2 ? ov : sv;
         k_gather_codes<<<g, 256, 0, s>>>(perm, N, code_by_tri, codes);
-        k_seg_climb<<<(N + 255) / 256, 256, 0, s>>>(codes, perm, b->d_tris, N, b->d_off, M, b->d_nodes, flags,
-                                                   b->d_info, 3u * N + 2u, c->ctrl);
+        // the climb of a single build, per mesh segment; the open-node list
+        // after the codes, its count in mesh 0's two spare box words
+        sqk::lbvh_climb_seg(codes, perm, b->d_tris, N, b->d_off, M, 3u * N + 2u, b->d_nodes, flags, b->d_info,
+                            codes + N, box_ord + 6, c->ctrl, s);
     }
     k_empty_roots<<<(M + 255) / 256, 256, 0, s>>>(b->d_off, M, b->d_nodes, 3u * N + 2u, 2u * N + 2u);
     const bool wide = b->params.wide != 0;
@@ -484,8 +396,8 @@ sq_status sq_batch_create(sq_ctx* c, const sq_batch_mesh* meshes, uint32_t mesh_
     b->d_tris8 = dalloc(c, sqk::bvh8_tri_bytes(N));
     b->d_ws8 = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * (sqk::bvh8_ws_words(N) + 4ull * M)));
     b->d_zero = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * zero));
-    b->d_keys = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * 6ull * (N ? N : 1)));
-    b->d_info = static_cast<float4*>(dalloc(c, sizeof(float4) * 4ull * (N ? N : 1)));
+    b->d_keys = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * 7ull * (N ? N : 1)));
+    b->d_info = static_cast<float4*>(dalloc(c, sizeof(float4) * 6ull * (N ? N : 1)));
     b->d_hits = static_cast<sq_hit*>(dalloc(c, sizeof(sq_hit) * (rays ? rays : 1)));
     b->d_heat = static_cast<uint8_t*>(dalloc(c, 3ull * (rays ? rays : 1)));
     if (!b->d_tris || !b->d_off || !b->d_rays || !b->d_jobs || !b->d_roots || !b->d_nodes || !b->d_nodes8 ||

@@ -216,6 +216,11 @@ void morton_codes(const float* tris, uint32_t n, uint32_t mode, const uint32_t* 
 // surv_count: one zeroed word.
 void lbvh_climb(const uint32_t* codes, const uint32_t* perm, const float* tris, uint32_t n, sq::Node* nodes,
                 uint32_t* flags, float4* info, uint32_t* surv, uint32_t* surv_count, uint32_t* err, cudaStream_t s);
+// The same climb over a batch: mesh m holds sorted positions [off[m],
+// off[m + 1]) and gets its own tree, rooted at record root0 + m.
+void lbvh_climb_seg(const uint32_t* codes, const uint32_t* perm, const float* tris, uint32_t n, const uint32_t* off,
+                    uint32_t M, uint32_t root0, sq::Node* nodes, uint32_t* flags, float4* info, uint32_t* surv,
+                    uint32_t* surv_count, uint32_t* err, cudaStream_t s);
 // 60-bit codes (build_hierarchy_morton2): codes as low / high words with the
 // histograms of 8 digit passes (4 per word); the high words re-ordered by
 // the first sort stage; the combined sorted codes and permutation; the

@@ -278,16 +278,31 @@ __device__ __forceinline__ void publish_record(float4* __restrict__ info, uint32
 // block takes its slots with one atomic on surv_count.  Splitting the climb
 // this way lets these blocks retire at once: waiting out a global climb held
 // their SM slots from the blocks still to run.
-template <class Code>
+//
+// SEG: positions [off[m], off[m + 1]) hold mesh m of a batch, sorted by
+// (mesh, code), and each mesh gets its own tree: runs, parents and the root
+// never cross a segment boundary, and mesh m's root record goes to slot
+// root0 + m (without SEG the single segment is [0, n) and its root slot 0).
+// Parent boundaries of different meshes never coincide: a node's parent
+// boundary lies strictly inside its mesh's range.
+template <class Code, bool SEG>
 __global__ void __launch_bounds__(256, 6) k_lbvh_climb(const Code* __restrict__ codes, const uint32_t* __restrict__ perm,
                                                     const float* __restrict__ tris, uint32_t n, Node* __restrict__ nodes,
                                                     float4* __restrict__ info, uint32_t* __restrict__ surv,
-                                                    uint32_t* __restrict__ surv_count, uint32_t* err)
+                                                    uint32_t* __restrict__ surv_count, const uint32_t* __restrict__ off,
+                                                    uint32_t M, uint32_t root0, uint32_t* err)
 {
     constexpr uint32_t FULL = 0xFFFFFFFFu;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = (int)(threadIdx.x & 31u);
     const uint32_t leaf0 = 2u * n + 2u;
+    // this position's segment [sb, se) and mesh
+    uint32_t sb = 0, se = n, m = 0;
+    if (SEG && i < n) {
+        m = mesh_of(off, M, i);
+        sb = __ldg(off + m);
+        se = __ldg(off + m + 1);
+    }
     // this lane's node: [l, r) with its box and split, while `active`
     bool active = false;
     uint32_t l = 0, r = 0, split = 0;
@@ -305,14 +320,14 @@ __global__ void __launch_bounds__(256, 6) k_lbvh_climb(const Code* __restrict__ 
     const Code d_own = prev ^ code;
     const Code d_end = __shfl_sync(FULL, code ^ next, 31);
     if (i < n) {
-        if (i == 0 || prev != code) {  // a run head
+        if (i == sb || prev != code) {  // a run head
             uint32_t e = i + 1;
-            if (e < n && next == code) {
+            if (e < se && next == code) {
                 ++e;
-                while (e < n && e < i + 8 && codes[e] == code) ++e;
+                while (e < se && e < i + 8 && codes[e] == code) ++e;
             }
-            if (e == i + 8 && e < n && codes[e] == code) {
-                uint32_t lo = e, hi = n;
+            if (e == i + 8 && e < se && codes[e] == code) {
+                uint32_t lo = e, hi = se;
                 while (lo < hi) {
                     const uint32_t mid = lo + ((hi - lo) >> 1);
                     if (codes[mid] == code) lo = mid + 1; else hi = mid;
@@ -343,7 +358,7 @@ __global__ void __launch_bounds__(256, 6) k_lbvh_climb(const Code* __restrict__ 
             dl = d_own;
             if (r_in) dr = dr_in;
             else if (r == W + 32u) dr = d_end;
-            else if (r < n) dr = codes[r - 1] ^ codes[r];
+            else if (r < se) dr = codes[r - 1] ^ codes[r];
         }
     }
 
@@ -351,14 +366,15 @@ __global__ void __launch_bounds__(256, 6) k_lbvh_climb(const Code* __restrict__ 
     // has the smaller code XOR with its neighbour); the node is its left
     // child when the split is at r.
     auto parent_of = [&](uint32_t& p, bool& left) {
-        if (l == 0) { p = r; left = true; }
-        else if (r == n) { p = l; left = false; }
+        if (l == sb) { p = r; left = true; }
+        else if (r == se) { p = l; left = false; }
         else if (dr < dl) { p = r; left = true; }
         else { p = l; left = false; }
     };
     auto write_root = [&]() {
-        if (n >= 8) store_node(nodes, box, 2u * split, 2u, 0);
-        else store_node(nodes, box, leaf0, n, 0);
+        Node* root = nodes + (SEG ? root0 + m : 0u);
+        if (se - sb >= 8) store_node(root, box, 2u * split, 2u, 0);
+        else store_node(root, box, leaf0 + sb, se - sb, 0);
     };
     // Merge this node with its sibling (ending or starting at s_end, with the
     // code XOR s_d at that far boundary): write both children's records when
@@ -385,7 +401,7 @@ __global__ void __launch_bounds__(256, 6) k_lbvh_climb(const Code* __restrict__ 
     // the nodes left then go to the global protocol (k_lbvh_global).  Most
     // small subtrees never touch the sibling records or the flags.
     for (;;) {
-        if (active && l == 0 && r == n) { write_root(); active = false; }
+        if (active && l == sb && r == se) { write_root(); active = false; }
         const uint32_t A = __ballot_sync(FULL, active);
         if (!A) break;
         bool merged = false;
@@ -436,11 +452,12 @@ __global__ void __launch_bounds__(256, 6) k_lbvh_climb(const Code* __restrict__ 
 // arrival at its parent boundary (release its record, acquire the sibling's);
 // the second arrival merges the two and continues with the parent, whose
 // record it publishes first.  Nothing waits: a first arrival stops.
-template <class Code>
+template <class Code, bool SEG>
 __global__ void __launch_bounds__(256) k_lbvh_global(const uint32_t* __restrict__ surv,
                                                      const uint32_t* __restrict__ surv_count, uint32_t n,
                                                      Node* __restrict__ nodes, uint32_t* __restrict__ flags,
-                                                     float4* __restrict__ info, uint32_t* err)
+                                                     float4* __restrict__ info, const uint32_t* __restrict__ off,
+                                                     uint32_t M, uint32_t root0, uint32_t* err)
 {
     const uint32_t leaf0 = 2u * n + 2u;
     const uint32_t count = *surv_count;
@@ -448,6 +465,13 @@ __global__ void __launch_bounds__(256) k_lbvh_global(const uint32_t* __restrict_
         const uint32_t e = surv[t];
         uint32_t p = e & 0x7FFFFFFFu;
         bool left = (e >> 31) != 0u;
+        // the node's segment: its parent boundary lies inside it
+        uint32_t sb = 0, se = n, m = 0;
+        if (SEG) {
+            m = mesh_of(off, M, p);
+            sb = __ldg(off + m);
+            se = __ldg(off + m + 1);
+        }
         // this node from its own record; the XOR at its near end (boundary p)
         // is not needed: the merge replaces it with the sibling's far XOR
         const float4* mine = info + 3ull * (2ull * p + (left ? 0u : 1u));
@@ -463,13 +487,14 @@ __global__ void __launch_bounds__(256) k_lbvh_global(const uint32_t* __restrict_
         else { l = p; r = __float_as_uint(m0.w); dr = dfar; }
         for (bool first = true;; first = false) {
             if (!first) {
-                if (l == 0 && r == n) {
-                    if (n >= 8) store_node(nodes, box, 2u * split, 2u, 0);
-                    else store_node(nodes, box, leaf0, n, 0);
+                if (l == sb && r == se) {
+                    Node* root = nodes + (SEG ? root0 + m : 0u);
+                    if (se - sb >= 8) store_node(root, box, 2u * split, 2u, 0);
+                    else store_node(root, box, leaf0 + sb, se - sb, 0);
                     break;
                 }
-                if (l == 0) { p = r; left = true; }
-                else if (r == n) { p = l; left = false; }
+                if (l == sb) { p = r; left = true; }
+                else if (r == se) { p = l; left = false; }
                 else if (dr < dl) { p = r; left = true; }
                 else { p = l; left = false; }
                 publish_record(info, p, left, box, left ? l : r, split, (uint64_t)(left ? dl : dr));
@@ -552,28 +577,38 @@ void combine64(const uint32_t* hi_sorted, const uint32_t* perm2, const uint32_t*
                                                                             codes64, perm);
 }
 
-template <class Code>
+template <class Code, bool SEG>
 void climb_launch(const Code* codes, const uint32_t* perm, const float* tris, uint32_t n, sq::Node* nodes,
-                  uint32_t* flags, float4* info, uint32_t* surv, uint32_t* surv_count, uint32_t* err, cudaStream_t s)
+                  uint32_t* flags, float4* info, uint32_t* surv, uint32_t* surv_count, const uint32_t* off, uint32_t M,
+                  uint32_t root0, uint32_t* err, cudaStream_t s)
 {
     if (n == 0) return;
-    k_lbvh_climb<Code><<<(n + 255) / 256, 256, 0, s>>>(codes, perm, tris, n, nodes, info, surv, surv_count, err);
+    k_lbvh_climb<Code, SEG><<<(n + 255) / 256, 256, 0, s>>>(codes, perm, tris, n, nodes, info, surv, surv_count, off, M,
+                                                            root0, err);
     // one thread per possible open node (their count is on the device): the
     // climbs are chains of round trips, so running them all at once beats a
     // grid-stride loop over fewer threads
-    k_lbvh_global<Code><<<(n + 255) / 256, 256, 0, s>>>(surv, surv_count, n, nodes, flags, info, err);
+    k_lbvh_global<Code, SEG><<<(n + 255) / 256, 256, 0, s>>>(surv, surv_count, n, nodes, flags, info, off, M, root0,
+                                                             err);
 }
 
 void lbvh_climb(const uint32_t* codes, const uint32_t* perm, const float* tris, uint32_t n, sq::Node* nodes,
                 uint32_t* flags, float4* info, uint32_t* surv, uint32_t* surv_count, uint32_t* err, cudaStream_t s)
 {
-    climb_launch<uint32_t>(codes, perm, tris, n, nodes, flags, info, surv, surv_count, err, s);
+    climb_launch<uint32_t, false>(codes, perm, tris, n, nodes, flags, info, surv, surv_count, nullptr, 1u, 0u, err, s);
+}
+
+void lbvh_climb_seg(const uint32_t* codes, const uint32_t* perm, const float* tris, uint32_t n, const uint32_t* off,
+                    uint32_t M, uint32_t root0, sq::Node* nodes, uint32_t* flags, float4* info, uint32_t* surv,
+                    uint32_t* surv_count, uint32_t* err, cudaStream_t s)
+{
+    climb_launch<uint32_t, true>(codes, perm, tris, n, nodes, flags, info, surv, surv_count, off, M, root0, err, s);
 }
 
 void lbvh_climb64(const uint64_t* codes, const uint32_t* perm, const float* tris, uint32_t n, sq::Node* nodes,
                   uint32_t* flags, float4* info, uint32_t* surv, uint32_t* surv_count, uint32_t* err, cudaStream_t s)
 {
-    climb_launch<uint64_t>(codes, perm, tris, n, nodes, flags, info, surv, surv_count, err, s);
+    climb_launch<uint64_t, false>(codes, perm, tris, n, nodes, flags, info, surv, surv_count, nullptr, 1u, 0u, err, s);
 }
 
 }  // namespace sqk

@@ -6,6 +6,18 @@
 
 namespace sq {
 
+// Mesh of position i in a batch whose mesh m holds positions
+// [off[m], off[m + 1]): the largest m < M with off[m] <= i.
+__device__ __forceinline__ uint32_t mesh_of(const uint32_t* __restrict__ off, uint32_t M, uint32_t i)
+{
+    uint32_t lo = 0, hi = M;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(off + mid) <= i) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
 struct RunFrame {
     uint32_t b, e, slot, state;
     Box acc;
