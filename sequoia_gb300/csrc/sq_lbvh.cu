@@ -259,8 +259,6 @@ __global__ void k_combine64(const uint32_t* __restrict__ hi_sorted, const uint32
 // ---------------------------------------------------------------------------
 // climb
 
-// 256 threads and at most 40 registers: six blocks per SM, so more blocks
-// overlap their leaf gathers and global-phase round trips.
 // Sibling record of a node beside its parent boundary p: box, far end,
 // split and the code XOR at the far end (left child: slot 2p, right: 2p + 1).
 __device__ __forceinline__ void publish_record(float4* __restrict__ info, uint32_t p, bool left, const Box& box,
@@ -284,7 +282,8 @@ __device__ __forceinline__ void publish_record(float4* __restrict__ info, uint32
 // never cross a segment boundary, and mesh m's root record goes to slot
 // root0 + m (without SEG the single segment is [0, n) and its root slot 0).
 // Parent boundaries of different meshes never coincide: a node's parent
-// boundary lies strictly inside its mesh's range.
+// boundary lies strictly inside its mesh's range.  256 threads and at most
+// 40 registers: six blocks per SM, so more blocks overlap their leaf gathers.
 template <class Code, bool SEG>
 __global__ void __launch_bounds__(256, 6) k_lbvh_climb(const Code* __restrict__ codes, const uint32_t* __restrict__ perm,
                                                     const float* __restrict__ tris, uint32_t n, Node* __restrict__ nodes,
