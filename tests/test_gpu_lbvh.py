@@ -151,6 +151,20 @@ def test_invalid_arguments(ctx):
         ctx.radix_sort_pairs(np.zeros(4, np.uint32), np.zeros(4, np.uint32), 0, 8)
 
 
+def test_wide_triangle_limit(ctx):
+    """The 8-wide form addresses at most 2^27 triangles (27-bit leaf entries):
+    a larger build is refused before the input is read."""
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+    import sequoia_gb300 as sq
+    one = torch.zeros(9, dtype=torch.float32, device="cuda")  # never read
+    p = sq._BuildParams(sq.BUILDERS["morton"], 8, 8, 8, 0, 2)
+    h = C.c_void_p()
+    st = sq.load_library().sq_build(ctx.handle, C.c_void_p(one.data_ptr()), (1 << 27) + 1, C.byref(p), C.byref(h))
+    assert st == 5 and not h.value  # SQ_ERR_UNSUPPORTED, no BVH
+    assert ctx.sync() == 0
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["ico3", "ico4", "soup3k", "dups2k"])
 def test_morton64_golden(ctx, oracle, name):
