@@ -262,9 +262,11 @@ sq_status sq_bvh_export_sorted64(sq_bvh* bvh, uint64_t* codes, uint32_t* perm);
  * array inside the library (about 12.6 MB, held on each GPU where the
  * library's code is loaded until the process exits).  n above
  * SQ_NOALLOC_MAX_KEYS returns SQ_ERR_TOO_LARGE before touching anything.
- * Runs on `stream` (NULL = legacy default stream) and returns when the sort
- * has finished.  The first call on a device looks up the scratch address
- * there; make it before any stream capture.  Calls share the scratch, so
+ * Runs on `stream` (NULL = legacy default stream).  Every call ends by
+ * reading the scratch's error word back and synchronising `stream`, so it
+ * returns only when the sort has finished.  The first call on a device also
+ * looks up the scratch address there; make it before any stream capture
+ * begins.  Calls share the scratch, so
  * calls that overlap on the GPU race and must not be issued.  keys_out /
  * values_out may alias keys_in / values_in.                                */
 #define SQ_NOALLOC_MAX_KEYS (1u << 20)

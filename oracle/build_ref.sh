@@ -2,9 +2,10 @@
 # Build the Sequoia reference's own CPU code into oracle/_ref/ (test
 # infrastructure only; outputs are git-ignored).
 #
-# Sources are read where they lie in the reference tree (default
-# /root/reference/src, override with SEQUOIA_REF_SRC) and are never copied
-# into this repository.  The only change made on the fly is the bin count:
+# Sources are read where they lie in a checkout of the reference: the
+# directory named by SEQUOIA_REF_SRC (its src/ folder), else the read-only
+# checkout this project was built beside, /root/reference/src.  They are
+# never copied into this repository.  The only change made on the fly is the bin count:
 # `#define NUM_BINS 8` (src/builder.cpp:11) is rewritten to 16 or 32 in a
 # stream fed to the compiler, which is how the 16- and 32-bin SAH
 # configurations of the reference are obtained.

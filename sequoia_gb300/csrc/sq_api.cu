@@ -392,12 +392,15 @@ sq_status sq_sync(sq_ctx* c, uint32_t* device_error)
 
 sq_status sq_build(sq_ctx* c, const sq_triangle* tris, uint32_t n, const sq_build_params* params, sq_bvh** out)
 {
-    if (!c || !out || !params || (n > 0 && !tris)) return fail(c, SQ_ERR_INVALID, "sq_build: null argument");
+    if (!c || !out || !params) return fail(c, SQ_ERR_INVALID, "sq_build: null argument");
+    *out = nullptr;
+    // size limits come before the triangle pointer is looked at, so an
+    // oversize request is refused whatever buffer comes with it
     if (n > (1u << 29)) return fail(c, SQ_ERR_INVALID, "sq_build: n=%u exceeds 2^29", n);
     // the 8-wide traversal's leaf entries hold a 27-bit first-triangle index
     if ((params->flags & SQ_BUILD_WIDE8) && n > sqk::kWide8MaxTris)
         return fail(c, SQ_ERR_UNSUPPORTED, "sq_build: the 8-wide BVH takes at most 2^27 triangles (n=%u)", n);
-    *out = nullptr;
+    if (n > 0 && !tris) return fail(c, SQ_ERR_INVALID, "sq_build: null triangles");
     Guard g(c->device);
     sq_build_params p = *params;
     if (p.kind != SQ_BUILDER_MORTON && p.kind != SQ_BUILDER_SAH && p.kind != SQ_BUILDER_GRID)

@@ -1301,7 +1301,10 @@ void launch8(const sqk::Trace8Args& a, cudaStream_t s)
     if (a.ray_kind == SQ_RAYS_EXPLICIT) batches = (a.ray_count + 31u) / 32u;
     else batches = ((a.width + 7u) / 8u) * ((a.height + 3u) / 4u);
     if (batches == 0) return;
-    static const int per_sm[2] = {blocks_per_sm(k_trace8_tiles<MODE>, 128), blocks_per_sm(k_trace8_refill<MODE>, 128)};
+    static PerDevice<std::array<int, 2>> cache;
+    const std::array<int, 2> per_sm = cache.get([] {
+        return std::array<int, 2>{blocks_per_sm(k_trace8_tiles<MODE>, 128), blocks_per_sm(k_trace8_refill<MODE>, 128)};
+    });
     const int v = a.refill ? 1 : 0;
     uint32_t grid = (uint32_t)(per_sm[v] * sm_count());
     const uint32_t need = (batches + 3u) / 4u;
@@ -1497,14 +1500,18 @@ template <int MODE>
 void launch8_batch(const sqk::BatchTraceArgs& a, int block, cudaStream_t s)
 {
     if (a.total_batches == 0) return;
-    static const int per_sm[2][3] = {
-        {blocks_per_sm(k_trace8_batch_tiles<MODE>, 64), blocks_per_sm(k_trace8_batch_tiles<MODE>, 128),
-         blocks_per_sm(k_trace8_batch_tiles<MODE>, 256)},
-        {blocks_per_sm(k_trace8_batch_refill<MODE>, 64), blocks_per_sm(k_trace8_batch_refill<MODE>, 128),
-         blocks_per_sm(k_trace8_batch_refill<MODE>, 256)}};
+    static PerDevice<std::array<int, 6>> cache;
+    const std::array<int, 6> per_sm = cache.get([] {
+        return std::array<int, 6>{blocks_per_sm(k_trace8_batch_tiles<MODE>, 64),
+                                  blocks_per_sm(k_trace8_batch_tiles<MODE>, 128),
+                                  blocks_per_sm(k_trace8_batch_tiles<MODE>, 256),
+                                  blocks_per_sm(k_trace8_batch_refill<MODE>, 64),
+                                  blocks_per_sm(k_trace8_batch_refill<MODE>, 128),
+                                  blocks_per_sm(k_trace8_batch_refill<MODE>, 256)};
+    });
     const int bi = block <= 64 ? 0 : (block <= 128 ? 1 : 2);
     const int v = a.refill ? 1 : 0;
-    uint32_t grid = (uint32_t)(per_sm[v][bi] * sm_count());
+    uint32_t grid = (uint32_t)(per_sm[3 * v + bi] * sm_count());
     const uint32_t need = (a.total_batches + (uint32_t)(block / 32) - 1) / (uint32_t)(block / 32);
     if (grid > need) grid = need;
     if (v) k_trace8_batch_refill<MODE><<<grid, block, 0, s>>>(a);
@@ -1537,7 +1544,8 @@ int build_bvh8_queue(const Node* rec, const uint32_t* roots_dev, uint32_t nroots
     cudaError_t e;
     if ((e = cudaMemsetAsync(ws, 0, sizeof(uint32_t) * (16 + kFixedLevels), s)) != cudaSuccess) return (int)e;
     k_fixed_seed<<<(nroots + 255) / 256, 256, 0, s>>>(roots_dev, nroots, ta, na, counts, node_counter);
-    static const int grid = blocks_per_sm(k_collapse_fixed, 128) * sm_count();
+    static PerDevice<int> cache;
+    const int grid = cache.get([] { return blocks_per_sm(k_collapse_fixed, 128) * sm_count(); });
     for (uint32_t level = 0; level < kFixedLevels; ++level) {
         uint32_t* in_t = (level & 1) ? tb : ta;
         uint32_t* in_n = (level & 1) ? nb : na;
@@ -1603,13 +1611,13 @@ int build_bvh8(const Node* rec, uint32_t root, uint32_t leaf0, const float* tris
     host_ctl[5] = 0;
     // every block of the cooperative collapse must be resident: the grid is
     // the occupancy limit (0: no cooperative launch, use the per-level path)
-    static const int grid = [] {
-        int dev = 0, coop = 0, per_sm = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    static PerDevice<int> cache;
+    const int grid = cache.get([] {
+        int coop = 0, per_sm = 0;
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, current_device());
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collapse_coop, 256, 0);
         return (coop && per_sm > 0) ? per_sm * sm_count() : 0;
-    }();
+    });
     if (grid == 0) return build_bvh8_levels(rec, root, leaf0, tris, n, nodes8, tris8, ws, host_ctl, err, s);
     const uint32_t capacity = bvh8_capacity(n);
     cudaError_t e;

@@ -6,9 +6,12 @@
 // reference's own comparisons (see ref_min / ref_max / simd_max below).
 #pragma once
 
+#include <array>
+#include <atomic>
 #include <cfloat>
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <cuda_runtime.h>
 
 #include "../../include/sequoia_gpu.h"
@@ -145,21 +148,57 @@ __device__ __forceinline__ void raise_error(uint32_t* err, uint32_t bit)
 }
 
 constexpr int kNumSMs = 152;
+constexpr int kMaxDevices = 64;
 
-// Multiprocessor count of the current device, queried once per process
-// (a function-local static: initialised once even under concurrent calls).
-inline int sm_count()
+inline int current_device()
 {
-    static const int v = [] {
-        int dev = 0, n = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        return n > 0 ? n : kNumSMs;
-    }();
-    return v;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return dev;
 }
 
-// Resident blocks per SM of a kernel at a block size (at least 1).
+// A launch setting computed once per device: the first use on each device
+// (the current one) computes it under a lock; later uses read it without
+// one.  Occupancy, SM counts and function attributes such as the
+// shared-memory opt-in belong to one device, so a process that drives
+// contexts on several GPUs gets each GPU's own value.  Declare instances as
+// function-local statics.
+template <class T>
+class PerDevice {
+public:
+    template <class Make>
+    T get(Make&& make)
+    {
+        const int dev = current_device();
+        if (dev < 0 || dev >= kMaxDevices) return make();
+        if (ready_[dev].load(std::memory_order_acquire)) return value_[dev];
+        std::lock_guard<std::mutex> lock(mu_);
+        if (!ready_[dev].load(std::memory_order_relaxed)) {
+            value_[dev] = make();
+            ready_[dev].store(true, std::memory_order_release);
+        }
+        return value_[dev];
+    }
+
+private:
+    std::mutex mu_;
+    std::atomic<bool> ready_[kMaxDevices] = {};
+    T value_[kMaxDevices] = {};
+};
+
+// Multiprocessor count of the current device.
+inline int sm_count()
+{
+    static PerDevice<int> cache;
+    return cache.get([] {
+        int n = 0;
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, current_device());
+        return n > 0 ? n : kNumSMs;
+    });
+}
+
+// Resident blocks per SM of a kernel at a block size on the current device
+// (at least 1).
 template <class Kernel>
 inline int blocks_per_sm(Kernel kernel, int threads)
 {

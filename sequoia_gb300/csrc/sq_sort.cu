@@ -245,11 +245,13 @@ void launch_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint3
                  const uint32_t* hist, uint32_t* lookback, uint32_t* counter, uint32_t* err, cudaStream_t s)
 {
     const size_t bytes = Smem<DB>::bytes;
-    static const bool configured = [] {
+    // the opt-in above 48 KB of dynamic shared memory is a per-device
+    // attribute of the function: set it on each device's first use
+    static PerDevice<bool> configured;
+    configured.get([] {
         cudaFuncSetAttribute(k_onesweep<DB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Smem<DB>::bytes);
         return true;
-    }();
-    (void)configured;
+    });
     const uint32_t tiles = (n + kTile - 1) / kTile;
     k_onesweep<DB><<<tiles, kBlock, bytes, s>>>(kin, vin, kout, vout, n, shift, hist, lookback, counter, err);
 }

@@ -427,7 +427,8 @@ void launch(const sqk::TraceArgs& a, cudaStream_t s)
     if (a.ray_kind == SQ_RAYS_EXPLICIT) batches = (a.ray_count + 31u) / 32u;
     else batches = ((a.width + 7u) / 8u) * ((a.height + 3u) / 4u);
     if (batches == 0) return;
-    static const int per_sm = blocks_per_sm(k_trace<MODE>, 128);
+    static PerDevice<int> cache;
+    const int per_sm = cache.get([] { return blocks_per_sm(k_trace<MODE>, 128); });
     uint32_t grid = (uint32_t)(per_sm * sm_count());
     const uint32_t need = (batches + 3u) / 4u;
     if (grid > need) grid = need;
@@ -515,8 +516,11 @@ template <int MODE>
 void launch_batch(const sqk::BatchTraceArgs& a, int block, cudaStream_t s)
 {
     if (a.total_batches == 0) return;
-    static const int per_sm[3] = {blocks_per_sm(k_trace_batch<MODE>, 64), blocks_per_sm(k_trace_batch<MODE>, 128),
+    static PerDevice<std::array<int, 3>> cache;
+    const std::array<int, 3> per_sm = cache.get([] {
+        return std::array<int, 3>{blocks_per_sm(k_trace_batch<MODE>, 64), blocks_per_sm(k_trace_batch<MODE>, 128),
                                   blocks_per_sm(k_trace_batch<MODE>, 256)};
+    });
     const int bi = block <= 64 ? 0 : (block <= 128 ? 1 : 2);
     uint32_t grid = (uint32_t)(per_sm[bi] * sm_count());
     const uint32_t need = (a.total_batches + (uint32_t)(block / 32) - 1) / (uint32_t)(block / 32);

@@ -153,15 +153,19 @@ def test_invalid_arguments(ctx):
 
 def test_wide_triangle_limit(ctx):
     """The 8-wide form addresses at most 2^27 triangles (27-bit leaf entries):
-    a larger build is refused before the input is read."""
-    torch = pytest.importorskip("torch")
+    a larger build is refused before the input is looked at.  No buffer comes
+    with the request (a null triangle pointer), so the call cannot read
+    memory whatever order its checks run in; the handle is cleared."""
     import ctypes as C
     import sequoia_gb300 as sq
-    one = torch.zeros(9, dtype=torch.float32, device="cuda")  # never read
     p = sq._BuildParams(sq.BUILDERS["morton"], 8, 8, 8, 0, 2)
-    h = C.c_void_p()
-    st = sq.load_library().sq_build(ctx.handle, C.c_void_p(one.data_ptr()), (1 << 27) + 1, C.byref(p), C.byref(h))
+    h = C.c_void_p(0x1000)  # not null: the call must clear it
+    st = sq.load_library().sq_build(ctx.handle, None, (1 << 27) + 1, C.byref(p), C.byref(h))
     assert st == 5 and not h.value  # SQ_ERR_UNSUPPORTED, no BVH
+    # within the limit, a null triangle pointer is an invalid argument
+    h = C.c_void_p(0x1000)
+    st = sq.load_library().sq_build(ctx.handle, None, 16, C.byref(p), C.byref(h))
+    assert st == 1 and not h.value
     assert ctx.sync() == 0
 
 

@@ -36,7 +36,9 @@ def test_noalloc_sort_matches_allocating_sort(lib_built):
     ctx = sq.Context(0)
     fn = noalloc_fn()
     stream = torch.cuda.current_stream().cuda_stream
-    cases = [(300_001, 30, 8), (MAX_KEYS, 32, 10), (4097, 32, 6), (1, 8, 8)]
+    # (n, key bits, digit bits): even and odd pass counts (4, 4, 6, 3, 1),
+    # the largest size, a size one past a tile, a single key
+    cases = [(300_001, 30, 8), (MAX_KEYS, 32, 10), (4097, 32, 6), (65_537, 24, 8), (1, 8, 8)]
     for n, key_bits, digit_bits in cases:
         for call in range(2):  # two calls in a row share the scratch
             rng = np.random.default_rng(1000 * call + n + digit_bits)
@@ -60,10 +62,11 @@ def test_noalloc_sort_matches_allocating_sort(lib_built):
 
 
 def test_noalloc_rejects_oversize_and_host_pointers(lib_built):
-    torch = pytest.importorskip("torch")
+    """Sizes beyond the fixed maximum are refused with SQ_ERR_TOO_LARGE.  The
+    oversize request carries null buffers, so it cannot touch memory whatever
+    order the checks run in; host buffers are refused as invalid."""
     fn = noalloc_fn()
-    d = torch.zeros(16, dtype=torch.int32, device="cuda")
-    p = d.data_ptr()
-    assert fn(p, p, MAX_KEYS + 1, 32, 8, p, p, None) == TOO_LARGE
+    assert fn(None, None, MAX_KEYS + 1, 32, 8, None, None, None) == TOO_LARGE
+    assert fn(None, None, 0xFFFFFFFF, 32, 8, None, None, None) == TOO_LARGE
     h = np.zeros(16, np.uint32)
     assert fn(h.ctypes.data, h.ctypes.data, 16, 32, 8, h.ctypes.data, h.ctypes.data, None) == 1
