@@ -14,6 +14,7 @@
 
 #include <omp.h>
 
+#include <chrono>
 #include <cstdint>
 #include <cstring>
 #include <string>
@@ -163,6 +164,30 @@ int ref_build_only(int kind, const float* tris, uint32_t n)
     return 0;
 }
 
+// Wall time of one build, in milliseconds (steady clock around the builder
+// call only; the triangle conversion and the node array's release are
+// outside).  kind as ref_build.  Returns a negative value for an unknown
+// kind.
+double ref_time_build(int kind, const float* tris, uint32_t n)
+{
+    std::vector<Triangle> v = to_tris(tris, n);
+    Hierarchy h;
+    const auto t0 = std::chrono::steady_clock::now();
+    switch (kind) {
+    case 0: h = Builder::build_hierarchy(v); break;
+    case 1: h = Builder::build_hierarchy_horizontal(v); break;
+    case 2: h = Builder::build_hierarchy_grid(v); break;
+    case 3: h = Builder::build_hierarchy_grid_sse(v); break;
+    case 4: h = Builder::build_hierarchy_grid_m128(v); break;
+    case 5: h = Builder::build_hierarchy_morton(v); break;
+    case 6: h = Builder::build_hierarchy_morton2(v); break;
+    default: return -1.0;
+    }
+    const auto t1 = std::chrono::steady_clock::now();
+    delete[] h.node_base;
+    return std::chrono::duration<double, std::milli>(t1 - t0).count();
+}
+
 static Hierarchy make_h(Node1* nodes, uint32_t node_count, uint32_t root, std::vector<Triangle>& v)
 {
     Hierarchy h;
@@ -202,6 +227,28 @@ int ref_trace(int tracer, const Node1* nodes, uint32_t node_count, uint32_t root
     memcpy(img, r, (size_t)w * h * 3);
     delete[] r;
     return 0;
+}
+
+// Wall time of one trace() / trace_packet<K> / trace_bundle<K> call in
+// milliseconds (steady clock around the tracer only).  tracer as ref_trace.
+double ref_time_trace(int tracer, const Node1* nodes, uint32_t node_count, uint32_t root, const float* tris,
+                      uint32_t n, uint32_t w, uint32_t h, const float* origin)
+{
+    std::vector<Triangle> v = to_tris(tris, n);
+    std::vector<Node1> nd(nodes, nodes + node_count);
+    Hierarchy hh = make_h(nd.data(), node_count, root, v);
+    vec3f1 o(origin[0], origin[1], origin[2]);
+    uint8_t* r = nullptr;
+    const auto t0 = std::chrono::steady_clock::now();
+    switch (tracer) {
+    case 0: r = trace(hh, w, h, o); break;
+    case 1: r = trace_packet<8>(hh, w, h, o); break;
+    case 2: r = trace_bundle<64>(hh, w, h, o); break;
+    default: return -1.0;
+    }
+    const auto t1 = std::chrono::steady_clock::now();
+    delete[] r;
+    return std::chrono::duration<double, std::milli>(t1 - t0).count();
 }
 
 // traverse (src/tracer.cpp:47) for explicit rays {ox,oy,oz,tmin,dx,dy,dz,tmax}

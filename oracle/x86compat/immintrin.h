@@ -241,13 +241,14 @@ SQX_INLINE int sqx_movemask(const V& v)
     }
     return m;
 }
-#define __builtin_ia32_pmovmskb(x) sqx_movemask(x)
-#define __builtin_ia32_pmovmskb128(x) sqx_movemask(x)
-#define __builtin_ia32_pmovmskb256(x) sqx_movemask(x)
-#define __builtin_ia32_movmskps(x) sqx_movemask(x)
-#define __builtin_ia32_movmskps256(x) sqx_movemask(x)
-#define __builtin_ia32_movmskpd(x) sqx_movemask(x)
-#define __builtin_ia32_movmskpd256(x) sqx_movemask(x)
+/* variadic: the argument may hold template commas, as in simd<K, char>(a) */
+#define __builtin_ia32_pmovmskb(...) sqx_movemask(__VA_ARGS__)
+#define __builtin_ia32_pmovmskb128(...) sqx_movemask(__VA_ARGS__)
+#define __builtin_ia32_pmovmskb256(...) sqx_movemask(__VA_ARGS__)
+#define __builtin_ia32_movmskps(...) sqx_movemask(__VA_ARGS__)
+#define __builtin_ia32_movmskps256(...) sqx_movemask(__VA_ARGS__)
+#define __builtin_ia32_movmskpd(...) sqx_movemask(__VA_ARGS__)
+#define __builtin_ia32_movmskpd256(...) sqx_movemask(__VA_ARGS__)
 #endif
 
 #endif /* SQ_X86COMPAT_IMMINTRIN_H */

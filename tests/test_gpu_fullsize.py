@@ -9,7 +9,8 @@ configuration names a builder.  The 8-wide quantised form must give the same
 ids and t as the binary tree on every ray.  The t error of each hit against
 an FP64 re-intersection of the same (ray, triangle) is printed and bounded;
 the GPU's t equals the oracle's bit for bit, so it is within 1e-6 relative
-of it by construction.
+of it by construction, and its FP64 error is no larger than that of the
+reference's own FP32 Moller-Trumbore t on the same hits.
 
 Configurations (seeded synthetic scenes of the stated shapes and sizes):
 
@@ -62,15 +63,42 @@ def assert_same_hits(hits, ids, ts, tests=None, what=""):
         assert np.array_equal(hits["tests"], tests), what + ": box-test counts"
 
 
+def moller_trumbore_t(tris, rays, ids):
+    """t of the reference's FP32 Moller-Trumbore formula (src/tracer.h:94-111:
+    edge1, edge2, h = d x edge2, a = edge1 . h, f = 1/a, s = o - v0,
+    q = s x edge1, t = f * (edge2 . q)), one rounding per operation, for
+    stating how far the reference's own arithmetic is from FP64."""
+    f32 = np.float32
+    v = tris[ids].reshape(-1, 3, 3).astype(f32)
+    o, d = rays[:, 0:3].astype(f32), rays[:, 4:7].astype(f32)
+
+    def cross(a, b):
+        return np.stack([a[:, 1] * b[:, 2] - b[:, 1] * a[:, 2], a[:, 2] * b[:, 0] - b[:, 2] * a[:, 0],
+                         a[:, 0] * b[:, 1] - b[:, 0] * a[:, 1]], 1)
+
+    def dot(a, b):
+        return (a[:, 0] * b[:, 0] + a[:, 1] * b[:, 1]) + a[:, 2] * b[:, 2]
+
+    e1, e2 = v[:, 1] - v[:, 0], v[:, 2] - v[:, 0]
+    a = dot(e1, cross(d, e2))
+    q = cross(o - v[:, 0], e1)
+    return (f32(1) / a) * dot(e2, q)
+
+
 def fp64_error(oracle, tris, rays, hits, label):
     """Relative |t - t64| / |t64| of every hit against the FP64
-    re-intersection; printed and returned as (max, mean, hits)."""
+    re-intersection of the same (ray, triangle), beside the same error of
+    the reference's FP32 Moller-Trumbore t on those hits; printed, and
+    returned as (max, mean, reference formula's max)."""
     m = hits["id"] != NO_HIT
     t64 = oracle.reintersect_f64(tris, rays[m], hits["id"][m])
     rel = np.abs(hits["t"][m].astype(np.float64) - t64) / np.abs(t64)
-    print("%s: t error vs FP64 re-intersection: max %.3g, mean %.3g relative over %d hits"
-          % (label, rel.max(), rel.mean(), int(m.sum())))
-    return float(rel.max()), float(rel.mean()), int(m.sum())
+    mt = moller_trumbore_t(tris, rays[m], hits["id"][m]).astype(np.float64)
+    rel_mt = np.abs(mt - t64) / np.abs(t64)
+    print("%s: t error vs FP64 re-intersection: max %.3g, mean %.3g relative over %d hits "
+          "(the reference's FP32 Moller-Trumbore t on the same hits: max %.3g, mean %.3g)"
+          % (label, rel.max(), rel.mean(), int(m.sum()), rel_mt.max(), rel_mt.mean()))
+    return float(rel.max()), float(rel.mean()), float(rel_mt.max())
 
 
 def test_icosphere_l6_sah16_leaf4(ctx, oracle):
@@ -98,8 +126,8 @@ def test_icosphere_l6_sah16_leaf4(ctx, oracle):
         wide, _ = ctx.trace(bvh, "closest", **cam_kw(cfg))
         assert_same_hits(wide, ids, ts, None, builder + " 8-wide")
         assert (ids != NO_HIT).sum() > len(rays) // 10
-        mx, _, _ = fp64_error(oracle, tris, rays, hits, "icosphere_l6 " + builder)
-        assert mx < T_FP64_BOUND
+        mx, _, mx_ref = fp64_error(oracle, tris, rays, hits, "icosphere_l6 " + builder)
+        assert mx < T_FP64_BOUND and mx <= mx_ref
         bvh.free()
     assert ctx.sync() == 0
 
@@ -127,8 +155,8 @@ def test_soup_2m_morton_every_ray(ctx, oracle, soup_2m):
     wide, _ = ctx.trace(bvh, "closest", **cam_kw(cfg))
     assert_same_hits(wide, ids, ts, None, "8-wide")
     assert (ids != NO_HIT).sum() > len(rays) // 20
-    mx, _, _ = fp64_error(oracle, tris, rays, hits, "soup_2m morton")
-    assert mx < T_FP64_BOUND
+    mx, _, mx_ref = fp64_error(oracle, tris, rays, hits, "soup_2m morton")
+    assert mx < T_FP64_BOUND and mx <= mx_ref
     bvh.free()
     assert ctx.sync() == 0
 
@@ -190,9 +218,10 @@ def test_terrain_4m_primary_and_bounce(ctx, oracle):
     assert_same_hits(bh, bids, bts, btests, "bounce")
     bw, _ = ctx.trace(bvh, "closest", rays=br)
     assert_same_hits(bw, bids, bts, None, "bounce 8-wide")
-    mx_p, _, _ = fp64_error(oracle, tris, rays, hits, "terrain_4m primary")
-    mx_b, _, _ = fp64_error(oracle, tris, br, bh, "terrain_4m bounce")
+    mx_p, _, ref_p = fp64_error(oracle, tris, rays, hits, "terrain_4m primary")
+    mx_b, _, ref_b = fp64_error(oracle, tris, br, bh, "terrain_4m bounce")
     assert mx_p < T_FP64_BOUND and mx_b < T_FP64_BOUND
+    assert mx_p <= ref_p and mx_b <= ref_b
     bvh.free()
     assert ctx.sync() == 0
 
