@@ -8,33 +8,48 @@ trace 3840x2160 pinhole primary rays from (0, 0, -40) aimed at the origin
 (closest hit), writing per-ray hit records and the test-count heatmap to HBM.
 L2 is flushed between steps (512 MB write).
 
-  value      Mrays/s of the whole step: rays / (build + collapse + trace)
-  e2e        the same step through the C ABI with pinned host buffers:
-             triangle upload, build, trace, hit + heatmap download inside
-  plain_fp32 the same rays on the same tree traced as the plain FP32 binary
-             BVH, with the hit ids and t of both forms compared
-  stress     8,000,000-triangle soup (256 clusters, seed 5) and 2^24 rays with
-             origins uniform in the scene box and directions uniform on the
-             sphere, in 64 batches of log-uniform size [16K, 1M] traced by
-             one launch: 8-wide quantised vs plain FP32, closest and any-hit
-  batch      256 meshes (displaced icospheres and soups, 1K-200K triangles
-             each, log-uniform, seeds 4000+i) with one square primary-ray
-             tile each (side log-uniform in [64, 512]): built and traced by
-             one CUDA-graph launch with the autotuned sort digit width, BVH
-             width and block shape, against 256 separate build+trace calls
-  roofline   the dominant kernel (the 8-wide trace): bytes it requested
-             (counted by the kernel: node loads, triangle loads, ray records
-             and outputs) / kernel time, against the measured HBM bandwidth
-  cpu_baseline  the CPU implementation (the reference's own code where it
-             builds, else the oracle's restatement) on a bounded sample
+  value        Mrays/s of the whole step: rays / (build + collapse + trace)
+  e2e          the same step through the C ABI with pinned host buffers:
+               triangle upload, build, trace, hit + heatmap download inside
+  plain_fp32   the same rays on the same tree traced as the plain FP32
+               binary BVH (both ray schedules), hit ids and t compared
+  stress       8,000,000-triangle soup (256 clusters, seed 5), 2^24 rays with
+               origins uniform in the scene box and directions uniform on the
+               sphere, in 64 batches of log-uniform size [16K, 1M], each in a
+               buffer of its own, traced by one batched launch
+               (sq_trace_batches) on the 8-wide BVH; against the plain FP32
+               binary BVH with its default 32-ray warp batches and with the
+               same per-lane refill schedule; closest and any-hit
+  icosphere    81,920-triangle displaced icosphere: SAH build at 16 bins,
+               leaf <= 4, 8-wide collapse, 1920x1080 closest hit, wide vs FP32
+  terrain      2048x1024-quad height field (4,194,304 triangles): Morton +
+               8-wide build, 1920x1080 primary rays and one cosine-weighted
+               bounce per hit, wide vs FP32
+  batch        256 meshes (displaced icospheres and soups, 1K-200K triangles
+               each, log-uniform, seeds 4000+i) with one square primary-ray
+               tile each (side log-uniform in [64, 512]): built and traced by
+               one CUDA-graph launch with the autotuned builder settings, BVH
+               width and block shape, against 256 separate build+trace calls
+  builders     device build time of every builder on the three scenes
+  coherent     trace() / trace_packet<8> / trace_bundle<64> heatmaps on the
+               8-bin SAH tree, the reference camera at 1920x1080
+  roofline     the dominant kernel (the 8-wide trace): bytes it requested
+               (counted by the kernel) / kernel time, against the measured
+               HBM bandwidth; its DRAM traffic from the committed ncu capture
+               of the same kernel source, and what actually limits it
+  cpu_baseline the same step on the host's cores in full (Morton build of
+               all triangles, closest-hit trace of every ray: the oracle's C
+               restatement, OpenMP), plus the restated builders and tracers
 
-`--impl reference` times only the CPU implementation.  Multi-GPU (torchrun):
+`--impl reference` times only the CPU step.  Multi-GPU (torchrun):
 independent replicas, one per GPU; value sums all ranks' rays over the
 slowest rank.
 """
 import argparse
+import hashlib
 import json
 import os
+import re
 import statistics
 import subprocess
 import sys
@@ -45,17 +60,19 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-import numpy as np  # noqa: E402,F401
+import numpy as np  # noqa: E402
 
 METRIC = "Mrays/s traced & Mtris/s built on 1 GB300: quantized+batched vs plain FP32, same hits"
 WORKLOAD = dict(name="soup_2m", tris=2_000_000, clusters=64, seed=2, width=3840, height=2160,
                 eye=(0.0, 0.0, -40.0), target=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0), vfov=60.0)
 STRESS = dict(tris=8_000_000, clusters=256, seed=5, rays=1 << 24, batches=64)
+CONFIG = {"workload": "soup_2m: 2,000,000-triangle 64-cluster Gaussian soup, 3840x2160 pinhole primary rays "
+                      "from (0,0,-40)",
+          "builder": "Morton LBVH + 8-wide 8-bit quantised collapse", "trace": "closest hit + heatmap",
+          "tris": 2_000_000, "rays": 3840 * 2160, "l2": "flushed between steps (512 MB write)"}
 LBVH_KERNELS = 8  # scene bounds, Morton codes, 4 onesweep passes, climb (local + global phase)
-# DRAM bytes (read + write) of one k_trace8_tiles<closest> launch on this
-# workload, from the ncu capture summarised in profiles/k_trace8_tiles_soup2m.md
-TRACE8_DRAM_BYTES = 115.0e6 + 106.3e6
-TRACE8_DRAM_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch (profiles/k_trace8_tiles_soup2m.md)"
+TRACE_PROFILE = os.path.join(ROOT, "profiles", "k_trace8_tiles_soup2m.md")
+TRACE_SOURCE = os.path.join(ROOT, "sequoia_gb300", "csrc", "sq_bvh8.cu")
 
 
 def measured_peaks():
@@ -65,6 +82,30 @@ def measured_peaks():
             d = json.load(fh)
         return float(d.get("hbm_gbs", 6800.0)), "measured"
     return 6800.0, "fallback"
+
+
+def source_digest(path):
+    with open(path, "rb") as fh:
+        return hashlib.sha256(fh.read()).hexdigest()[:16]
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the 8-wide trace kernel from the committed
+    ncu summary, with the source digest of the kernel it measured.  Returns
+    (bytes or None, note): None when the kernel source changed since."""
+    try:
+        with open(TRACE_PROFILE) as fh:
+            text = fh.read()
+    except OSError:
+        return None, "no ncu summary committed"
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", text)
+    d = re.search(r"kernel_source_sha256_16:\s*([0-9a-f]{16})", text)
+    if not m or not d:
+        return None, "ncu summary has no traffic line"
+    if d.group(1) != source_digest(TRACE_SOURCE):
+        return None, "stale: the kernel source changed after the ncu capture"
+    return float(m.group(1)), "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch, same kernel source " \
+                              "(%s)" % os.path.relpath(TRACE_PROFILE, ROOT)
 
 
 class ClockSampler:
@@ -147,46 +188,30 @@ def make_scene():
     return scenes.gaussian_soup(w["tris"], w["clusters"], seed=w["seed"])
 
 
-def host_threads():
-    try:
-        return len(os.sched_getaffinity(0))
-    except AttributeError:
-        return os.cpu_count() or 1
+# ------------------------------------------------------------------ CPU legs
 
-
-def cpu_sample(tris, threads, row_step):
-    """CPU build of the whole scene and closest-hit trace of every
-    `row_step`-th image row.  Returns (build s, trace s, sampled rays, kind)."""
+def cpu_step(tris, steps, warmup):
+    """The step on the host's cores, every ray of it: the oracle's Morton
+    build of all triangles and closest-hit trace of all 3840x2160 rays with
+    the heatmap (OpenMP over every host thread).  Returns (Mrays/s, s per
+    step, threads)."""
+    import cpu_baselines as CB
     import oracle as O
-    w = WORKLOAD
+    threads = CB.host_threads()
     O.set_threads(threads)
-    t0 = time.perf_counter()
-    nodes, root, _, _ = O.build_morton(tris)
-    t1 = time.perf_counter()
-    rays = O.rays_pinhole(w["width"], w["height"], w["eye"], w["target"], w["up"], w["vfov"])
-    rays = rays.reshape(w["height"], w["width"], 8)[::row_step].reshape(-1, 8).copy()
-    t2 = time.perf_counter()
-    O.trace(nodes, root, tris, rays, 1)
-    t3 = time.perf_counter()
-    return t1 - t0, t3 - t2, len(rays), "port"
-
-
-def cpu_line(tris, steps, warmup):
-    w = WORKLOAD
-    rays_total = w["width"] * w["height"]
-    threads = host_threads()
-    row_step = 16
     times = []
     for i in range(warmup + steps):
-        tb, tt, ns, _ = cpu_sample(tris, threads, row_step)
+        tb, tt, nrays = CB.port_step(tris, WORKLOAD)
         if i >= warmup:
-            times.append(tb + tt * (rays_total / ns))
+            times.append(tb + tt)
     step_s = statistics.mean(times)
-    value = rays_total / step_s / 1e6
-    sample = ("Morton build of all %d tris + closest-hit trace of every %dth image row (%d rays), extrapolated to "
-              "%d rays; the oracle's C restatement with OpenMP (the reference's own code needs x86 intrinsics)"
-              % (len(tris), row_step, rays_total // row_step, rays_total))
-    return value, step_s, threads, sample
+    return nrays / step_s / 1e6, step_s, threads
+
+
+CPU_SAMPLE = ("every step in full: Morton build of all 2,000,000 triangles and closest-hit trace of all 8,294,400 "
+              "pinhole rays with the heatmap, by the oracle's C restatement of the reference's Morton builder and "
+              "traversal (OpenMP, every host thread); the reference's own code cannot run on this host (its "
+              "sources are not here and it has no closest hit)")
 
 
 def run_reference(args):
@@ -194,57 +219,182 @@ def run_reference(args):
     if rank != 0:
         return
     tris = make_scene()
-    value, step_s, threads, sample = cpu_line(tris, args.steps, args.warmup)
+    value, step_s, threads = cpu_step(tris, args.steps, args.warmup)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": "soup_2m: 2M-triangle Gaussian soup, 3840x2160 pinhole primary rays",
-                       "builder": "morton", "trace": "closest"},
-            "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port", "sample": sample},
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded 64-cluster Gaussian triangle soup (no dataset ships with the reference)",
+            "config": dict(CONFIG, parallelism="replicas" if args.gpus > 1 else "1 GPU"),
+            "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                             "sample": CPU_SAMPLE},
             "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
+def cpu_tables(scenes_by_name):
+    """The oracle's restated builders and tracers timed on this host (ms)."""
+    import cpu_baselines as CB
+    out = {"threads": CB.host_threads(), "kind": "port", "builders": {}, "tracers": {}}
+    for name in ("icosphere_l6", "soup_2m"):
+        tris = scenes_by_name[name]
+        out["builders"][name] = CB.port_builders(tris, reps=2, which=("sah8", "sah16_leaf4", "sah32", "grid",
+                                                                     "morton", "morton60"))
+        out["tracers"][name] = CB.port_tracers(tris, reps=2)
+    return out
+
+
+# ------------------------------------------------------------------ GPU legs
+
+def best_trace_ms(ctx, flush, fn, reps=3):
+    best = None
+    for _ in range(reps):
+        flush.zero_()
+        fn()
+        ms = ctx.timings()["trace"]
+        best = ms if best is None else min(best, ms)
+    return best
+
+
+def plain_leg(ctx, flush, torch, d_tris, d_hits, cam, rays_total):
+    """The bench's rays on the same tree as the plain FP32 binary BVH: its
+    default schedule (32-ray warp batches) and per-lane refill, against the
+    8-wide trace; same hits."""
+    bvh = ctx.build(d_tris, "morton", wide=True)
+    d_hits2 = torch.empty_like(d_hits)
+    wide = best_trace_ms(ctx, flush, lambda: ctx.trace(bvh, "closest", hits=d_hits, **cam))
+    binary = best_trace_ms(ctx, flush, lambda: ctx.trace(bvh, "closest", hits=d_hits2, binary=True, **cam))
+    same = bool(torch.equal(d_hits.view(-1, 3)[:, :2], d_hits2.view(-1, 3)[:, :2]))
+    refill = best_trace_ms(ctx, flush, lambda: ctx.trace(bvh, "closest", hits=d_hits2, binary=True, sched="refill",
+                                                         **cam))
+    same = same and bool(torch.equal(d_hits.view(-1, 3)[:, :2], d_hits2.view(-1, 3)[:, :2]))
+    bvh.free()
+    return {"trace_ms": binary, "trace_mrays_s": rays_total / binary / 1e3, "refill_trace_ms": refill,
+            "wide_trace_ms": wide, "speedup": binary / wide, "same_hits": same}
+
+
 def stress_leg(ctx, flush, torch):
-    """8M-triangle soup, 2^24 incoherent rays in 64 batches, one launch per
-    form: 8-wide quantised vs plain FP32 binary, closest and any-hit."""
+    """8M-triangle soup, 2^24 incoherent rays in 64 batches with buffers of
+    their own, one batched launch (sq_trace_batches) on the 8-wide BVH,
+    against the plain FP32 binary BVH: closest and any-hit."""
     from sequoia_gb300 import scenes
     s = STRESS
     tris = scenes.gaussian_soup(s["tris"], s["clusters"], seed=s["seed"])
     lo, hi = scenes.scene_box(tris)
     sizes = scenes.batch_sizes(s["rays"], s["batches"], seed=s["seed"])
     rays = torch.from_numpy(scenes.random_rays(int(sizes.sum()), lo, hi, seed=s["seed"])).cuda()
+    cuts = np.concatenate([[0], np.cumsum(sizes)])
+    batches = [rays[cuts[k]:cuts[k + 1]].clone() for k in range(len(sizes))]
+    del rays
     d_tris = torch.from_numpy(tris).cuda()
-    h_a = torch.empty(s["rays"] * 3, dtype=torch.int32, device="cuda")
-    h_b = torch.empty_like(h_a)
+    h_wide = torch.empty(s["rays"] * 3, dtype=torch.int32, device="cuda")
+    h_bin = torch.empty_like(h_wide)
+    flush.zero_()
     bvh = ctx.build(d_tris, "morton", wide=True)
     out = {"tris": len(tris), "rays": int(sizes.sum()), "batches": len(sizes),
            "batch_sizes_min_max": [int(sizes.min()), int(sizes.max())], "build_ms": ctx.timings()["build"]}
     for mode in ("closest", "anyhit"):
-        t = {}
-        for form in ("binary", "wide"):
-            best = None
-            for _ in range(2):
-                flush.zero_()
-                ctx.trace(bvh, mode, rays=rays, hits=h_b if form == "binary" else h_a, binary=(form == "binary"))
-                ms = ctx.timings()["trace"]
-                best = ms if best is None else min(best, ms)
-            t[form] = best
-        a = h_a.view(-1, 3)
-        b = h_b.view(-1, 3)
-        if mode == "closest":
-            same = bool(torch.equal(a[:, :2], b[:, :2]))
-        else:
-            same = bool(torch.equal(a[:, 0] != -1, b[:, 0] != -1))
-        out[mode] = {"wide_mrays_s": s["rays"] / t["wide"] / 1e3, "plain_fp32_mrays_s": s["rays"] / t["binary"] / 1e3,
-                     "speedup": t["binary"] / t["wide"], "same_hits": same}
+        t = {"wide_batched": best_trace_ms(ctx, flush, lambda: ctx.trace_batches(bvh, mode, batches, hits=h_wide), 2)}
+        a = h_wide.view(-1, 3).clone()
+        same = True
+        for key, sched in (("binary", "tiles"), ("binary_refill", "refill")):
+            t[key] = best_trace_ms(ctx, flush, lambda: ctx.trace_batches(bvh, mode, batches, hits=h_bin, binary=True,
+                                                                         sched=sched), 2)
+            b = h_bin.view(-1, 3)
+            if mode == "closest":
+                same = same and bool(torch.equal(a[:, :2], b[:, :2]))
+            else:
+                same = same and bool(torch.equal(a[:, 0] != -1, b[:, 0] != -1))
+        n = s["rays"]
+        out[mode] = {"wide_mrays_s": n / t["wide_batched"] / 1e3,
+                     "plain_fp32_mrays_s": n / t["binary"] / 1e3,
+                     "plain_fp32_refill_mrays_s": n / t["binary_refill"] / 1e3,
+                     "speedup": t["binary"] / t["wide_batched"],
+                     "speedup_same_schedule": t["binary_refill"] / t["wide_batched"],
+                     "ms": t, "same_hits": same}
     bvh.free()
     return out
 
 
-def batch_leg(ctx, flush, torch, sq):
+def icosphere_leg(ctx, flush, torch):
+    """81,920-triangle icosphere: SAH-16 leaf-4 build + 8-wide collapse,
+    1920x1080 closest hit with heatmap, wide vs FP32 binary."""
+    from sequoia_gb300 import scenes
+    cfg = scenes.CONFIGS["icosphere_l6"]
+    d_tris = torch.from_numpy(scenes.displaced_icosphere(6, seed=1)).cuda()
+    n = len(d_tris)
+    cam = dict(camera="pinhole", width=cfg["width"], height=cfg["height"], origin=cfg["eye"], target=cfg["target"],
+               up=cfg["up"], vfov=cfg["vfov"])
+    rays = cfg["width"] * cfg["height"]
+    d_hits = torch.empty(rays * 3, dtype=torch.int32, device="cuda")
+    d_heat = torch.empty(rays * 3, dtype=torch.uint8, device="cuda")
+    builds = []
+    for _ in range(3):
+        flush.zero_()
+        bvh = ctx.build(d_tris, "sah", bins=16, leaf=4, wide=True)
+        builds.append(ctx.timings()["build"])
+        bvh.free()
+    bvh = ctx.build(d_tris, "sah", bins=16, leaf=4, wide=True)
+    wide = best_trace_ms(ctx, flush, lambda: ctx.trace(bvh, "closest", hits=d_hits, heatmap=d_heat, **cam))
+    d_hits2 = torch.empty_like(d_hits)
+    binary = best_trace_ms(ctx, flush, lambda: ctx.trace(bvh, "closest", hits=d_hits2, heatmap=d_heat, binary=True,
+                                                         **cam))
+    same = bool(torch.equal(d_hits.view(-1, 3)[:, :2], d_hits2.view(-1, 3)[:, :2]))
+    bvh.free()
+    b = min(builds)
+    return {"tris": n, "rays": rays, "build": "SAH 16 bins, leaf <= 4, + 8-wide collapse", "build_ms": b,
+            "build_mtris_s": n / b / 1e3, "wide_trace_ms": wide, "wide_mrays_s": rays / wide / 1e3,
+            "plain_fp32_trace_ms": binary, "plain_fp32_mrays_s": rays / binary / 1e3, "speedup": binary / wide,
+            "same_hits": same}
+
+
+def terrain_leg(ctx, flush, torch):
+    """4,194,304-triangle terrain: Morton + 8-wide build, 1920x1080 primary
+    rays and one cosine-weighted bounce per hit, wide vs FP32 binary."""
+    from sequoia_gb300 import scenes
+    cfg = scenes.CONFIGS["terrain_4m"]
+    tris = scenes.heightfield(2048, 1024, seed=3)
+    d_tris = torch.from_numpy(tris).cuda()
+    n = len(tris)
+    cam = dict(camera="pinhole", width=cfg["width"], height=cfg["height"], origin=cfg["eye"], target=cfg["target"],
+               up=cfg["up"], vfov=cfg["vfov"])
+    rays = cfg["width"] * cfg["height"]
+    builds = []
+    for _ in range(3):
+        flush.zero_()
+        bvh = ctx.build(d_tris, "morton", wide=True)
+        builds.append(ctx.timings()["build"])
+        bvh.free()
+    bvh = ctx.build(d_tris, "morton", wide=True)
+    h_wide = torch.empty(rays * 3, dtype=torch.int32, device="cuda")
+    h_bin = torch.empty_like(h_wide)
+    pw = best_trace_ms(ctx, flush, lambda: ctx.trace(bvh, "closest", hits=h_wide, **cam))
+    pb = best_trace_ms(ctx, flush, lambda: ctx.trace(bvh, "closest", hits=h_bin, binary=True, **cam))
+    same = bool(torch.equal(h_wide.view(-1, 3)[:, :2], h_bin.view(-1, 3)[:, :2]))
+    # bounce rays from the primary hits (generated on the host, before timing)
+    hits = h_bin.view(-1, 3).cpu().numpy()
+    ids, ts = hits[:, 0].view(np.uint32), hits[:, 1].view(np.float32)
+    prim = scenes.pinhole_rays(cfg["width"], cfg["height"], cfg["eye"], cfg["target"], cfg["up"], cfg["vfov"])
+    br, _ = scenes.bounce_rays(tris, prim, ids, ts, seed=3)
+    d_br = torch.from_numpy(br).cuda()
+    b_wide = torch.empty(len(br) * 3, dtype=torch.int32, device="cuda")
+    b_bin = torch.empty_like(b_wide)
+    bw = best_trace_ms(ctx, flush, lambda: ctx.trace(bvh, "closest", rays=d_br, hits=b_wide))
+    bb = best_trace_ms(ctx, flush, lambda: ctx.trace(bvh, "closest", rays=d_br, hits=b_bin, binary=True))
+    same = same and bool(torch.equal(b_wide.view(-1, 3)[:, :2], b_bin.view(-1, 3)[:, :2]))
+    bb_refill = best_trace_ms(ctx, flush, lambda: ctx.trace(bvh, "closest", rays=d_br, hits=b_bin, binary=True,
+                                                            sched="refill"))
+    bvh.free()
+    b = min(builds)
+    return {"tris": n, "primary_rays": rays, "bounce_rays": len(br), "build_ms": b, "build_mtris_s": n / b / 1e3,
+            "primary": {"wide_ms": pw, "plain_fp32_ms": pb, "wide_mrays_s": rays / pw / 1e3, "speedup": pb / pw},
+            "bounce": {"wide_ms": bw, "plain_fp32_ms": bb, "plain_fp32_refill_ms": bb_refill,
+                       "wide_mrays_s": len(br) / bw / 1e3, "speedup": bb / bw},
+            "same_hits": same}
+
+
+def batch_leg(ctx, flush, torch):
     """256 meshes with one ray tile each: one graph launch (autotuned) vs 256
-    separate plain build + trace calls, same hits."""
+    separate plain build + trace calls, same hits; Morton and SAH batches."""
     from sequoia_gb300 import scenes
     meshes, tiles = scenes.mesh_batch(256, seed=4000)
     d_meshes = [torch.from_numpy(m).cuda() for m in meshes]
@@ -258,52 +408,102 @@ def batch_leg(ctx, flush, torch, sq):
                           target=tuple(float(x) for x in c), up=(0.0, 1.0, 0.0), vfov=50.0))
     n_tris = sum(len(m) for m in meshes)
     n_rays = sum(int(t) * int(t) for t in tiles)
-    b = ctx.batch(descs, mode="closest", wide=True, graph=True)
-    best, tune_ms = b.autotune()
-    for _ in range(3):
-        b.run(hits=False)
-    times = []
     stream = torch.cuda.current_stream()
-    for _ in range(5):
-        flush.zero_()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        b.run(hits=False)
-        e1.record(stream)
-        e1.synchronize()
-        times.append(e0.elapsed_time(e1))
-    got, _ = b.run()
-    b.free()
-    # 256 separate plain (binary FP32, default digits) build + trace calls
     d_hits = torch.empty(n_rays * 3, dtype=torch.int32, device="cuda")
-    def separate():
-        off = 0
-        for d in descs:
-            bvh = ctx.build(d["tris"], "morton")
-            cnt = d["width"] * d["height"]
-            ctx.trace(bvh, "closest", hits=d_hits[3 * off:3 * (off + cnt)], camera="pinhole", width=d["width"],
-                      height=d["height"], origin=d["origin"], target=d["target"], up=d["up"], vfov=d["vfov"])
-            bvh.free()
-            off += cnt
-    separate()
-    sep = []
-    for _ in range(3):
-        flush.zero_()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
+    out = {"meshes": len(meshes), "tris": n_tris, "rays": n_rays}
+    for builder in ("morton", "sah"):
+        b = ctx.batch(descs, mode="closest", wide=True, graph=True, builder=builder)
+        best, _ = b.autotune()
+        for _ in range(3):
+            b.run(hits=False)
+        times = []
+        for _ in range(5):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            b.run(hits=False)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        got, _ = b.run()
+        b.free()
+
+        def separate():
+            off = 0
+            for d in descs:
+                kw = dict(bins=best.get("sah_bins", 8), leaf=8) if builder == "sah" else {}
+                bvh = ctx.build(d["tris"], builder, **kw)
+                cnt = d["width"] * d["height"]
+                ctx.trace(bvh, "closest", hits=d_hits[3 * off:3 * (off + cnt)], camera="pinhole", width=d["width"],
+                          height=d["height"], origin=d["origin"], target=d["target"], up=d["up"], vfov=d["vfov"])
+                bvh.free()
+                off += cnt
         separate()
-        e1.record(stream)
-        e1.synchronize()
-        sep.append(e0.elapsed_time(e1))
-    ref = d_hits.view(-1, 3).cpu().numpy()
-    same = bool(np.array_equal(got["id"], ref[:, 0].view(np.uint32)) and np.array_equal(got["t"], ref[:, 1].view(np.float32)))
-    ms, sms = min(times), min(sep)
-    return {"meshes": len(meshes), "tris": n_tris, "rays": n_rays, "autotuned": best,
-            "graph_ms": ms, "graph_mrays_s": n_rays / ms / 1e3, "graph_mtris_s": n_tris / ms / 1e3,
-            "separate_launches_ms": sms, "separate_mrays_s": n_rays / sms / 1e3, "speedup": sms / ms,
-            "same_hits": same}
+        sep = []
+        for _ in range(3):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            separate()
+            e1.record(stream)
+            e1.synchronize()
+            sep.append(e0.elapsed_time(e1))
+        ref = d_hits.view(-1, 3).cpu().numpy()
+        same = bool(np.array_equal(got["id"], ref[:, 0].view(np.uint32)) and
+                    np.array_equal(got["t"], ref[:, 1].view(np.float32)))
+        ms, sms = min(times), min(sep)
+        out[builder] = {"autotuned": best, "graph_ms": ms, "graph_mrays_s": n_rays / ms / 1e3,
+                        "graph_mtris_s": n_tris / ms / 1e3, "separate_launches_ms": sms,
+                        "separate_mrays_s": n_rays / sms / 1e3, "speedup": sms / ms, "same_hits": same}
+    return out
+
+
+def builders_leg(ctx, flush, torch, scenes_by_name):
+    """Device build time (ms, best of 3, L2 flushed) of every builder."""
+    kinds = {"morton": dict(builder="morton"), "morton_wide8": dict(builder="morton", wide=True),
+             "morton60": dict(builder="morton", morton64=True), "sah8": dict(builder="sah", bins=8, leaf=8),
+             "sah16_leaf4": dict(builder="sah", bins=16, leaf=4), "sah32": dict(builder="sah", bins=32, leaf=8),
+             "grid": dict(builder="grid", bins=8, leaf=8)}
+    out = {}
+    for name, tris in scenes_by_name.items():
+        d_tris = torch.from_numpy(tris).cuda()
+        row = {"tris": len(tris)}
+        for k, kw in kinds.items():
+            best = None
+            for _ in range(3):
+                flush.zero_()
+                bvh = ctx.build(d_tris, **kw)
+                ms = ctx.timings()["build"]
+                bvh.free()
+                best = ms if best is None else min(best, ms)
+            row[k] = best
+        out[name] = row
+        del d_tris
+    return out
+
+
+def coherent_leg(ctx, flush, torch, scenes_by_name):
+    """trace() (REF mode), trace_packet<8>, trace_bundle<64> heatmaps on the
+    8-bin SAH tree, the reference camera at 1920x1080 (ms, best of 3)."""
+    w, h = 1920, 1080
+    out = {}
+    heat = torch.empty(w * h * 3, dtype=torch.uint8, device="cuda")
+    for name in ("icosphere_l6", "soup_2m"):
+        tris = scenes_by_name[name]
+        v = tris.reshape(-1, 3)
+        lo, hi = v.min(0), v.max(0)
+        c = (lo + hi) * np.float32(0.5)
+        cam = (float(c[0]), float(c[1]), float(np.float32(2) * lo[2] - c[2]))
+        bvh = ctx.build(torch.from_numpy(tris).cuda(), "sah", bins=8, leaf=8)
+        kw = dict(camera="reference", width=w, height=h, origin=cam)
+        out[name] = {
+            "trace": best_trace_ms(ctx, flush, lambda: ctx.trace(bvh, "ref", hits=False, heatmap=heat, **kw)),
+            "packet8": best_trace_ms(ctx, flush, lambda: ctx.trace(bvh, "packet", k=8, heatmap=heat, **kw)),
+            "bundle64": best_trace_ms(ctx, flush, lambda: ctx.trace(bvh, "bundle", k=64, heatmap=heat, **kw))}
+        bvh.free()
+    return out
 
 
 def main():
@@ -407,25 +607,20 @@ def main():
     e2e_total = reduce_max(sum(e2e_ms) if e2e_ms else float("nan"), dist)
     e2e_value = whole_job_value(rays_total, args.steps, world, e2e_total)
 
-    plain = stress = batch = None
+    extra = {}
+    scenes_by_name = None
+    if not args.no_extra or not args.no_cpu_baseline:
+        from sequoia_gb300 import scenes
+        scenes_by_name = {"icosphere_l6": scenes.displaced_icosphere(6, seed=1), "soup_2m": tris,
+                          "terrain_4m": scenes.heightfield(2048, 1024, seed=3)}
     if not args.no_extra:
-        # plain FP32 binary traversal of the same tree, same rays; same hits?
-        bvh = ctx.build(d_tris, "morton", wide=True)
-        d_hits2 = torch.empty_like(d_hits)
-        times = {"wide": [], "binary": []}
-        for _ in range(3):
-            for form in ("binary", "wide"):
-                flush.zero_()
-                ctx.trace(bvh, "closest", hits=d_hits if form == "wide" else d_hits2, binary=(form == "binary"), **cam)
-                times[form].append(ctx.timings()["trace"])
-        same = bool(torch.equal(d_hits.view(-1, 3)[:, :2], d_hits2.view(-1, 3)[:, :2]))
-        bvh.free()
-        plain = {"trace_ms": min(times["binary"]), "trace_mrays_s": rays_total / min(times["binary"]) / 1e3,
-                 "wide_trace_ms": min(times["wide"]), "speedup": min(times["binary"]) / min(times["wide"]),
-                 "same_hits": same}
-        del d_hits2
-        stress = stress_leg(ctx, flush, torch)
-        batch = batch_leg(ctx, flush, torch, sq)
+        extra["plain_fp32"] = plain_leg(ctx, flush, torch, d_tris, d_hits, cam, rays_total)
+        extra["stress"] = stress_leg(ctx, flush, torch)
+        extra["icosphere"] = icosphere_leg(ctx, flush, torch)
+        extra["terrain"] = terrain_leg(ctx, flush, torch)
+        extra["batch"] = batch_leg(ctx, flush, torch)
+        extra["builders_ms"] = builders_leg(ctx, flush, torch, scenes_by_name)
+        extra["coherent_ms"] = coherent_leg(ctx, flush, torch, scenes_by_name)
 
     if rank != 0:
         if dist:
@@ -440,22 +635,20 @@ def main():
     lbvh_ms = b_ms - statistics.mean(wide_ms)
     build_gbs = n * (200 + 16 * 4) / (lbvh_ms / 1e3) / 1e9
     hits_np = d_hits.view(-1, 3).cpu().numpy()
+    traffic, traffic_note = profiled_traffic()
 
     cpu = None
     if not args.no_cpu_baseline:
-        value_c, _, threads, sample = cpu_line(tris, 1, 0)
-        cpu = {"value": value_c, "unit": "Mrays/s", "cores": threads, "kind": "port", "sample": sample}
+        value_c, step_s, threads = cpu_step(tris, 1, 0)
+        cpu = {"value": value_c, "unit": "Mrays/s", "cores": threads, "kind": "port", "sample": CPU_SAMPLE,
+               "ms_per_step": step_s * 1e3, "tables_ms": cpu_tables(scenes_by_name)}
 
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
         "data": "synthetic: seeded 64-cluster Gaussian triangle soup (no dataset ships with the reference)",
-        "config": {"workload": "soup_2m: %d-triangle Gaussian soup, %dx%d pinhole primary rays from (0,0,-40)"
-                               % (n, w["width"], w["height"]),
-                   "builder": "Morton LBVH + 8-wide 8-bit quantised collapse", "trace": "closest hit + heatmap",
-                   "tris": n, "rays": rays_total, "l2": "flushed between steps (512 MB write)",
-                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "config": dict(CONFIG, parallelism="replicas" if world > 1 else "1 GPU"),
         "build_mtris_s": n / (b_ms / 1e3) / 1e6,
         "lbvh_mtris_s": n / (lbvh_ms / 1e3) / 1e6,
         "trace_mrays_s": rays_total / (tr_ms / 1e3) / 1e6,
@@ -467,22 +660,23 @@ def main():
                     "wide_nodes": statistics.mean(s["nodes"] for s in stats) / rays_total,
                     "requested_bytes": req_bytes / rays_total},
         "hit_rays": int((hits_np[:, 0] != -1).sum()),
-        "roofline": {"bound": "hbm", "kernel": "k_trace8<closest>", "achieved": achieved, "peak": peak,
+        "roofline": {"bound": "hbm", "kernel": "k_trace8_tiles<closest>", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-                     "traffic": TRACE8_DRAM_BYTES, "traffic_source": TRACE8_DRAM_SOURCE,
+                     "traffic": traffic, "traffic_source": traffic_note,
+                     "dram_frac": (traffic / (tr_ms / 1e3) / 1e9 / peak) if traffic else None,
                      "bytes_model": "kernel-counted requested bytes: 80 B per wide node loaded, 48 B per "
-                                    "triangle tested, 15 B of outputs per ray"},
+                                    "triangle tested, 15 B of outputs per ray",
+                     "limiter": "instruction issue (ALU pipe), not HBM: the tree stays in L2 and L1, so DRAM "
+                                "moves ~2% of the requested bytes; issue-slot and pipe figures in the ncu summary"},
         "build_roofline": {"bound": "hbm", "achieved": build_gbs, "peak": peak, "unit": "GB/s",
                            "frac": build_gbs / peak, "bytes_model": "264 B/tri (200 + 16 x 4 sort passes)"},
-        "plain_fp32": plain,
-        "stress": stress,
-        "batch": batch,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": n * 36,
                 "d2h_bytes_per_step": rays_total * 15, "ms_per_step": e2e_total / args.steps},
         "gpu_launches": launches,
         "clocks": clk,
     }
+    line.update(extra)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -168,6 +168,22 @@ typedef enum sq_trace_mode {
 /* OR into the mode: trace the binary (Node1) tree even when the BVH also has
  * an 8-wide quantised tree.                                                  */
 #define SQ_TRACE_FORCE_BINARY 0x100u
+/* OR into a CLOSEST or ANYHIT mode to choose how rays are assigned to GPU
+ * lanes (the results are the same either way; only the speed differs):
+ *   SQ_TRACE_SCHED_REFILL  a lane whose ray has finished takes the next ray
+ *                          at once (best for incoherent rays);
+ *   SQ_TRACE_SCHED_TILES   a warp traces 32 rays (an 8x4 pixel tile, or 32
+ *                          consecutive explicit rays) to the end, then takes
+ *                          the next 32 (best for coherent camera rays).
+ * Without either: the binary tree uses TILES; the 8-wide tree uses REFILL
+ * for explicit rays and TILES for camera rays.                               */
+#define SQ_TRACE_SCHED_REFILL 0x200u
+#define SQ_TRACE_SCHED_TILES 0x400u
+/* OR into any mode: heatmap pixels in the reference's colour ramp
+ * get_heatmap_colour (src/tracer.cpp:25-45, defined there but unused) of
+ * tests / 200 -- black, blue, cyan, green, yellow, red -- each channel
+ * (uint8)(c * 255), instead of the grey (uint8)(min(1, tests / 200) * 255). */
+#define SQ_TRACE_HEAT_RAMP 0x800u
 
 typedef enum sq_ray_kind {
     SQ_RAYS_REFERENCE_CAMERA = 0, /* trace()'s camera (src/tracer.cpp:202-216)   */
@@ -191,6 +207,8 @@ typedef struct sq_ray_source {
 
 /* No reference counterpart: the reference is a global OpenMP program.       */
 sq_status sq_create(sq_ctx** out, const sq_options* options);
+/* Releases all device memory the context holds, that of its BVHs and
+ * batches included: free those first; none may be used or freed after.     */
 sq_status sq_destroy(sq_ctx* ctx);
 const char* sq_last_error(const sq_ctx* ctx);
 uint32_t sq_abi_version(void);
@@ -289,6 +307,29 @@ sq_status sq_radix_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* v
 sq_status sq_trace(sq_ctx* ctx, const sq_bvh* bvh, const sq_ray_source* rays,
                    uint32_t mode, sq_hit* hits, uint8_t* heatmap_rgb);
 
+/* traverse() (src/tracer.h:118, src/tracer.cpp:47-65) for n explicit rays
+ * (host or device): the reference's traversal -- every box of the node
+ * group [index, index + count) tested, then the groups of the inner nodes
+ * hit, no ordering, no early exit, Moller-Trumbore triangle tests -- started
+ * from that node group rather than the root.  hits[i] (host or device) gets
+ * id 0 (hit) or SQ_NO_HIT and the ray's box-test count, as SQ_TRACE_REF.
+ * Host hits are complete when the call returns.                             */
+sq_status sq_traverse(sq_ctx* ctx, const sq_bvh* bvh, uint32_t index, uint32_t count, const sq_ray* rays,
+                      uint32_t n, sq_hit* hits);
+
+/* Many ray batches against one BVH in one kernel launch.  No reference
+ * counterpart (the reference traces one image per call, src/tracer.cpp:195).
+ * Each of the `count` batches is a ray source of its own: explicit rays in
+ * their own buffer (device buffers are read in place, others are copied
+ * first) or a camera.  hits / heatmap_rgb (optional, host or device) receive
+ * the results batch after batch, exactly as `count` sq_trace calls would
+ * write them; one launch traces all batches, its warps taking 32-ray pieces
+ * of any batch.  mode: SQ_TRACE_REF, CLOSEST or ANYHIT, with
+ * SQ_TRACE_FORCE_BINARY and the schedule flags (default: per-lane refill
+ * when most rays are explicit).                                              */
+sq_status sq_trace_batches(sq_ctx* ctx, const sq_bvh* bvh, const sq_ray_source* batches, uint32_t count,
+                           uint32_t mode, sq_hit* hits, uint8_t* heatmap_rgb);
+
 /* ---- batches: many meshes and ray tiles, one launch sequence ------------ */
 
 /* Build-and-trace of many independent meshes at once: the reference's
@@ -353,6 +394,39 @@ sq_status sq_last_timings(sq_ctx* ctx, float stage_ms[8]);
  * No reference counterpart (the reference keeps only the per-ray count,
  * src/tracer.h:32).                                                          */
 sq_status sq_last_trace_stats(sq_ctx* ctx, uint64_t stats[4]);
+
+/* ---- failure-detection test hooks ---------------------------------------- */
+
+/* Fault injection for the failure-detection tests; no reference counterpart
+ * (the reference asserts or exits on failure).  Each injection is armed for
+ * one use on this context, then clears itself:
+ *   SQ_DEBUG_STALL_LOOKBACK  the next sq_radix_sort_pairs, which must be a
+ *                            one-pass sort (key_bits <= digit_bits) of more
+ *                            than 4096 keys, runs without its first tile: the
+ *                            look-back of the tiles after it waits on words
+ *                            that nothing publishes, gives up after `limit`
+ *                            polls and raises SQ_DEVERR_LOOKBACK_TIMEOUT.
+ *   SQ_DEBUG_STALL_BARRIER   the next 8-wide collapse's grid barrier waits
+ *                            for one block more than the grid: every block
+ *                            gives up after `limit` polls and raises
+ *                            SQ_DEVERR_SAH_QUEUE.
+ *   SQ_DEBUG_FAIL_ALLOC      device allocation number `limit` from now (0 =
+ *                            the next one) fails as if the GPU were out of
+ *                            memory; the call reports SQ_ERR_OOM.
+ *   SQ_DEBUG_OFF             disarm all of them.
+ * No injection faults or hangs the GPU: a wait that gives up returns, the
+ * kernel finishes, and the context stays usable (the error word is reported
+ * and cleared by the next sq_sync).  The results of the call that carried
+ * the injection are not valid.                                               */
+#define SQ_DEBUG_OFF 0u
+#define SQ_DEBUG_STALL_LOOKBACK 1u
+#define SQ_DEBUG_STALL_BARRIER 2u
+#define SQ_DEBUG_FAIL_ALLOC 3u
+sq_status sq_debug_inject(sq_ctx* ctx, uint32_t what, uint32_t limit);
+/* Device memory the context holds in its caching allocator: out[0] / out[1]
+ * = blocks / bytes held by live objects (BVHs, batches, buffers of a call in
+ * flight), out[2] / out[3] = blocks / bytes cached for reuse.               */
+sq_status sq_debug_memory(const sq_ctx* ctx, uint64_t out[4]);
 
 #ifdef __cplusplus
 }

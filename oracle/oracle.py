@@ -66,6 +66,8 @@ def _declare(L):
         "sqo_trace": (i32, [vp, u32, vp, vp, u32, i32, vp, vp, vp]),
         "sqo_brute_closest": (None, [vp, u32, vp, u32, vp, vp]),
         "sqo_heatmap": (None, [vp, u32, vp]),
+        "sqo_heatmap_colour": (None, [f32, vp]),
+        "sqo_heatmap_ramp": (None, [vp, u32, vp]),
         "sqo_trace_coherent": (i32, [vp, u32, u32, u32, vp, i32, u32, vp]),
         "sqo_reintersect_f64": (None, [vp, vp, u32, vp, vp]),
         "sqo_canonical_bfs": (u32, [vp, u32, u32, vp, u32]),
@@ -231,6 +233,23 @@ def heatmap(tests):
     return rgb
 
 
+def heatmap_colour(xs):
+    """get_heatmap_colour (src/tracer.cpp:25-45) of each x: float32 (n, 3)."""
+    xs = np.ascontiguousarray(xs, np.float32).ravel()
+    out = np.empty((len(xs), 3), np.float32)
+    for i, x in enumerate(xs):
+        lib().sqo_heatmap_colour(float(x), _p(out[i]))
+    return out
+
+
+def heatmap_ramp(values):
+    """Colour-ramp heatmap bytes (n * 3) of box-test values (counts)."""
+    v = np.ascontiguousarray(values, np.float32)
+    rgb = np.empty(len(v) * 3, np.uint8)
+    lib().sqo_heatmap_ramp(_p(v), len(v), _p(rgb))
+    return rgb
+
+
 def trace_coherent(nodes, root, w, h, origin, bundle, k):
     """trace_packet<k> / trace_bundle<k> heatmap bytes (w*h*3)."""
     o = np.asarray(origin, np.float32)
@@ -299,6 +318,7 @@ def ref(variant="b8"):
         L.ref_radix_sort64.argtypes = [vp, vp, u32]
         L.ref_find_split_morton2.argtypes = [vp, u32]
         L.ref_find_split_morton2.restype = u32
+        L.ref_heatmap_colour.argtypes = [vp, u32, vp]
         _refs[variant] = L
     return _refs[variant]
 
@@ -374,6 +394,14 @@ def ref_traverse(nodes, root, tris, rays, variant="b8"):
     ref(variant).ref_traverse(_p(nodes), len(nodes), root, _p(tris), len(tris), _p(rays), len(rays),
                               _p(hit), _p(tests))
     return hit, tests
+
+
+def ref_heatmap_colour(xs, variant="b8"):
+    """The reference's own get_heatmap_colour of each x: float32 (n, 3)."""
+    xs = np.ascontiguousarray(xs, np.float32).ravel()
+    out = np.empty((len(xs), 3), np.float32)
+    ref(variant).ref_heatmap_colour(_p(xs), len(xs), _p(out))
+    return out
 
 
 def ref_write_bmp(path, w, h, rgb, variant="b8"):

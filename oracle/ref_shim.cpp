@@ -42,6 +42,7 @@ unsigned find_split_morton(std::vector<RadixInput32>::iterator begin, std::vecto
 void setup_morton2(std::vector<Triangle>& primitives, std::vector<RadixInput64>& morton_codes, AABB1& scene_aabb);
 unsigned find_split_morton2(std::vector<RadixInput64>::iterator begin, std::vector<RadixInput64>::iterator end);
 std::vector<Triangle> loadOBJFromFile(std::string filename);
+vec3f1 get_heatmap_colour(float normalised);  // src/tracer.cpp:25-45, not declared in a header
 // stb_image_write v1.14 as compiled into the reference's main.cpp
 extern "C" int stbi_write_bmp(char const* filename, int w, int h, int comp, const void* data);
 extern "C" void stbi_flip_vertically_on_write(int flag);
@@ -287,6 +288,17 @@ uint32_t ref_load_obj(const char* path, float* out, uint32_t cap)
         p[6] = v[i].v2.x; p[7] = v[i].v2.y; p[8] = v[i].v2.z;
     }
     return (uint32_t)v.size();
+}
+
+// get_heatmap_colour (src/tracer.cpp:25-45) of each x: rgb[3 * i + k]
+void ref_heatmap_colour(const float* x, uint32_t n, float* rgb)
+{
+    for (uint32_t i = 0; i < n; ++i) {
+        const vec3f1 c = get_heatmap_colour(x[i]);
+        rgb[3 * (size_t)i] = c.x;
+        rgb[3 * (size_t)i + 1] = c.y;
+        rgb[3 * (size_t)i + 2] = c.z;
+    }
 }
 
 // The reference's image output (src/main.cpp:335-336): flip on, 24-bit BMP

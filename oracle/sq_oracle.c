@@ -1346,6 +1346,42 @@ void sqo_heatmap(const uint32_t* tests, uint32_t n, uint8_t* rgb)
     }
 }
 
+/* get_heatmap_colour (src/tracer.cpp:25-45): six stops black, blue, cyan,
+ * green, yellow, red; out-of-range values clamp to the end stops; between
+ * stops s = x * 5, i0 = floor(s), i2 = ceil(s), fract = i2 - s and the
+ * colour is col[i0] * fract + col[i2] * (1 - fract), each operation rounded
+ * once (vec3f1's component-wise * and +, src/vec3.h). */
+void sqo_heatmap_colour(float x, float rgb[3])
+{
+    static const float col[6][3] = {{0, 0, 0}, {0, 0, 1}, {0, 1, 1}, {0, 1, 0}, {1, 1, 0}, {1, 0, 0}};
+    if (x <= 0.0f) { rgb[0] = col[0][0]; rgb[1] = col[0][1]; rgb[2] = col[0][2]; return; }
+    if (x >= 1.0f) { rgb[0] = col[5][0]; rgb[1] = col[5][1]; rgb[2] = col[5][2]; return; }
+    const float s = x * 5.0f;
+    const int i0 = (int)floorf(s);
+    const int i2 = (int)ceilf(s);
+    const float fract = (float)i2 - s;
+    const float rest = 1.0f - fract;
+    for (int k = 0; k < 3; ++k) {
+        const float a = col[i0][k] * fract;
+        const float b = col[i2][k] * rest;
+        rgb[k] = a + b;
+    }
+}
+
+/* The colour-ramp heatmap of box-test values v (counts, or a packet's
+ * tests / k): get_heatmap_colour(v / 200) per pixel, each channel
+ * (uint8)(c * 255) as the grey heatmap converts (src/tracer.cpp:222-225).  A
+ * non-positive or NaN normalised value is black. */
+void sqo_heatmap_ramp(const float* values, uint32_t n, uint8_t* rgb)
+{
+    for (uint32_t i = 0; i < n; ++i) {
+        const float x = values[i] / 200.0f;
+        float c[3] = {0.0f, 0.0f, 0.0f};
+        if (x > 0.0f) sqo_heatmap_colour(x, c);
+        for (int k = 0; k < 3; ++k) rgb[3 * (size_t)i + k] = (uint8_t)f2u(c[k] * 255.0f);
+    }
+}
+
 void sqo_reintersect_f64(const float* tris, const float* rays, uint32_t nrays,
                          const uint32_t* ids, double* t64)
 {

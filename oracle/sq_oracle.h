@@ -121,6 +121,9 @@ void sqo_brute_closest(const float* tris, uint32_t n, const float* rays,
 
 /* Heatmap bytes (src/tracer.cpp:222-225): 3 bytes per ray */
 void sqo_heatmap(const uint32_t* tests, uint32_t n, uint8_t* rgb);
+/* get_heatmap_colour (src/tracer.cpp:25-45) and the colour-ramp heatmap */
+void sqo_heatmap_colour(float x, float rgb[3]);
+void sqo_heatmap_ramp(const float* values, uint32_t n, uint8_t* rgb);
 /* trace_packet<k> (bundle = 0; k = 1, 2, 4, 8) or trace_bundle<k> (bundle =
  * 1; k = 16, 64) heatmap of the reference camera at origin, w x h (w and h
  * multiples of the packet or tile size).  Returns 0, 1 on a stack overflow,

@@ -15,6 +15,7 @@ address.  Triangles are float32 (n, 9); rays float32 (n, 8)
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 import os
 
 import numpy as np
@@ -30,6 +31,7 @@ NODE1 = np.dtype([("min", "<f4", 3), ("count", "<u2"), ("flags", "<u2"), ("max",
 HIT = np.dtype([("id", "<u4"), ("t", "<f4"), ("tests", "<u4")])
 
 MODES = {"ref": 0, "closest": 1, "anyhit": 2, "packet": 3, "bundle": 4}
+SCHEDS = {None: 0, "refill": 0x200, "tiles": 0x400}
 BUILDERS = {"morton": 0, "sah": 1, "recursive": 1, "grid": 2}
 STATUS = {0: "OK", 1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "device error",
           5: "unsupported", 6: "no CUDA device", 7: "exceeds a fixed capacity"}
@@ -112,6 +114,10 @@ def load_library():
         "sq_bvh_export_sorted": (i32, [vp, vp, vp]),
         "sq_bvh_export_sorted64": (i32, [vp, vp, vp]),
         "sq_trace": (i32, [vp, vp, C.POINTER(_RaySource), u32, vp, vp]),
+        "sq_trace_batches": (i32, [vp, vp, C.POINTER(_RaySource), u32, u32, vp, vp]),
+        "sq_traverse": (i32, [vp, vp, u32, u32, vp, u32, vp]),
+        "sq_debug_inject": (i32, [vp, u32, u32]),
+        "sq_debug_memory": (i32, [vp, vp]),
         "sq_last_timings": (i32, [vp, C.POINTER(C.c_float * 8)]),
         "sq_last_trace_stats": (i32, [vp, C.POINTER(C.c_uint64 * 4)]),
         "sq_batch_create": (i32, [vp, C.POINTER(_BatchMesh), u32, C.POINTER(_BatchParams), C.POINTER(vp)]),
@@ -172,6 +178,7 @@ class Bvh:
         self.ctx = ctx
         self.handle = handle
         self._tris_ref = tris_ref  # keeps a device triangle buffer alive
+        ctx._owned.add(self)
 
     def info(self):
         info = _BvhInfo()
@@ -209,9 +216,11 @@ class Bvh:
         return codes, perm
 
     def free(self):
-        if self.handle:
+        # after the context is closed the library has released the BVH's
+        # memory; the handle must not reach sq_bvh_free then
+        if self.handle and self.ctx.handle:
             load_library().sq_bvh_free(self.handle)
-            self.handle = None
+        self.handle = None
 
     def __del__(self):
         try:
@@ -228,6 +237,7 @@ class Batch:
         self.ctx = ctx
         self.handle = handle
         self._keep = keep
+        ctx._owned.add(self)
 
     def info(self):
         i = _BatchInfo()
@@ -252,9 +262,9 @@ class Batch:
         return {"sort_digit_bits": best.sort_digit_bits, "wide": best.wide, "block_threads": best.block_threads}, ms.value
 
     def free(self):
-        if self.handle:
+        if self.handle and self.ctx.handle:
             load_library().sq_batch_free(self.handle)
-            self.handle = None
+        self.handle = None
 
     def __del__(self):
         try:
@@ -270,6 +280,8 @@ class Context:
         L = load_library()
         opt = _Options(device, stream if stream is not None else None, 1 if stream is not None else 0)
         h = C.c_void_p()
+        self.handle = None
+        self._owned = weakref.WeakSet()  # BVHs and batches made on this context
         st = L.sq_create(C.byref(h), C.byref(opt))
         if st != 0:
             raise SequoiaError(st, "sq_create failed")
@@ -281,7 +293,11 @@ class Context:
             raise SequoiaError(st, msg.decode() if msg else "")
 
     def close(self):
+        """Free every BVH and batch still open on the context, then the
+        context (sq_destroy)."""
         if getattr(self, "handle", None):
+            for obj in list(self._owned):
+                obj.free()
             load_library().sq_destroy(self.handle)
             self.handle = None
 
@@ -353,20 +369,69 @@ class Context:
         return src, width * height
 
     def trace(self, bvh, mode="closest", rays=None, camera=None, width=0, height=0, origin=(0, 0, 0),
-              target=(0, 0, -1), up=(0, 1, 0), vfov=60.0, hits=True, heatmap=False, binary=False, k=0):
+              target=(0, 0, -1), up=(0, 1, 0), vfov=60.0, hits=True, heatmap=False, binary=False, k=0,
+              sched=None, ramp=False):
         """Trace rays; returns (hits structured array or None, heatmap bytes or None).
         `hits` / `heatmap` may also be device buffers to write into.  `binary`
-        forces the binary tree when the BVH also has an 8-wide one.  Modes
-        "packet" and "bundle" (trace_packet<k> / trace_bundle<k>) take the
-        packet size `k`, the reference camera and produce the heatmap only."""
+        forces the binary tree when the BVH also has an 8-wide one.  `sched`
+        ("refill" or "tiles", closest / any-hit) chooses how rays are given
+        to GPU lanes; the results do not depend on it.  `ramp`: heatmap in
+        the reference's colour ramp instead of grey.  Modes "packet" and
+        "bundle" (trace_packet<k> / trace_bundle<k>) take the packet size
+        `k`, the reference camera and produce the heatmap only."""
         if mode in ("packet", "bundle"):
             hits, heatmap = False, (True if heatmap is False else heatmap)
         src, count = self._ray_source(rays, camera, width, height, origin, target, up, vfov)
         h_arr = np.empty(count, HIT) if hits is True else (hits if hits is not False else None)
         m_arr = np.empty(count * 3, np.uint8) if heatmap is True else (heatmap if heatmap is not False else None)
-        m = MODES[mode] | (0x100 if binary else 0) | (int(k) << 16)
+        m = MODES[mode] | (0x100 if binary else 0) | (int(k) << 16) | SCHEDS[sched] | (0x800 if ramp else 0)
         self._check(load_library().sq_trace(self.handle, bvh.handle, C.byref(src), m, _addr(h_arr), _addr(m_arr)))
         return h_arr, m_arr
+
+    def trace_batches(self, bvh, mode="closest", batches=(), hits=True, heatmap=False, binary=False, sched=None):
+        """Trace many ray batches against one BVH in one launch
+        (sq_trace_batches).  `batches`: a list whose items are explicit ray
+        arrays (numpy or device tensors, (n, 8) float32) or camera dicts
+        (`camera`, `width`, `height`, `origin`, `target`, `up`, `vfov`).
+        Returns (hits, heatmap) laid out batch after batch."""
+        arr = (_RaySource * max(1, len(batches)))()
+        total = 0
+        for k, item in enumerate(batches):
+            if isinstance(item, dict):
+                src, cnt = self._ray_source(**item)
+            else:
+                src, cnt = self._ray_source(rays=item)
+            arr[k] = src
+            total += cnt
+        h_arr = np.empty(total, HIT) if hits is True else (hits if hits is not False else None)
+        m_arr = np.empty(total * 3, np.uint8) if heatmap is True else (heatmap if heatmap is not False else None)
+        m = MODES[mode] | (0x100 if binary else 0) | SCHEDS[sched]
+        self._check(load_library().sq_trace_batches(self.handle, bvh.handle, arr, len(batches), m, _addr(h_arr),
+                                                    _addr(m_arr)))
+        return h_arr, m_arr
+
+    def traverse(self, bvh, index, count, rays, hits=True):
+        """traverse() from the node group [index, index + count) for explicit
+        rays (sq_traverse): per ray the hit flag (id 0 or NO_HIT) and the
+        box-test count."""
+        n = _len(rays, 8)
+        h_arr = np.empty(n, HIT) if hits is True else hits
+        self._check(load_library().sq_traverse(self.handle, bvh.handle, int(index), int(count), _addr(rays), n,
+                                               _addr(h_arr)))
+        return h_arr
+
+    # failure-detection test hooks (sq_debug_inject / sq_debug_memory)
+    INJECT = {"off": 0, "stall_lookback": 1, "stall_barrier": 2, "fail_alloc": 3}
+
+    def debug_inject(self, what, limit=0):
+        self._check(load_library().sq_debug_inject(self.handle, self.INJECT[what], int(limit)))
+
+    def debug_memory(self):
+        """{live_blocks, live_bytes, cached_blocks, cached_bytes} of the
+        context's device allocator."""
+        arr = (C.c_uint64 * 4)()
+        self._check(load_library().sq_debug_memory(self.handle, C.byref(arr)))
+        return {"live_blocks": arr[0], "live_bytes": arr[1], "cached_blocks": arr[2], "cached_bytes": arr[3]}
 
     def trace_stats(self):
         arr = (C.c_uint64 * 4)()

@@ -33,6 +33,7 @@ static size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 // Caching allocator: freed blocks are kept by size and reused.
 void* dalloc(sq_ctx* c, size_t bytes)
 {
+    if (c->fail_alloc_in >= 0 && c->fail_alloc_in-- == 0) return nullptr;  // injected failure
     if (bytes == 0) bytes = 256;
     const size_t sz = bytes < (1u << 20) ? round_up(bytes, 256) : round_up(bytes, 2u << 20);
     auto it = c->free_blocks.lower_bound(sz);
@@ -91,6 +92,37 @@ void* pinned_device_alias(const void* p)
         return nullptr;
     }
     return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+void camera_params(const sq_ray_source& rs, float* cam)
+{
+    if (rs.kind == SQ_RAYS_REFERENCE_CAMERA) {
+        for (int k = 0; k < 3; ++k) cam[k] = rs.origin[k];
+        return;
+    }
+    // pinhole basis in double, rounded to float: eye, forward, right, up,
+    // then the half extents of the image plane at distance 1
+    double f[3], r[3], u[3], up[3];
+    for (int k = 0; k < 3; ++k) { f[k] = (double)rs.target[k] - (double)rs.origin[k]; up[k] = rs.up[k]; }
+    const double fl = sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+    for (double& x : f) x /= fl;
+    r[0] = f[1] * up[2] - f[2] * up[1];
+    r[1] = f[2] * up[0] - f[0] * up[2];
+    r[2] = f[0] * up[1] - f[1] * up[0];
+    const double rl = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+    for (double& x : r) x /= rl;
+    u[0] = r[1] * f[2] - r[2] * f[1];
+    u[1] = r[2] * f[0] - r[0] * f[2];
+    u[2] = r[0] * f[1] - r[1] * f[0];
+    const double th = tan((double)rs.vfov_deg * 3.14159265358979323846 / 360.0);
+    for (int k = 0; k < 3; ++k) {
+        cam[k] = rs.origin[k];
+        cam[3 + k] = (float)f[k];
+        cam[6 + k] = (float)r[k];
+        cam[9 + k] = (float)u[k];
+    }
+    cam[12] = (float)(th * (double)rs.width / (double)rs.height);
+    cam[13] = (float)th;
 }
 
 sq_status check_device_error(sq_ctx* c, uint32_t* bits_out)
@@ -301,8 +333,11 @@ sq_status build_wide(sq_ctx* c, sq_bvh* b)
     if (!b->nodes8 || !b->tris8 || !b->ws8) return fail(c, SQ_ERR_OOM, "8-wide BVH allocation failed (n=%u)", n);
     b->meta8 = static_cast<uint32_t*>(dalloc(c, 2 * sizeof(uint32_t)));
     if (!b->meta8) return fail(c, SQ_ERR_OOM, "8-wide BVH allocation failed (n=%u)", n);
+    sqk::BarrierStall stall{c->stall_barrier ? c->stall_barrier - 1u : 0u};
+    const bool stalled = c->stall_barrier != 0;
+    c->stall_barrier = 0;
     const int rc = sqk::build_bvh8(b->nodes, b->root, b->leaf0, b->tris, n, b->nodes8, b->tris8, b->ws8, c->host_ctl,
-                                   c->ctrl, c->stream, b->meta8);
+                                   c->ctrl, c->stream, b->meta8, stalled ? &stall : nullptr);
     if (rc != 0) return fail(c, SQ_ERR_CUDA, "8-wide collapse: %s", cudaGetErrorString((cudaError_t)rc));
     b->launches8 = c->host_ctl[4];
     if (!c->host_ctl[5]) {
@@ -602,6 +637,13 @@ sq_status sq_radix_sort_pairs(sq_ctx* c, const uint32_t* keys_in, const uint32_t
     const size_t lb_words = sqk::sort_lookback_words(n, digit_bits, passes);
     const size_t z_hist = 0, z_ctr = passes * radix, z_lb = z_ctr + 8;
     const size_t z_words = z_lb + lb_words;
+    // an armed look-back stall applies to a one-pass sort of two tiles or
+    // more, where every scatter stays inside the output (see SortStall)
+    sqk::SortStall stall{c->stall_lookback ? c->stall_lookback - 1u : 0u};
+    const bool stalled = c->stall_lookback != 0;
+    c->stall_lookback = 0;
+    if (stalled && (passes != 1 || n <= 4096))
+        return fail(c, SQ_ERR_INVALID, "look-back stall injection needs a one-pass sort of more than 4096 keys");
     uint32_t* zero = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * z_words));
     uint32_t* buf = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * 4ull * n));
     if (!zero || !buf) { dfree(c, zero); dfree(c, buf); return fail(c, SQ_ERR_OOM, "allocation failed"); }
@@ -613,7 +655,7 @@ sq_status sq_radix_sort_pairs(sq_ctx* c, const uint32_t* keys_in, const uint32_t
     SQ_CUDA(c, cudaEventRecord(c->ev[1], s));
     sqk::sort_histogram(ka, n, zero + z_hist, digit_bits, passes, s);
     const int which = sqk::sort_passes(ka, va, kb, vb, n, zero + z_hist, zero + z_lb, zero + z_ctr, digit_bits, passes,
-                                       c->ctrl, s);
+                                       c->ctrl, s, stalled ? &stall : nullptr);
     SQ_CUDA(c, cudaEventRecord(c->ev[2], s));
     const uint32_t* rk = which ? kb : ka;
     const uint32_t* rv = which ? vb : va;
@@ -633,7 +675,11 @@ sq_status sq_trace(sq_ctx* c, const sq_bvh* b, const sq_ray_source* rays, uint32
 {
     if (!c || !b || !rays) return fail(c, SQ_ERR_INVALID, "sq_trace: null argument");
     const bool force_binary = (mode & SQ_TRACE_FORCE_BINARY) != 0;
+    const bool sched_refill = (mode & SQ_TRACE_SCHED_REFILL) != 0;
+    const bool sched_tiles = (mode & SQ_TRACE_SCHED_TILES) != 0;
+    const bool heat_ramp = (mode & SQ_TRACE_HEAT_RAMP) != 0;
     const uint32_t width_k = (mode >> 16) & 0xFFu;
+    if (sched_refill && sched_tiles) return fail(c, SQ_ERR_INVALID, "sq_trace: choose one ray schedule");
     mode &= 0xFFu;
     if (mode > SQ_TRACE_BUNDLE) return fail(c, SQ_ERR_INVALID, "sq_trace: unknown mode %u", mode);
     const bool coherent = mode == SQ_TRACE_PACKET || mode == SQ_TRACE_BUNDLE;
@@ -660,6 +706,9 @@ sq_status sq_trace(sq_ctx* c, const sq_bvh* b, const sq_ray_source* rays, uint32
     a.tris = b->tris;
     a.mode = mode;
     a.ray_kind = rays->kind;
+    a.refill = sched_refill ? 1u : 0u;  // the binary tree: 32-ray batches per warp unless asked
+    a.heat_ramp = heat_ramp ? 1u : 0u;
+    a.root_group = 1u;
     uint64_t count = 0;
     float* rays_own = nullptr;
     if (rays->kind == SQ_RAYS_REFERENCE_CAMERA || rays->kind == SQ_RAYS_PINHOLE) {
@@ -667,32 +716,7 @@ sq_status sq_trace(sq_ctx* c, const sq_bvh* b, const sq_ray_source* rays, uint32
         a.width = rays->width;
         a.height = rays->height;
         count = (uint64_t)rays->width * rays->height;
-        if (rays->kind == SQ_RAYS_REFERENCE_CAMERA) {
-            for (int k = 0; k < 3; ++k) a.cam[k] = rays->origin[k];
-        } else {
-            // pinhole basis in double, rounded to float
-            double f[3], r[3], u[3], up[3];
-            for (int k = 0; k < 3; ++k) { f[k] = (double)rays->target[k] - (double)rays->origin[k]; up[k] = rays->up[k]; }
-            const double fl = sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
-            for (double& x : f) x /= fl;
-            r[0] = f[1] * up[2] - f[2] * up[1];
-            r[1] = f[2] * up[0] - f[0] * up[2];
-            r[2] = f[0] * up[1] - f[1] * up[0];
-            const double rl = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
-            for (double& x : r) x /= rl;
-            u[0] = r[1] * f[2] - r[2] * f[1];
-            u[1] = r[2] * f[0] - r[0] * f[2];
-            u[2] = r[0] * f[1] - r[1] * f[0];
-            const double th = tan((double)rays->vfov_deg * 3.14159265358979323846 / 360.0);
-            for (int k = 0; k < 3; ++k) {
-                a.cam[k] = rays->origin[k];
-                a.cam[3 + k] = (float)f[k];
-                a.cam[6 + k] = (float)r[k];
-                a.cam[9 + k] = (float)u[k];
-            }
-            a.cam[12] = (float)(th * (double)rays->width / (double)rays->height);
-            a.cam[13] = (float)th;
-        }
+        camera_params(*rays, a.cam);
     } else if (rays->kind == SQ_RAYS_EXPLICIT) {
         count = rays->ray_count;
         a.ray_count = rays->ray_count;
@@ -752,7 +776,10 @@ sq_status sq_trace(sq_ctx* c, const sq_bvh* b, const sq_ray_source* rays, uint32
             w.work = a.work;
             w.err = a.err;
             w.stats = a.stats;
-            w.refill = a.ray_kind == SQ_RAYS_EXPLICIT ? 1u : 0u;  // camera rays: coherent 8x4 tiles per warp
+            w.heat_ramp = a.heat_ramp;
+            // default: explicit rays refill lanes; camera rays keep coherent
+            // 8x4 tiles per warp
+            w.refill = sched_refill ? 1u : (sched_tiles ? 0u : (a.ray_kind == SQ_RAYS_EXPLICIT ? 1u : 0u));
             sqk::trace8(w, s);
         } else {
             sqk::trace(a, s);
@@ -769,6 +796,234 @@ sq_status sq_trace(sq_ctx* c, const sq_bvh* b, const sq_ray_source* rays, uint32
     dfree(c, hits_tmp);
     dfree(c, heat_tmp);
     return st;
+}
+
+sq_status sq_traverse(sq_ctx* c, const sq_bvh* b, uint32_t index, uint32_t count, const sq_ray* rays, uint32_t n,
+                      sq_hit* hits)
+{
+    if (!c || !b || (n && (!rays || !hits))) return fail(c, SQ_ERR_INVALID, "sq_traverse: null argument");
+    if (count == 0 || (uint64_t)index + count > b->cap)
+        return fail(c, SQ_ERR_INVALID, "sq_traverse: node group [%u, %u + %u) outside the %u nodes", index, index,
+                    count, b->cap);
+    if (n == 0) return SQ_OK;
+    Guard g(c->device);
+    sqk::TraceArgs a;
+    memset(&a, 0, sizeof a);
+    a.nodes = b->nodes;
+    a.node_count = b->cap;
+    a.tri_count = b->n;
+    a.root = index;
+    a.root_group = count;
+    a.tris = b->tris;
+    a.mode = SQ_TRACE_REF;
+    a.ray_kind = SQ_RAYS_EXPLICIT;
+    a.ray_count = n;
+    float* rays_own = nullptr;
+    if (is_device_ptr(rays) && (reinterpret_cast<uintptr_t>(rays) & 15u) == 0) {
+        a.rays = reinterpret_cast<const float*>(rays);
+    } else {
+        rays_own = static_cast<float*>(dalloc(c, sizeof(sq_ray) * (size_t)n));
+        if (!rays_own) return fail(c, SQ_ERR_OOM, "sq_traverse: ray allocation failed");
+        a.rays = rays_own;
+    }
+    const bool hits_dev = is_device_ptr(hits);
+    sq_hit* hits_map = hits_dev ? nullptr : static_cast<sq_hit*>(pinned_device_alias(hits));
+    sq_hit* hits_tmp = nullptr;
+    if (!hits_dev && !hits_map) {
+        hits_tmp = static_cast<sq_hit*>(dalloc(c, sizeof(sq_hit) * (size_t)n));
+        if (!hits_tmp) {
+            dfree(c, rays_own);
+            return fail(c, SQ_ERR_OOM, "sq_traverse: hit buffer allocation failed");
+        }
+    }
+    a.hits = hits_dev ? hits : (hits_map ? hits_map : hits_tmp);
+    a.work = c->ctrl + 1;
+    a.err = c->ctrl;
+    a.stats = reinterpret_cast<unsigned long long*>(c->ctrl + 4);
+    cudaStream_t s = c->stream;
+    cudaError_t e = cudaSuccess;
+    if (rays_own) e = cudaMemcpyAsync(rays_own, rays, sizeof(sq_ray) * (size_t)n, cudaMemcpyDefault, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->ctrl + 1, 0, 11 * sizeof(uint32_t), s);
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev[4], s);
+    if (e == cudaSuccess) {
+        sqk::trace(a, s);
+        e = cudaEventRecord(c->ev[5], s);
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess && hits_tmp)
+        e = cudaMemcpyAsync(hits, hits_tmp, sizeof(sq_hit) * (size_t)n, cudaMemcpyDeviceToHost, s);
+    sq_status st = e == cudaSuccess ? SQ_OK : fail(c, SQ_ERR_CUDA, "sq_traverse: %s", cudaGetErrorString(e));
+    if (st == SQ_OK) {
+        c->trace_timed = true;
+        if (!hits_dev) st = check_device_error(c, nullptr);
+    }
+    dfree(c, rays_own);
+    dfree(c, hits_tmp);
+    return st;
+}
+
+sq_status sq_trace_batches(sq_ctx* c, const sq_bvh* b, const sq_ray_source* batches, uint32_t count, uint32_t mode,
+                           sq_hit* hits, uint8_t* heatmap_rgb)
+{
+    if (!c || !b || (count && !batches)) return fail(c, SQ_ERR_INVALID, "sq_trace_batches: null argument");
+    const bool force_binary = (mode & SQ_TRACE_FORCE_BINARY) != 0;
+    const bool sched_refill = (mode & SQ_TRACE_SCHED_REFILL) != 0;
+    const bool sched_tiles = (mode & SQ_TRACE_SCHED_TILES) != 0;
+    if (sched_refill && sched_tiles) return fail(c, SQ_ERR_INVALID, "sq_trace_batches: choose one ray schedule");
+    if (mode >> 16) return fail(c, SQ_ERR_INVALID, "sq_trace_batches: packet and bundle modes are single-image");
+    const uint32_t heat_ramp = (mode & SQ_TRACE_HEAT_RAMP) ? 1u : 0u;
+    mode &= 0xFFu;
+    if (mode > SQ_TRACE_ANYHIT) return fail(c, SQ_ERR_INVALID, "sq_trace_batches: unknown mode %u", mode);
+    const bool wide = b->nodes8 && mode != SQ_TRACE_REF && !force_binary;
+    Guard g(c->device);
+    // the job table: one job per batch, outputs batch after batch
+    std::vector<sqk::BatchJob> jobs(count);
+    uint64_t rays = 0, batches32 = 0, xrays = 0, staged = 0;
+    for (uint32_t k = 0; k < count; ++k) {
+        const sq_ray_source& rs = batches[k];
+        sqk::BatchJob& j = jobs[k];
+        memset(&j, 0, sizeof j);
+        j.ray_kind = rs.kind;
+        j.root = wide ? 0u : b->root;
+        j.out_offset = (uint32_t)rays;
+        j.batch_begin = (uint32_t)batches32;
+        uint64_t cnt;
+        if (rs.kind == SQ_RAYS_EXPLICIT) {
+            cnt = rs.ray_count;
+            if (cnt && !rs.rays) return fail(c, SQ_ERR_INVALID, "sq_trace_batches: batch %u has no ray array", k);
+            if (cnt && !(is_device_ptr(rs.rays) && (reinterpret_cast<uintptr_t>(rs.rays) & 15u) == 0)) {
+                j.ray_offset = (uint32_t)staged;  // copied to the staging array below
+                staged += cnt;
+            } else {
+                j.rays = reinterpret_cast<const float*>(rs.rays);
+            }
+            xrays += cnt;
+            batches32 += (cnt + 31) / 32;
+        } else if (rs.kind == SQ_RAYS_PINHOLE || rs.kind == SQ_RAYS_REFERENCE_CAMERA) {
+            if (rs.width == 0 || rs.height == 0) return fail(c, SQ_ERR_INVALID, "sq_trace_batches: batch %u: empty image", k);
+            j.width = rs.width;
+            j.height = rs.height;
+            cnt = (uint64_t)rs.width * rs.height;
+            batches32 += (uint64_t)((rs.width + 7) / 8) * ((rs.height + 3) / 4);
+            camera_params(rs, j.cam);
+        } else {
+            return fail(c, SQ_ERR_INVALID, "sq_trace_batches: batch %u: unknown ray kind %u", k, rs.kind);
+        }
+        j.ray_count = (uint32_t)cnt;
+        rays += cnt;
+        if (rays > 0xFFFFFFFFull / 3 || batches32 > 0xFFFFFFFFull)
+            return fail(c, SQ_ERR_INVALID, "sq_trace_batches: too many rays");
+    }
+    sqk::BatchJob* d_jobs = count ? static_cast<sqk::BatchJob*>(dalloc(c, sizeof(sqk::BatchJob) * count)) : nullptr;
+    float* d_staged = staged ? static_cast<float*>(dalloc(c, sizeof(sq_ray) * staged)) : nullptr;
+    const bool hits_dev = hits && is_device_ptr(hits);
+    const bool heat_dev = heatmap_rgb && is_device_ptr(heatmap_rgb);
+    sq_hit* hits_map = (hits && !hits_dev) ? static_cast<sq_hit*>(pinned_device_alias(hits)) : nullptr;
+    uint8_t* heat_map = (heatmap_rgb && !heat_dev) ? static_cast<uint8_t*>(pinned_device_alias(heatmap_rgb)) : nullptr;
+    sq_hit* hits_tmp = (hits && !hits_dev && !hits_map && rays) ? static_cast<sq_hit*>(dalloc(c, sizeof(sq_hit) * rays))
+                                                                 : nullptr;
+    uint8_t* heat_tmp = (heatmap_rgb && !heat_dev && !heat_map && rays) ? static_cast<uint8_t*>(dalloc(c, 3ull * rays))
+                                                                        : nullptr;
+    auto release = [&]() {
+        dfree(c, d_jobs);
+        dfree(c, d_staged);
+        dfree(c, hits_tmp);
+        dfree(c, heat_tmp);
+    };
+    if ((count && !d_jobs) || (staged && !d_staged) || (hits && !hits_dev && !hits_map && rays && !hits_tmp) ||
+        (heatmap_rgb && !heat_dev && !heat_map && rays && !heat_tmp)) {
+        release();
+        return fail(c, SQ_ERR_OOM, "sq_trace_batches: allocation failed");
+    }
+    cudaStream_t s = c->stream;
+    auto cuda_fail = [&](cudaError_t e, const char* what) {
+        release();
+        return fail(c, e == cudaErrorMemoryAllocation ? SQ_ERR_OOM : SQ_ERR_CUDA, "sq_trace_batches: %s: %s", what,
+                    cudaGetErrorString(e));
+    };
+    cudaError_t e;
+    for (uint32_t k = 0; k < count; ++k)
+        if (batches[k].kind == SQ_RAYS_EXPLICIT && batches[k].ray_count && !jobs[k].rays &&
+            (e = cudaMemcpyAsync(d_staged + 8ull * jobs[k].ray_offset, batches[k].rays,
+                                 sizeof(sq_ray) * batches[k].ray_count, cudaMemcpyDefault, s)) != cudaSuccess)
+            return cuda_fail(e, "ray copy");
+    for (auto& j : jobs)
+        if (j.ray_kind == SQ_RAYS_EXPLICIT && !j.rays) j.rays = d_staged;
+    if (count && (e = cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(sqk::BatchJob) * count, cudaMemcpyHostToDevice, s)) !=
+                     cudaSuccess)
+        return cuda_fail(e, "job table copy");
+    sqk::BatchTraceArgs a;
+    memset(&a, 0, sizeof a);
+    a.nodes = b->nodes;
+    a.node_count = b->cap;
+    a.tri_count = b->n;
+    a.nodes8 = b->nodes8;
+    a.tris8 = static_cast<const float4*>(b->tris8);
+    a.tris = b->tris;
+    a.rays = d_staged;
+    a.jobs = d_jobs;
+    a.njobs = count;
+    a.total_batches = (uint32_t)batches32;
+    a.mode = mode;
+    a.hits = hits_dev ? hits : (hits_map ? hits_map : hits_tmp);
+    a.heat = heat_dev ? heatmap_rgb : (heat_map ? heat_map : heat_tmp);
+    a.work = c->ctrl + 1;
+    a.err = c->ctrl;
+    a.stats = reinterpret_cast<unsigned long long*>(c->ctrl + 4);
+    // per-lane refill by default when most rays are explicit (incoherent)
+    a.refill = sched_refill ? 1u : (sched_tiles ? 0u : (2ull * xrays > rays ? 1u : 0u));
+    a.heat_ramp = heat_ramp;
+    if ((e = cudaMemsetAsync(c->ctrl + 1, 0, 11 * sizeof(uint32_t), s)) != cudaSuccess) return cuda_fail(e, "reset");
+    if ((e = cudaEventRecord(c->ev[4], s)) != cudaSuccess) return cuda_fail(e, "event");
+    if (rays) {
+        if (wide) sqk::trace8_batch(a, 128, s);
+        else sqk::trace_batch(a, 128, s);
+    }
+    if ((e = cudaEventRecord(c->ev[5], s)) != cudaSuccess) return cuda_fail(e, "event");
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "launch");
+    c->trace_timed = true;
+    if (hits_tmp && (e = cudaMemcpyAsync(hits, hits_tmp, sizeof(sq_hit) * rays, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+        return cuda_fail(e, "hit copy");
+    if (heat_tmp && (e = cudaMemcpyAsync(heatmap_rgb, heat_tmp, 3ull * rays, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+        return cuda_fail(e, "heatmap copy");
+    sq_status st = SQ_OK;
+    if (hits_tmp || heat_tmp || hits_map || heat_map) st = check_device_error(c, nullptr);
+    release();
+    return st;
+}
+
+sq_status sq_debug_inject(sq_ctx* c, uint32_t what, uint32_t limit)
+{
+    if (!c) return SQ_ERR_INVALID;
+    switch (what) {
+    case SQ_DEBUG_OFF:
+        c->stall_lookback = c->stall_barrier = 0;
+        c->fail_alloc_in = -1;
+        return SQ_OK;
+    case SQ_DEBUG_STALL_LOOKBACK:
+    case SQ_DEBUG_STALL_BARRIER:
+        if (limit == 0 || limit > (1u << 20))
+            return fail(c, SQ_ERR_INVALID, "sq_debug_inject: a poll limit of 1..2^20 is needed");
+        (what == SQ_DEBUG_STALL_LOOKBACK ? c->stall_lookback : c->stall_barrier) = limit + 1u;
+        return SQ_OK;
+    case SQ_DEBUG_FAIL_ALLOC:
+        c->fail_alloc_in = limit;
+        return SQ_OK;
+    default:
+        return fail(c, SQ_ERR_INVALID, "sq_debug_inject: unknown injection %u", what);
+    }
+}
+
+sq_status sq_debug_memory(const sq_ctx* c, uint64_t out[4])
+{
+    if (!c || !out) return SQ_ERR_INVALID;
+    out[0] = c->live_blocks.size();
+    out[1] = 0;
+    for (const auto& kv : c->live_blocks) out[1] += kv.second;
+    out[2] = c->free_blocks.size();
+    out[3] = 0;
+    for (const auto& kv : c->free_blocks) out[3] += kv.first;
+    return SQ_OK;
 }
 
 sq_status sq_last_trace_stats(sq_ctx* c, uint64_t stats[4])

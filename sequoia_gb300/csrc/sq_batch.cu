@@ -341,31 +341,7 @@ sq_status sq_batch_create(sq_ctx* c, const sq_batch_mesh* meshes, uint32_t mesh_
             j.height = rs.height;
             cnt = (uint64_t)rs.width * rs.height;
             batches += (uint64_t)((rs.width + 7) / 8) * ((rs.height + 3) / 4);
-            if (rs.kind == SQ_RAYS_REFERENCE_CAMERA) {
-                for (int k = 0; k < 3; ++k) j.cam[k] = rs.origin[k];
-            } else {
-                double f[3], r[3], u[3], up[3];
-                for (int k = 0; k < 3; ++k) { f[k] = (double)rs.target[k] - (double)rs.origin[k]; up[k] = rs.up[k]; }
-                const double fl = sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
-                for (double& x : f) x /= fl;
-                r[0] = f[1] * up[2] - f[2] * up[1];
-                r[1] = f[2] * up[0] - f[0] * up[2];
-                r[2] = f[0] * up[1] - f[1] * up[0];
-                const double rl = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
-                for (double& x : r) x /= rl;
-                u[0] = r[1] * f[2] - r[2] * f[1];
-                u[1] = r[2] * f[0] - r[0] * f[2];
-                u[2] = r[0] * f[1] - r[1] * f[0];
-                const double th = tan((double)rs.vfov_deg * 3.14159265358979323846 / 360.0);
-                for (int k = 0; k < 3; ++k) {
-                    j.cam[k] = rs.origin[k];
-                    j.cam[3 + k] = (float)f[k];
-                    j.cam[6 + k] = (float)r[k];
-                    j.cam[9 + k] = (float)u[k];
-                }
-                j.cam[12] = (float)(th * (double)rs.width / (double)rs.height);
-                j.cam[13] = (float)th;
-            }
+            camera_params(rs, j.cam);
         } else {
             delete b;
             return fail(c, SQ_ERR_INVALID, "sq_batch_create: unknown ray kind for mesh %u", m);

@@ -405,14 +405,16 @@ __global__ void __launch_bounds__(128) k_collapse_fixed(const Node* __restrict__
 // polls more than kBarrierSpins times raises SQ_DEVERR_SAH_QUEUE and returns
 // (the other blocks then time out at their next barrier too).  Task lists
 // are read through L2 (__ldcg): the same lists are rewritten every other
-// level, so an SM's L1 may hold stale lines of them.
+// level, so an SM's L1 may hold stale lines of them.  The failure-detection
+// tests pass a small poll limit and one phantom block (barrier_extra = 1)
+// that never arrives: every block then gives up at the first barrier.
 constexpr uint32_t kBarrierSpins = 1u << 24;
 
 // Grid barrier; the last block to arrive runs on_last() (thread 0 only)
 // after every other block's writes before the barrier are visible to it and
 // before any block leaves.
 template <class OnLast>
-__device__ bool grid_barrier(uint32_t* bar, uint32_t nblocks, uint32_t* err, OnLast on_last)
+__device__ bool grid_barrier(uint32_t* bar, uint32_t nblocks, uint32_t spin_limit, uint32_t* err, OnLast on_last)
 {
     __shared__ int s_ok;
     __syncthreads();
@@ -430,7 +432,7 @@ __device__ bool grid_barrier(uint32_t* bar, uint32_t nblocks, uint32_t* err, OnL
         } else {
             uint32_t spins = 0;
             while (ld_acquire_u32(bar + 1) == gen) {
-                if (++spins > kBarrierSpins) {
+                if (++spins > spin_limit) {
                     raise_error(err, SQ_DEVERR_SAH_QUEUE);
                     ok = 0;
                     break;
@@ -453,7 +455,8 @@ __device__ bool grid_barrier(uint32_t* bar, uint32_t nblocks, uint32_t* err, OnL
 __global__ void __launch_bounds__(256) k_collapse_coop(const Node* __restrict__ rec, uint32_t leaf0,
                                                        const float* __restrict__ tris, uint32_t* __restrict__ ws,
                                                        uint32_t capacity, Node8* __restrict__ nodes8,
-                                                       float4* __restrict__ tris8, uint32_t* err)
+                                                       float4* __restrict__ tris8, uint32_t* err,
+                                                       uint32_t barrier_extra, uint32_t spin_limit)
 {
     // ws: [0] node counter, [1] triangle counter (one 64-bit pair), [2..3]
     // barrier, [4] levels done, [5] end of the next level's nodes, then the
@@ -492,7 +495,7 @@ __global__ void __launch_bounds__(256) k_collapse_coop(const Node* __restrict__ 
             collapse_node_group(rec, leaf0, tris, active, active ? __ldcg(tasks + i) : 0u, lo + i, nodes8, tris8, err,
                                 s_group[threadIdx.x >> 5], alloc, publish);
         }
-        const bool ok = grid_barrier(bar, gridDim.x, err, [&]() {
+        const bool ok = grid_barrier(bar, gridDim.x + barrier_extra, spin_limit, err, [&]() {
             const uint32_t end = ld_acquire_u32(ws);
             st_relaxed_u32(ws + 5, end < capacity ? end : capacity);
         });
@@ -919,7 +922,6 @@ __device__ Res8 trace8(const Node8* __restrict__ nodes, uint32_t root, const flo
     return trace8_impl<ANY, false>(nodes, root, t8, rp);
 }
 
-__device__ __forceinline__ uint32_t f2u(float x) { return (x >= 0.0f) ? (uint32_t)x : 0u; }
 
 // ---------------------------------------------------------------------------
 // Persistent traversal kernels hand out rays in one of two ways (persistent
@@ -1179,11 +1181,7 @@ __global__ void __launch_bounds__(128) k_trace8_tiles(const sqk::Trace8Args a, u
             h[2] = res.tests;
         }
         if (a.heat) {
-            float x = (float)res.tests / 200.0f;
-            x = (x < 1.0f) ? x : 1.0f;
-            const uint8_t v = (uint8_t)f2u(x * 255.0f);
-            uint8_t* hp = a.heat + 3ull * rid;
-            hp[0] = v; hp[1] = v; hp[2] = v;
+            write_heat(a.heat + 3ull * rid, (float)res.tests, a.heat_ramp);
         }
     }
     if (a.stats) ws.flush(lane, a.stats);
@@ -1251,8 +1249,10 @@ __global__ void __launch_bounds__(128, 6) k_trace8_refill(const sqk::Trace8Args 
             continue;
         }
         if (has) {
-            // slab form: sign-selected planes when no lane's ray can produce NaN
-            if (__all_sync(busy, no_nan_slabs(L.rp))) visit8<ANY, true>(L, nodes, a.tris8, st_e, st_t);
+            // slab form chosen per ray, as trace8 does (sign-selected planes
+            // for a ray that cannot produce NaN), so a ray's box tests do not
+            // depend on the rays it shares a warp with
+            if (no_nan_slabs(L.rp)) visit8<ANY, true>(L, nodes, a.tris8, st_e, st_t);
             else visit8<ANY, false>(L, nodes, a.tris8, st_e, st_t);
             if (L.cur == kNoHit) {
                 has = false;
@@ -1271,11 +1271,7 @@ __global__ void __launch_bounds__(128, 6) k_trace8_refill(const sqk::Trace8Args 
                     h[2] = L.tests;
                 }
                 if (a.heat) {
-                    float x = (float)L.tests / 200.0f;
-                    x = (x < 1.0f) ? x : 1.0f;
-                    const uint8_t v = (uint8_t)f2u(x * 255.0f);
-                    uint8_t* hp = a.heat + 3ull * rid;
-                    hp[0] = v; hp[1] = v; hp[2] = v;
+                    write_heat(a.heat + 3ull * rid, (float)L.tests, a.heat_ramp);
                 }
             }
         }
@@ -1344,7 +1340,7 @@ __global__ void __launch_bounds__(256) k_trace8_batch_tiles(const sqk::BatchTrac
             rid = lb * 32u + lane;
             active = rid < job.ray_count;
             if (active) {
-                const float4* p = reinterpret_cast<const float4*>(a.rays) + 2ull * (job.ray_offset + rid);
+                const float4* p = reinterpret_cast<const float4*>(job.rays ? job.rays : a.rays) + 2ull * (job.ray_offset + rid);
                 const float4 x0 = __ldg(p), x1 = __ldg(p + 1);
                 r.o[0] = x0.x; r.o[1] = x0.y; r.o[2] = x0.z; r.tmin = x0.w;
                 r.d[0] = x1.x; r.d[1] = x1.y; r.d[2] = x1.z; r.tmax = x1.w;
@@ -1376,11 +1372,7 @@ __global__ void __launch_bounds__(256) k_trace8_batch_tiles(const sqk::BatchTrac
             h[2] = res.tests;
         }
         if (a.heat) {
-            float x = (float)res.tests / 200.0f;
-            x = (x < 1.0f) ? x : 1.0f;
-            const uint8_t v = (uint8_t)f2u(x * 255.0f);
-            uint8_t* hp = a.heat + 3ull * out;
-            hp[0] = v; hp[1] = v; hp[2] = v;
+            write_heat(a.heat + 3ull * out, (float)res.tests, a.heat_ramp);
         }
     }
     if (a.stats) ws.flush(lane, a.stats);
@@ -1399,6 +1391,10 @@ __global__ void __launch_bounds__(256) k_trace8_batch_refill(const sqk::BatchTra
     L.cur = kNoHit;
     bool has = false, exhausted = false, explicit_rays = false;
     uint32_t out = 0, tri_offset = 0;
+    // the lane's current job and its 32-ray batch range [jlo, jhi): a lane
+    // takes consecutive slots, so the job search runs only when a slot
+    // leaves the range
+    uint32_t cj = 0, jlo = 1, jhi = 0;
     unsigned long long s_bt = 0, s_tt = 0, s_by = 0, s_nv = 0;
     for (;;) {
         const uint32_t need = __ballot_sync(0xFFFFFFFFu, !has && !exhausted);
@@ -1414,9 +1410,13 @@ __global__ void __launch_bounds__(256) k_trace8_batch_refill(const sqk::BatchTra
                 } else {
                     // ray slot g: lane g mod 32 of the job's 32-ray batch g / 32
                     const uint32_t b = g >> 5, l = g & 31u;
-                    const uint32_t j = find_job(a.jobs, a.njobs, b);
-                    const sqk::BatchJob& job = a.jobs[j];
-                    const uint32_t lb = b - job.batch_begin;
+                    if (b < jlo || b >= jhi) {
+                        cj = find_job(a.jobs, a.njobs, b);
+                        jlo = __ldg(&a.jobs[cj].batch_begin);
+                        jhi = cj + 1 < a.njobs ? __ldg(&a.jobs[cj + 1].batch_begin) : a.total_batches;
+                    }
+                    const sqk::BatchJob& job = a.jobs[cj];
+                    const uint32_t lb = b - jlo;
                     Ray8 r;
                     bool ok;
                     uint32_t rid;
@@ -1432,7 +1432,7 @@ __global__ void __launch_bounds__(256) k_trace8_batch_refill(const sqk::BatchTra
                         rid = lb * 32u + l;
                         ok = rid < job.ray_count;
                         if (ok) {
-                            const float4* p = reinterpret_cast<const float4*>(a.rays) + 2ull * (job.ray_offset + rid);
+                            const float4* p = reinterpret_cast<const float4*>(job.rays ? job.rays : a.rays) + 2ull * (job.ray_offset + rid);
                             const float4 x0 = __ldg(p), x1 = __ldg(p + 1);
                             r.o[0] = x0.x; r.o[1] = x0.y; r.o[2] = x0.z; r.tmin = x0.w;
                             r.d[0] = x1.x; r.d[1] = x1.y; r.d[2] = x1.z; r.tmax = x1.w;
@@ -1453,7 +1453,7 @@ __global__ void __launch_bounds__(256) k_trace8_batch_refill(const sqk::BatchTra
             continue;
         }
         if (has) {
-            if (__all_sync(busy, no_nan_slabs(L.rp))) visit8<ANY, true>(L, nodes, a.tris8, st_e, st_t);
+            if (no_nan_slabs(L.rp)) visit8<ANY, true>(L, nodes, a.tris8, st_e, st_t);
             else visit8<ANY, false>(L, nodes, a.tris8, st_e, st_t);
             if (L.cur == kNoHit) {
                 has = false;
@@ -1473,11 +1473,7 @@ __global__ void __launch_bounds__(256) k_trace8_batch_refill(const sqk::BatchTra
                     h[2] = L.tests;
                 }
                 if (a.heat) {
-                    float x = (float)L.tests / 200.0f;
-                    x = (x < 1.0f) ? x : 1.0f;
-                    const uint8_t v = (uint8_t)f2u(x * 255.0f);
-                    uint8_t* hp = a.heat + 3ull * out;
-                    hp[0] = v; hp[1] = v; hp[2] = v;
+                    write_heat(a.heat + 3ull * out, (float)L.tests, a.heat_ramp);
                 }
             }
         }
@@ -1606,7 +1602,8 @@ static int build_bvh8_levels(const Node* rec, uint32_t root, uint32_t leaf0, con
 }
 
 int build_bvh8(const Node* rec, uint32_t root, uint32_t leaf0, const float* tris, uint32_t n, void* nodes8, void* tris8,
-               uint32_t* ws, uint32_t* host_ctl, uint32_t* err, cudaStream_t s, uint32_t* meta)
+               uint32_t* ws, uint32_t* host_ctl, uint32_t* err, cudaStream_t s, uint32_t* meta,
+               const BarrierStall* stall)
 {
     host_ctl[5] = 0;
     // every block of the cooperative collapse must be resident: the grid is
@@ -1623,8 +1620,10 @@ int build_bvh8(const Node* rec, uint32_t root, uint32_t leaf0, const float* tris
     cudaError_t e;
     if ((e = cudaMemsetAsync(ws, 0, sizeof(uint32_t) * (16 + kFixedLevels), s)) != cudaSuccess) return (int)e;
     k_coop_seed<<<1, 1, 0, s>>>(ws, root);
+    const uint32_t extra = stall ? 1u : 0u;
+    const uint32_t spins = stall ? stall->spin_limit : kBarrierSpins;
     void* args[] = {(void*)&rec, (void*)&leaf0, (void*)&tris, (void*)&ws, (void*)&capacity, (void*)&nodes8,
-                    (void*)&tris8, (void*)&err};
+                    (void*)&tris8, (void*)&err, (void*)&extra, (void*)&spins};
     if ((e = cudaLaunchCooperativeKernel((const void*)k_collapse_coop, dim3(grid), dim3(256), args, 0, s)) !=
         cudaSuccess)
         return (int)e;

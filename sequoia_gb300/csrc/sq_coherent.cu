@@ -32,15 +32,6 @@ using namespace sq;
 
 constexpr int kPacketStack = 128;  // the reference's packet stack (src/tracer.cpp:94)
 
-__device__ __forceinline__ uint32_t f2u(float x) { return (x >= 0.0f) ? (uint32_t)x : 0u; }
-
-// (uint8)(min(1, tests / 200) * 255), src/tracer.cpp:222-225, 270, 353-354
-__device__ __forceinline__ uint8_t heat_byte(float tests)
-{
-    const float x = tests / 200.0f;
-    const float m = (x < 1.0f) ? x : 1.0f;
-    return (uint8_t)f2u(m * 255.0f);
-}
 
 // traverse_packet_stack from nodes [index, index + count) for the packet of
 // lanes `pmask` (all of which call this together): returns the packet's box
@@ -100,9 +91,7 @@ __global__ void __launch_bounds__(128) k_trace_packet(const sqk::TraceArgs a)
             bool fault = false;
             const uint32_t t = packet_tests(a.nodes, a.node_count, a.root, 1u, r.o, inv, pmask, &fault);
             if (fault && m == 0) raise_error(a.err, SQ_DEVERR_STACK_OVERFLOW);
-            const uint8_t v = heat_byte((float)t / (float)K);
-            uint8_t* hp = a.heat + 3ull * ((size_t)y * a.width + x);
-            hp[0] = v; hp[1] = v; hp[2] = v;
+            write_heat(a.heat + 3ull * ((size_t)y * a.width + x), (float)t / (float)K, a.heat_ramp);
             if (m == 0) tests_sum += t;
         }
     }
@@ -237,9 +226,7 @@ __global__ void __launch_bounds__(128) k_trace_bundle(const sqk::TraceArgs a)
         for (int s = 0; s < SLOTS; ++s) {
             if (!valid[s]) continue;
             const float t = (float)btests / (float)K + (float)ptests[s] / 8.0f;
-            const uint8_t v = heat_byte(t);
-            uint8_t* hp = a.heat + 3ull * px[s];
-            hp[0] = v; hp[1] = v; hp[2] = v;
+            write_heat(a.heat + 3ull * px[s], t, a.heat_ramp);
             if ((lane & 7) == 0) tests_sum += ptests[s];
         }
         if (lane == 0) tests_sum += btests;

@@ -147,6 +147,52 @@ __device__ __forceinline__ void raise_error(uint32_t* err, uint32_t bit)
     if (err) atomicOr(err, bit);
 }
 
+// float -> unsigned by truncation toward zero, negative values to 0 (the
+// (uint8_t) conversions of src/tracer.cpp:222-225)
+__host__ __device__ __forceinline__ uint32_t heat_f2u(float x) { return (x >= 0.0f) ? (uint32_t)x : 0u; }
+
+// One heatmap pixel for a box-test count `tests` (or a packet's tests / k):
+//   grey  (uint8)(min(1, tests / 200) * 255) in all three channels
+//         (src/tracer.cpp:222-225);
+//   ramp  the reference's get_heatmap_colour (src/tracer.cpp:25-45) of
+//         tests / 200: black, blue, cyan, green, yellow, red at 0, 0.2, ...,
+//         1, linear between neighbours; each channel (uint8)(c * 255).
+// The ramp's arithmetic is the reference's, one rounding per operation:
+// s = x * 5, i0 = floor(s), i2 = ceil(s), fract = i2 - s,
+// c = col[i0] * fract + col[i2] * (1 - fract).
+__device__ __forceinline__ void write_heat(uint8_t* hp, float tests, uint32_t ramp)
+{
+    const float x = tests / 200.0f;
+    if (!ramp) {
+        const float m = (x < 1.0f) ? x : 1.0f;
+        const uint8_t v = (uint8_t)heat_f2u(m * 255.0f);
+        hp[0] = v; hp[1] = v; hp[2] = v;
+        return;
+    }
+    // stops: (r, g, b) bits of black, blue, cyan, green, yellow, red
+    constexpr uint32_t kR = 0x30u, kG = 0x1Cu, kB = 0x06u;  // bit i: channel of stop i is 1
+    float c[3];
+    if (!(x > 0.0f)) {
+        c[0] = c[1] = c[2] = 0.0f;
+    } else if (x >= 1.0f) {
+        c[0] = 1.0f; c[1] = 0.0f; c[2] = 0.0f;
+    } else {
+        const float s = x * 5.0f;
+        const int i0 = (int)floorf(s), i2 = (int)ceilf(s);
+        const float fract = (float)i2 - s;
+        const float rest = 1.0f - fract;
+        const uint32_t bits[3] = {kR, kG, kB};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float a = (float)((bits[k] >> i0) & 1u), b = (float)((bits[k] >> i2) & 1u);
+            const float pa = a * fract, pb = b * rest;
+            c[k] = pa + pb;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) hp[k] = (uint8_t)heat_f2u(c[k] * 255.0f);
+}
+
 constexpr int kNumSMs = 152;
 constexpr int kMaxDevices = 64;
 
@@ -277,12 +323,21 @@ void lbvh_climb64(const uint64_t* codes, const uint32_t* perm, const float* tris
 size_t sort_lookback_words(uint32_t n, uint32_t digit_bits, uint32_t passes);
 void sort_histogram(const uint32_t* keys, uint32_t n, uint32_t* hist, uint32_t digit_bits, uint32_t passes,
                     cudaStream_t s);
+// Fault injection for the failure-detection tests: the first pass runs
+// without its first tile, so the look-back of the tiles after it waits on
+// words that nothing publishes and gives up after spin_limit empty polls
+// (SQ_DEVERR_LOOKBACK_TIMEOUT).  Only for a one-pass sort whose output
+// nothing else reads: every scatter position stays below the true one, so
+// all writes stay inside the output.
+struct SortStall {
+    uint32_t spin_limit;
+};
 // Runs `passes` onesweep passes; hist/lookback/counters must be zeroed
 // before (lookback and counters) and filled (hist).  Returns which buffer
 // holds the result: 0 = (keys_a, vals_a), 1 = (keys_b, vals_b).
 int sort_passes(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b, uint32_t* vals_b, uint32_t n,
                 const uint32_t* hist, uint32_t* lookback, uint32_t* counters, uint32_t digit_bits,
-                uint32_t passes, uint32_t* err, cudaStream_t s);
+                uint32_t passes, uint32_t* err, cudaStream_t s, const SortStall* stall = nullptr);
 
 // binned SAH / grid builders (sq_sah.cu)
 size_t sah_workspace_bytes(uint32_t n);
@@ -309,6 +364,9 @@ struct TraceArgs {
     uint32_t* work;       // persistent work counter (zeroed)
     uint32_t* err;
     unsigned long long* stats;  // {box tests, triangle tests, bytes requested, node visits}
+    uint32_t refill;      // closest / any-hit: 1 = per-lane ray refill, 0 = 32-ray batches per warp
+    uint32_t heat_ramp;   // heatmap pixels: 0 = grey, 1 = the reference's colour ramp (write_heat)
+    uint32_t root_group;  // REF mode: start from the node group [root, root + root_group) (1 = the root)
 };
 void trace(const TraceArgs& a, cudaStream_t s);
 // packet / bundle tracers of the reference (sq_coherent.cu): heatmap only
@@ -329,6 +387,7 @@ struct Trace8Args {
     uint32_t* err;
     unsigned long long* stats;
     uint32_t refill;       // 1: per-lane ray refill; 0: whole 32-ray batches per warp
+    uint32_t heat_ramp;    // heatmap pixels: 0 = grey, 1 = colour ramp (write_heat)
 };
 // Triangles an 8-wide BVH can address: a traversal stack entry holds the
 // first triangle of a leaf range in 27 bits (and its count in 4).
@@ -342,8 +401,15 @@ size_t bvh8_tri_bytes(uint32_t n);
 // stream instead of being read back (no host synchronisation); host_ctl[4]
 // then holds 2 and host_ctl[0] / [3] are not written.  Returns 1 in
 // host_ctl[5] when meta was filled that way, else 0.
+// Fault injection for the failure-detection tests: the cooperative
+// collapse's grid barrier waits for one block more than the grid, so every
+// block gives up after spin_limit polls (SQ_DEVERR_SAH_QUEUE) and returns.
+struct BarrierStall {
+    uint32_t spin_limit;
+};
 int build_bvh8(const sq::Node* rec, uint32_t root, uint32_t leaf0, const float* tris, uint32_t n, void* nodes8,
-               void* tris8, uint32_t* ws, uint32_t* host_ctl, uint32_t* err, cudaStream_t s, uint32_t* meta = nullptr);
+               void* tris8, uint32_t* ws, uint32_t* host_ctl, uint32_t* err, cudaStream_t s, uint32_t* meta = nullptr,
+               const BarrierStall* stall = nullptr);
 void trace8(const Trace8Args& a, cudaStream_t s);
 
 // batched trace over many BVHs and ray tiles (sq_trace.cu, sq_bvh8.cu)
@@ -356,7 +422,8 @@ struct BatchJob {
     uint32_t root;         // binary root record, or 8-wide root node
     uint32_t batch_begin;  // first 32-ray batch of this job
     uint32_t tri_offset;   // subtracted from reported triangle ids
-    uint32_t pad[3];
+    uint32_t pad;
+    const float* rays;     // explicit rays of this job (null: the shared ray array at ray_offset)
     float cam[16];         // reference camera origin, or pinhole basis (14 floats)
 };
 static_assert(sizeof(BatchJob) == 112, "BatchJob is 112 bytes");
@@ -376,6 +443,7 @@ struct BatchTraceArgs {
     uint32_t* err;
     unsigned long long* stats;
     uint32_t refill;       // 8-wide kernel: 1 = per-lane ray refill (see sq_bvh8.cu)
+    uint32_t heat_ramp;    // heatmap pixels: 0 = grey, 1 = colour ramp (write_heat)
 };
 void trace_batch(const BatchTraceArgs& a, int block_threads, cudaStream_t s);
 void trace8_batch(const BatchTraceArgs& a, int block_threads, cudaStream_t s);

@@ -21,6 +21,11 @@ struct sq_ctx {
     cudaEvent_t ev[8] = {};
     bool build_timed = false, trace_timed = false;
     uint32_t* host_ctl = nullptr;  // pinned, 64 bytes: per-level task counts of the SAH build
+    // fault injection (sq_debug_inject), each armed for one use: 0 = off,
+    // else the wait's poll limit + 1; fail_alloc_in: allocations to let
+    // through before one fails (-1 = off)
+    uint32_t stall_lookback = 0, stall_barrier = 0;
+    int64_t fail_alloc_in = -1;
 };
 
 struct sq_bvh {
@@ -53,6 +58,10 @@ void* dalloc(sq_ctx* c, size_t bytes);
 void dfree(sq_ctx* c, void* p);
 bool is_device_ptr(const void* p);
 sq_status check_device_error(sq_ctx* c, uint32_t* bits_out);
+// Camera constants of a camera ray source as the kernels take them: the
+// reference camera's origin, or the pinhole's eye, forward / right / up
+// basis and image-plane half extents (14 floats).
+void camera_params(const sq_ray_source& rs, float* cam);
 
 struct Guard {
     int prev = -1;

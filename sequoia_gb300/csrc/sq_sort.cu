@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_onesweep(const uint32_t* __restri
                                                      uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n,
                                                      uint32_t shift, const uint32_t* __restrict__ hist,
                                                      uint32_t* __restrict__ lookback, uint32_t* __restrict__ counter,
-                                                     uint32_t* err)
+                                                     uint32_t* err, uint32_t spin_limit, uint32_t tile_base)
 {
     constexpr int RADIX = 1 << DB;
     constexpr uint32_t MASK = RADIX - 1;
@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_onesweep(const uint32_t* __restri
     __shared__ uint32_t s_tile;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) s_tile = atomicAdd(counter, 1u);
+    if (tid == 0) s_tile = atomicAdd(counter, 1u) + tile_base;
     for (int j = tid; j < kWarps * RADIX; j += kBlock) s_whist[j] = 0;
     __syncthreads();
     const uint32_t tile = s_tile;
@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_onesweep(const uint32_t* __restri
                     if (f == kFlagInc || j - q == 0) done = true;
                 }
                 j -= used;
-                if (!done && used == 0 && ++spins > kSpinLimit) {
+                if (!done && used == 0 && ++spins > spin_limit) {
                     raise_error(err, SQ_DEVERR_LOOKBACK_TIMEOUT);
                     break;
                 }
@@ -242,7 +242,8 @@ __global__ void __launch_bounds__(256) k_sort_hist(const uint32_t* __restrict__ 
 
 template <int DB>
 void launch_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, uint32_t n, uint32_t shift,
-                 const uint32_t* hist, uint32_t* lookback, uint32_t* counter, uint32_t* err, cudaStream_t s)
+                 const uint32_t* hist, uint32_t* lookback, uint32_t* counter, uint32_t* err, uint32_t spin_limit,
+                 uint32_t tile_base, cudaStream_t s)
 {
     const size_t bytes = Smem<DB>::bytes;
     // the opt-in above 48 KB of dynamic shared memory is a per-device
@@ -253,7 +254,9 @@ void launch_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint3
         return true;
     });
     const uint32_t tiles = (n + kTile - 1) / kTile;
-    k_onesweep<DB><<<tiles, kBlock, bytes, s>>>(kin, vin, kout, vout, n, shift, hist, lookback, counter, err);
+    if (tiles <= tile_base) return;
+    k_onesweep<DB><<<tiles - tile_base, kBlock, bytes, s>>>(kin, vin, kout, vout, n, shift, hist, lookback, counter,
+                                                            err, spin_limit, tile_base);
 }
 
 int sms() { return sm_count(); }
@@ -281,7 +284,7 @@ void sort_histogram(const uint32_t* keys, uint32_t n, uint32_t* hist, uint32_t d
 
 int sort_passes(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b, uint32_t* vals_b, uint32_t n, const uint32_t* hist,
                 uint32_t* lookback, uint32_t* counters, uint32_t digit_bits, uint32_t passes, uint32_t* err,
-                cudaStream_t s)
+                cudaStream_t s, const SortStall* stall)
 {
     if (n == 0) return 0;
     const size_t radix = (size_t)1 << digit_bits;
@@ -295,9 +298,11 @@ int sort_passes(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b, uint32_t* 
         const uint32_t shift = p * digit_bits;
         const uint32_t* h = hist + p * radix;
         uint32_t* lb = lookback + p * lb_words;
-        if (digit_bits == 8) launch_pass<8>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, s);
-        else if (digit_bits == 10) launch_pass<10>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, s);
-        else launch_pass<6>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, s);
+        const uint32_t spin = stall ? stall->spin_limit : kSpinLimit;
+        const uint32_t tb = (stall && p == 0) ? 1u : 0u;
+        if (digit_bits == 8) launch_pass<8>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, spin, tb, s);
+        else if (digit_bits == 10) launch_pass<10>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, spin, tb, s);
+        else launch_pass<6>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, spin, tb, s);
         cur ^= 1;
     }
     return cur;

@@ -183,8 +183,11 @@ struct Result {
     bool bad;  // an index outside the node or triangle array
 };
 
+// traverse(hierarchy, index, count, ray, attributes) (src/tracer.cpp:47-65)
+// from the node group [root, root + group): every node of the group is
+// tested in turn, then the groups of the hit inner nodes, depth first.
 __device__ Result trace_ref(const Node* __restrict__ nodes, uint32_t nn, uint32_t nt, uint32_t root,
-                            const float* __restrict__ tris, const Ray& r)
+                            const float* __restrict__ tris, const Ray& r, uint32_t group = 1u)
 {
     float inv[3] = {1.0f / r.d[0], 1.0f / r.d[1], 1.0f / r.d[2]};
     uint32_t st_child[kStack], st_count[kStack];
@@ -192,7 +195,7 @@ __device__ Result trace_ref(const Node* __restrict__ nodes, uint32_t nn, uint32_
     uint32_t cnt = 0, tcnt = 0;
     bool hit = false, overflow = false;
     bool bad = false;
-    uint32_t gidx = root, gcnt = 1;
+    uint32_t gidx = root, gcnt = group;
     for (;;) {
         if ((uint64_t)gidx + gcnt > nn) { bad = true; break; }
         for (uint32_t i = 0; i < gcnt; ++i) {
@@ -227,8 +230,130 @@ __device__ Result trace_ref(const Node* __restrict__ nodes, uint32_t nn, uint32_
     return res;
 }
 
-// Stack entries: node index, or (triangle index | 0x80000000) for a leaf
-// record whose triangle is still to be tested.
+// One ray's closest-hit (or any-hit) traversal, resumable one inner node at
+// a time so that a warp can refill a finished lane with a new ray while the
+// others continue.  Stack entries: node index, or (triangle index |
+// 0x80000000) for a leaf record whose triangle is still to be tested.
+struct Lane2 {
+    RayPre rp;
+    float best_t;
+    uint32_t best;
+    uint32_t cnt, tcnt;  // box tests, triangle tests
+    uint32_t cur;        // inner node to visit next; kNoHit when the ray is done
+    int sp;
+    bool overflow, bad;
+};
+
+template <bool ANY>
+__device__ __forceinline__ bool lane2_tri(Lane2& L, const float* __restrict__ tris, uint32_t tri)
+{
+    float t;
+    L.tcnt++;
+    if (tri_watertight(tris, tri, L.rp, L.best_t, t)) {
+        if (t < L.best_t || (t == L.best_t && tri < L.best)) { L.best_t = t; L.best = tri; }
+        if (ANY) return true;
+    }
+    return false;
+}
+
+// The root: its box test, and the triangles of a root that is a leaf record.
+template <bool ANY>
+__device__ __forceinline__ void lane2_start(Lane2& L, const Node* __restrict__ nodes, uint32_t nn, uint32_t nt,
+                                            uint32_t root, const float* __restrict__ tris, const Ray& ray)
+{
+    ray_prepare(ray, L.rp);
+    L.best_t = L.rp.tmax;
+    L.best = kNoHit;
+    L.cnt = 1;
+    L.tcnt = 0;
+    L.sp = 0;
+    L.overflow = false;
+    L.bad = false;
+    L.cur = kNoHit;
+    float tn;
+    if (root >= nn) { L.bad = true; return; }
+    const NodeRec rn = load_node(nodes, root);
+    if (!box_robust(rn, L.rp, L.best_t, tn)) return;
+    if (!node_is_leaf(rn.cf)) { L.cur = root; return; }
+    const uint32_t c = node_count(rn.cf);
+    if ((uint64_t)rn.child + c > nt) { L.bad = true; return; }
+    for (uint32_t k = 0; k < c; ++k)
+        if (lane2_tri<ANY>(L, tris, rn.child + k)) return;
+}
+
+// Visit L.cur (an inner node that passed its box test and the cull test):
+// test all its children's boxes, order the hits by entry distance (ties:
+// slot order), push them, then pop until an inner node survives the cull
+// test, testing leaf triangles on the way.  Leaves L.cur at that node, or at
+// kNoHit when the ray is done.
+template <bool ANY>
+__device__ __forceinline__ void visit2(Lane2& L, const Node* __restrict__ nodes, uint32_t nn, uint32_t nt,
+                                       const float* __restrict__ tris, uint32_t* st_node, float* st_tn)
+{
+    const NodeRec nd = load_node(nodes, L.cur);
+    L.cur = kNoHit;
+    const uint32_t c = node_count(nd.cf);
+    if ((uint64_t)nd.child + c > nn) { L.bad = true; return; }
+    uint32_t hn[8];
+    float ht[8];
+    int nh = 0;
+    for (uint32_t i = 0; i < c; ++i) {
+        const NodeRec ch = load_node(nodes, nd.child + i);
+        L.cnt++;
+        float t;
+        if (box_robust(ch, L.rp, L.best_t, t)) {
+            if (nh >= 8) { L.overflow = true; return; }
+            if (node_is_leaf(ch.cf) && (uint64_t)ch.child + node_count(ch.cf) > nt) { L.bad = true; return; }
+            const uint32_t ent = (node_is_leaf(ch.cf) && node_count(ch.cf) == 1u) ? (ch.child | 0x80000000u)
+                                                                                  : (nd.child + i);
+            // insertion by (tn, slot): equal distances keep slot order
+            int b = nh - 1;
+            while (b >= 0 && ht[b] > t) { hn[b + 1] = hn[b]; ht[b + 1] = ht[b]; --b; }
+            hn[b + 1] = ent;
+            ht[b + 1] = t;
+            nh++;
+        }
+    }
+    if (L.sp + nh > kStack) { L.overflow = true; return; }
+    for (int a = nh - 1; a >= 0; --a) { st_node[L.sp] = hn[a]; st_tn[L.sp] = ht[a]; L.sp++; }
+    while (L.sp > 0) {
+        --L.sp;
+        const uint32_t e = st_node[L.sp];
+        if (st_tn[L.sp] > L.best_t * kRobust) continue;
+        if (e & 0x80000000u) {
+            if (lane2_tri<ANY>(L, tris, e & 0x7FFFFFFFu)) return;
+            continue;
+        }
+        const NodeRec lr = load_node(nodes, e);
+        if (node_is_leaf(lr.cf)) {
+            // leaf record holding several triangles
+            const uint32_t lc = node_count(lr.cf);
+            for (uint32_t k = 0; k < lc; ++k)
+                if (lane2_tri<ANY>(L, tris, lr.child + k)) return;
+            continue;
+        }
+        L.cur = e;
+        return;
+    }
+}
+
+__device__ __forceinline__ Result lane2_result(const Lane2& L)
+{
+    Result res;
+    res.id = L.best;
+    res.t = (L.best == kNoHit) ? 0.0f : L.best_t;
+    res.tests = L.cnt;
+    res.tri_tests = L.tcnt;
+    res.overflow = L.overflow;
+    res.bad = L.bad;
+    return res;
+}
+
+// One ray traced to the end (the tiles kernels): the same traversal as
+// lane2_start + visit2 above, written as one loop, which the compiler fits
+// in fewer registers (48 against 56) -- the per-lane refill kernel needs the
+// resumable form, the tiles kernels do not.  The tests compare the two
+// schedules ray for ray (ids, t and box-test counts).
 template <bool ANY>
 __device__ Result trace_closest(const Node* __restrict__ nodes, uint32_t nn, uint32_t nt, uint32_t root,
                                 const float* __restrict__ tris, const Ray& ray)
@@ -346,7 +471,6 @@ __device__ Result trace_closest(const Node* __restrict__ nodes, uint32_t nn, uin
     return res;
 }
 
-__device__ __forceinline__ uint32_t f2u(float x) { return (x >= 0.0f) ? (uint32_t)x : 0u; }
 
 template <int MODE>
 __global__ void __launch_bounds__(128) k_trace(const sqk::TraceArgs a, uint32_t batches)
@@ -388,7 +512,8 @@ __global__ void __launch_bounds__(128) k_trace(const sqk::TraceArgs a, uint32_t 
         res.tests = 0;
         res.tri_tests = 0;
         if (active) {
-            if (MODE == SQ_TRACE_REF) res = trace_ref(a.nodes, a.node_count, a.tri_count, a.root, a.tris, r);
+            if (MODE == SQ_TRACE_REF) res = trace_ref(a.nodes, a.node_count, a.tri_count, a.root, a.tris, r,
+                                                      a.root_group);
             else res = trace_closest<MODE == SQ_TRACE_ANYHIT>(a.nodes, a.node_count, a.tri_count, a.root, a.tris, r);
             if (res.overflow) raise_error(a.err, SQ_DEVERR_STACK_OVERFLOW);
             if (res.bad) raise_error(a.err, SQ_DEVERR_TOPOLOGY);
@@ -410,14 +535,113 @@ __global__ void __launch_bounds__(128) k_trace(const sqk::TraceArgs a, uint32_t 
             h[2] = res.tests;
         }
         if (a.heat) {
-            float x = (float)res.tests / 200.0f;
-            x = (x < 1.0f) ? x : 1.0f;
-            const uint8_t v = (uint8_t)f2u(x * 255.0f);
-            uint8_t* hp = a.heat + 3ull * rid;
-            hp[0] = v; hp[1] = v; hp[2] = v;
+            write_heat(a.heat + 3ull * rid, (float)res.tests, a.heat_ramp);
         }
     }
     if (a.stats) ws.flush(lane, a.stats);
+}
+
+// Per-lane ray refill (closest / any-hit): a lane whose ray has finished
+// takes the next ray at once (one atomic per warp for all lanes that need
+// one) and every iteration visits one node per lane, so a warp does not
+// wait for its slowest ray.  Each ray is traced with the same arithmetic and
+// visit order as in k_trace, so results are identical; only the assignment
+// of rays to lanes changes.  Ray g is explicit ray g, or pixel (g mod 32) of
+// 8x4 tile g / 32 for camera rays.
+template <int MODE>
+__global__ void __launch_bounds__(128) k_trace_refill(const sqk::TraceArgs a, uint32_t total)
+{
+    constexpr bool ANY = MODE == SQ_TRACE_ANYHIT;
+    const uint32_t lane = threadIdx.x & 31u;
+    const bool camera = a.ray_kind != SQ_RAYS_EXPLICIT;
+    const uint32_t tiles_x = (a.width + 7u) >> 3;
+    uint32_t st_node[kStack];
+    float st_tn[kStack];
+    Lane2 L;
+    L.cur = kNoHit;
+    bool has = false, exhausted = false;
+    uint32_t rid = 0;
+    unsigned long long s_bt = 0, s_tt = 0, s_by = 0;
+    for (;;) {
+        const uint32_t need = __ballot_sync(0xFFFFFFFFu, !has && !exhausted);
+        if (need) {
+            const uint32_t leader = __ffs(need) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(a.work, __popc(need));
+            base = __shfl_sync(0xFFFFFFFFu, base, leader);
+            if (!has && !exhausted) {
+                const uint32_t g = base + __popc(need & ((1u << lane) - 1u));
+                if (g >= total) {
+                    exhausted = true;
+                } else {
+                    Ray r;
+                    bool ok;
+                    if (camera) {
+                        const uint32_t b = g >> 5, l = g & 31u;
+                        const uint32_t x = (b % tiles_x) * 8u + (l & 7u);
+                        const uint32_t y = (b / tiles_x) * 4u + (l >> 3);
+                        ok = x < a.width && y < a.height;
+                        rid = y * a.width + x;
+                        if (ok) {
+                            if (a.ray_kind == SQ_RAYS_REFERENCE_CAMERA) gen_reference_camera(x, y, a.width, a.height, a.cam, r);
+                            else gen_pinhole(x, y, a.width, a.height, a.cam, r);
+                        }
+                    } else {
+                        rid = g;
+                        ok = true;
+                        const float4* p = reinterpret_cast<const float4*>(a.rays) + 2ull * rid;
+                        const float4 x0 = __ldg(p), x1 = __ldg(p + 1);
+                        r.o[0] = x0.x; r.o[1] = x0.y; r.o[2] = x0.z; r.tmin = x0.w;
+                        r.d[0] = x1.x; r.d[1] = x1.y; r.d[2] = x1.z; r.tmax = x1.w;
+                    }
+                    if (ok) {
+                        lane2_start<ANY>(L, a.nodes, a.node_count, a.tri_count, a.root, a.tris, r);
+                        has = true;
+                    }
+                }
+            }
+        }
+        const uint32_t busy = __ballot_sync(0xFFFFFFFFu, has);
+        if (!busy) {
+            if (__all_sync(0xFFFFFFFFu, exhausted)) break;
+            continue;
+        }
+        if (has) {
+            if (L.cur != kNoHit) visit2<ANY>(L, a.nodes, a.node_count, a.tri_count, a.tris, st_node, st_tn);
+            if (L.cur == kNoHit) {
+                has = false;
+                const Result res = lane2_result(L);
+                if (res.overflow) raise_error(a.err, SQ_DEVERR_STACK_OVERFLOW);
+                if (res.bad) raise_error(a.err, SQ_DEVERR_TOPOLOGY);
+                if (a.stats) {
+                    s_bt += res.tests;
+                    s_tt += res.tri_tests;
+                    s_by += (camera ? 0u : 32u) + (a.hits ? 12u : 0u) + (a.heat ? 3u : 0u) + 32ull * res.tests +
+                            36ull * res.tri_tests;
+                }
+                if (a.hits) {
+                    uint32_t* h = reinterpret_cast<uint32_t*>(a.hits) + 3ull * rid;
+                    h[0] = res.id;
+                    h[1] = __float_as_uint(res.t);
+                    h[2] = res.tests;
+                }
+                if (a.heat) {
+                    write_heat(a.heat + 3ull * rid, (float)res.tests, a.heat_ramp);
+                }
+            }
+        }
+    }
+    if (a.stats) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            s_bt += __shfl_xor_sync(0xFFFFFFFFu, s_bt, o);
+            s_tt += __shfl_xor_sync(0xFFFFFFFFu, s_tt, o);
+            s_by += __shfl_xor_sync(0xFFFFFFFFu, s_by, o);
+        }
+        if (lane == 0) {
+            atomicAdd(a.stats, s_bt); atomicAdd(a.stats + 1, s_tt); atomicAdd(a.stats + 2, s_by); atomicAdd(a.stats + 3, s_bt);
+        }
+    }
 }
 
 template <int MODE>
@@ -427,12 +651,21 @@ void launch(const sqk::TraceArgs& a, cudaStream_t s)
     if (a.ray_kind == SQ_RAYS_EXPLICIT) batches = (a.ray_count + 31u) / 32u;
     else batches = ((a.width + 7u) / 8u) * ((a.height + 3u) / 4u);
     if (batches == 0) return;
-    static PerDevice<int> cache;
-    const int per_sm = cache.get([] { return blocks_per_sm(k_trace<MODE>, 128); });
-    uint32_t grid = (uint32_t)(per_sm * sm_count());
+    const bool refill = a.refill && MODE != SQ_TRACE_REF;
+    static PerDevice<std::array<int, 2>> cache;
+    const std::array<int, 2> per_sm = cache.get([] {
+        return std::array<int, 2>{blocks_per_sm(k_trace<MODE>, 128),
+                                  blocks_per_sm(k_trace_refill<MODE == SQ_TRACE_REF ? SQ_TRACE_CLOSEST : MODE>, 128)};
+    });
+    uint32_t grid = (uint32_t)(per_sm[refill ? 1 : 0] * sm_count());
     const uint32_t need = (batches + 3u) / 4u;
     if (grid > need) grid = need;
-    k_trace<MODE><<<grid, 128, 0, s>>>(a, batches);
+    if (refill) {
+        const uint32_t total = a.ray_kind == SQ_RAYS_EXPLICIT ? a.ray_count : batches * 32u;
+        k_trace_refill<MODE == SQ_TRACE_REF ? SQ_TRACE_CLOSEST : MODE><<<grid, 128, 0, s>>>(a, total);
+    } else {
+        k_trace<MODE><<<grid, 128, 0, s>>>(a, batches);
+    }
 }
 
 // Batched trace: warps take 32-ray batches of any job (a mesh's BVH and its
@@ -469,7 +702,7 @@ __global__ void __launch_bounds__(256) k_trace_batch(const sqk::BatchTraceArgs a
             rid = lb * 32u + lane;
             active = rid < job.ray_count;
             if (active) {
-                const float4* p = reinterpret_cast<const float4*>(a.rays) + 2ull * (job.ray_offset + rid);
+                const float4* p = reinterpret_cast<const float4*>(job.rays ? job.rays : a.rays) + 2ull * (job.ray_offset + rid);
                 const float4 x0 = __ldg(p), x1 = __ldg(p + 1);
                 r.o[0] = x0.x; r.o[1] = x0.y; r.o[2] = x0.z; r.tmin = x0.w;
                 r.d[0] = x1.x; r.d[1] = x1.y; r.d[2] = x1.z; r.tmax = x1.w;
@@ -502,11 +735,7 @@ __global__ void __launch_bounds__(256) k_trace_batch(const sqk::BatchTraceArgs a
             h[2] = res.tests;
         }
         if (a.heat) {
-            float x = (float)res.tests / 200.0f;
-            x = (x < 1.0f) ? x : 1.0f;
-            const uint8_t v = (uint8_t)f2u(x * 255.0f);
-            uint8_t* hp = a.heat + 3ull * out;
-            hp[0] = v; hp[1] = v; hp[2] = v;
+            write_heat(a.heat + 3ull * out, (float)res.tests, a.heat_ramp);
         }
     }
     if (a.stats) ws.flush(lane, a.stats);

@@ -209,6 +209,30 @@ uint8_t* trace(Hierarchy& hierarchy, uint32_t w, uint32_t h, vec3f1 origin)
     return camera_trace(hierarchy, w, h, origin, SQ_TRACE_REF);
 }
 
+void traverse(Hierarchy& hierarchy, uint32_t index, uint32_t count, const Ray<1>* rays,
+              HitAttributes<1>* attributes, size_t n)
+{
+    if (n == 0) return;
+    if (n > 0xFFFFFFFFull) throw Error(SQ_ERR_TOO_LARGE, "traverse: more than 2^32-1 rays");
+    std::vector<sq_hit> hits(n);
+    {
+        std::lock_guard<std::mutex> lock(g_mu);
+        sq_ctx* c = ctx_locked();
+        sq_bvh* bvh = tree_locked(c, hierarchy);
+        check(sq_traverse(c, bvh, index, count, reinterpret_cast<const sq_ray*>(rays), (uint32_t)n, hits.data()),
+              "sq_traverse");
+    }
+    for (size_t i = 0; i < n; ++i) {
+        if (hits[i].id != SQ_NO_HIT) attributes[i].hit = -1;
+        attributes[i].num_tests += (int32_t)hits[i].tests;
+    }
+}
+
+void traverse(Hierarchy& hierarchy, uint32_t index, uint32_t count, Ray<1>& ray, HitAttributes<1>& attributes)
+{
+    traverse(hierarchy, index, count, &ray, &attributes, 1);
+}
+
 uint8_t* trace_coherent(Hierarchy& hierarchy, uint32_t w, uint32_t h, vec3f1 origin, bool bundle, uint32_t k)
 {
     return camera_trace(hierarchy, w, h, origin, (bundle ? SQ_TRACE_BUNDLE : SQ_TRACE_PACKET) | SQ_TRACE_WIDTH(k));

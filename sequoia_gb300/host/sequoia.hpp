@@ -88,6 +88,36 @@ public:
     static Hierarchy build_hierarchy_horizontal(std::vector<Triangle>& primitives);
 };
 
+// src/ray.h:8-14 and 25-30 for one ray (K = 1): the same 32-byte ray layout
+// as sq_ray, and the hit flag plus box-test count of traverse().
+template <size_t K>
+struct Ray;
+template <>
+struct Ray<1> {
+    vec3f1 origin;
+    float tmin;
+    vec3f1 direction;
+    float tmax;
+};
+template <size_t K>
+struct HitAttributes;
+template <>
+struct HitAttributes<1> {
+    int32_t hit = 0;        // all bits set (-1) once a triangle was hit, as the reference's SIMD mask
+    int32_t num_tests = 0;  // ray-box tests, added to what the attributes held
+};
+static_assert(sizeof(Ray<1>) == sizeof(sq_ray), "Ray<1> layout");
+
+// src/tracer.h:118, src/tracer.cpp:47-65: the reference's traversal of one
+// ray from the node group [index, index + count) -- usually (root_index, 1)
+// -- OR-ing the hit flag into attributes.hit and adding the box tests to
+// attributes.num_tests.  One ray per call is one GPU launch; the overload
+// below takes many rays at once.
+void traverse(Hierarchy& hierarchy, uint32_t index, uint32_t count, Ray<1>& ray, HitAttributes<1>& attributes);
+// The same for n rays in one launch (attributes[i] for rays[i]).
+void traverse(Hierarchy& hierarchy, uint32_t index, uint32_t count, const Ray<1>* rays,
+              HitAttributes<1>* attributes, size_t n);
+
 // src/tracer.cpp:195-230: w*h rays from the reference camera at `origin`, the
 // per-ray box-test count as a grey heatmap (new[]'d, w*h*3 bytes).
 uint8_t* trace(Hierarchy& hierarchy, uint32_t w, uint32_t h, vec3f1 origin);

@@ -211,6 +211,36 @@ def random_rays(n: int, lo, hi, seed: int = 5, tmax: float = 3.4e38):
     return r
 
 
+def pinhole_rays(w: int, h: int, eye, target, up, vfov: float):
+    """Pinhole camera rays, one per pixel centre, row after row, as float32
+    (n, 8) records {origin, tmin = 0, direction, tmax = FLT_MAX}: the
+    library's pinhole (basis in double, rounded to float; each float32
+    operation rounded once, in the kernels' order)."""
+    f = np.asarray(target, np.float64) - np.asarray(eye, np.float64)
+    f /= np.sqrt((f * f).sum())
+    upv = np.asarray(up, np.float64)
+    r = np.array([f[1] * upv[2] - f[2] * upv[1], f[2] * upv[0] - f[0] * upv[2], f[0] * upv[1] - f[1] * upv[0]])
+    r /= np.sqrt((r * r).sum())
+    u = np.array([r[1] * f[2] - r[2] * f[1], r[2] * f[0] - r[0] * f[2], r[0] * f[1] - r[1] * f[0]])
+    th = math.tan(vfov * math.pi / 360.0)
+    f32 = np.float32
+    fb, rb, ub = f.astype(f32), r.astype(f32), u.astype(f32)
+    sx, sy = f32(th * w / h), f32(th)
+    px = ((np.arange(w, dtype=f32) + f32(0.5)) / f32(w)) * f32(2) - f32(1)
+    py = ((np.arange(h, dtype=f32) + f32(0.5)) / f32(h)) * f32(2) - f32(1)
+    px, py = np.meshgrid(px * sx, py * sy)
+    px, py = px.ravel(), py.ravel()
+    d = np.stack([(fb[k] + px * rb[k]) + py * ub[k] for k in range(3)], 1)
+    l2 = (d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]
+    d = d / np.sqrt(l2)[:, None]
+    out = np.empty((w * h, 8), np.float32)
+    out[:, 0:3] = np.asarray(eye, np.float32)
+    out[:, 3] = 0.0
+    out[:, 4:7] = d
+    out[:, 7] = np.finfo(np.float32).max
+    return out
+
+
 def _hash_u32(x):
     x = x.astype(np.uint64)
     x = (x ^ (x >> np.uint64(16))) * np.uint64(0x7FEB352D) & np.uint64(0xFFFFFFFF)

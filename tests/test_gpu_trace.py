@@ -1,4 +1,6 @@
 """GPU traversal against the reference's golden heatmaps and the oracle."""
+import os
+
 import numpy as np
 import pytest
 
@@ -166,3 +168,95 @@ def test_packet_bundle_argument_checks(ctx):
     for mode, k, w, h in (("packet", 3, 64, 64), ("packet", 8, 63, 64), ("bundle", 64, 64, 60), ("bundle", 8, 64, 64)):
         with pytest.raises(sq.SequoiaError):
             ctx.trace(bvh, mode, k=k, camera="reference", width=w, height=h, origin=(0, 0, -3))
+
+
+@pytest.mark.gpu
+def test_heatmap_colour_ramp(ctx, oracle):
+    """SQ_TRACE_HEAT_RAMP: heatmap pixels in the reference's colour ramp
+    (get_heatmap_colour, src/tracer.cpp:25-45) of the same box-test counts,
+    byte for byte the oracle's, for the reference tracer on the reference's
+    own tree and for closest hit on both tree forms."""
+    from conftest import load_golden
+    g = load_golden("ico4")
+    w, h = int(g["w"]), int(g["h"])
+    bvh = ctx.import_node1(g["sah8_nodes"], int(g["sah8_root"]), g["tris"])
+    hits, heat = ctx.trace(bvh, "ref", camera="reference", width=w, height=h, origin=g["cam"], heatmap=True,
+                           ramp=True)
+    assert np.array_equal(hits["tests"], g["ref_tests"])
+    assert np.array_equal(heat, oracle.heatmap_ramp(g["ref_tests"].astype(np.float32)))
+    from sequoia_gb300 import scenes
+    tris = scenes.gaussian_soup(200_000, 16, seed=91)
+    wbvh = ctx.build(tris, "morton", wide=True)
+    cam = dict(camera="pinhole", width=320, height=200, origin=(0, 0, -40), target=(0, 0, 0))
+    for binary in (True, False):
+        hh, hm = ctx.trace(wbvh, "closest", heatmap=True, ramp=True, binary=binary, **cam)
+        assert np.array_equal(hm, oracle.heatmap_ramp(hh["tests"].astype(np.float32)))
+        # the grey heatmap of the same counts is unchanged
+        _, grey = ctx.trace(wbvh, "closest", heatmap=True, binary=binary, **cam)
+        assert np.array_equal(grey, oracle.heatmap(hh["tests"]))
+    assert ctx.sync() == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["ico3", "soup3k"])
+def test_traverse_node_groups(ctx, name):
+    """sq_traverse (traverse(), src/tracer.cpp:47-65) on the reference's own
+    SAH tree: from (root, 1) it gives the reference's per-ray counts and hit
+    flags (tests/golden); from a node group it gives the sum of the counts
+    and the OR of the hits of its nodes taken one by one, and from the root's
+    child group exactly the root's counts minus the root's own test."""
+    from conftest import load_golden
+    import oracle as O
+    g = load_golden(name)
+    nodes, root = g["sah8_nodes"], int(g["sah8_root"])
+    bvh = ctx.import_node1(nodes, root, g["tris"])
+    rays = O.rays_reference_camera(int(g["w"]), int(g["h"]), g["cam"])
+    h = ctx.traverse(bvh, root, 1, rays)
+    assert np.array_equal(h["tests"], g["ref_tests"])
+    assert np.array_equal((h["id"] == 0).astype(np.uint32), g["ref_hit"])
+    first, count = int(nodes[root]["child"]), int(nodes[root]["count"])
+    grp = ctx.traverse(bvh, first, count, rays)
+    singles = [ctx.traverse(bvh, first + j, 1, rays) for j in range(count)]
+    assert np.array_equal(grp["tests"], sum(s["tests"] for s in singles))
+    hit_any = np.zeros(len(rays), bool)
+    for s in singles:
+        hit_any |= s["id"] == 0
+    assert np.array_equal(grp["id"] == 0, hit_any)
+    root_hit = h["tests"] > 1
+    assert np.array_equal(h["tests"][root_hit], 1 + grp["tests"][root_hit])
+    import sequoia_gb300 as sq
+    with pytest.raises(sq.SequoiaError):
+        ctx.traverse(bvh, len(nodes) - 1, 2, rays)  # a group past the node array
+    assert ctx.sync() == 0
+
+
+@pytest.mark.gpu
+def test_drop_in_traverse(lib_built, tmp_path, oracle):
+    """The C++ drop-in's traverse() (single ray and many rays) on a tree from
+    Builder::build_hierarchy: the oracle's reference-mode counts and hit
+    flags on the same tree; attributes accumulate over calls."""
+    import subprocess
+    from conftest import ROOT
+    from sequoia_gb300 import scenes
+    tris = scenes.displaced_icosphere(4, seed=1)
+    lo, hi = scenes.scene_box(tris)
+    rays = scenes.random_rays(5000, lo, hi, seed=19)
+    rays[:, 7] = 1e4
+    (tmp_path / "tris.bin").write_bytes(tris.tobytes())
+    (tmp_path / "rays.bin").write_bytes(rays.tobytes())
+    exe = str(tmp_path / "drop_in_traverse")
+    inc = ["-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(ROOT, "sequoia_gb300", "host")]
+    lib = os.path.join(ROOT, "sequoia_gb300")
+    subprocess.run(["g++", "-std=c++17", "-O1", *inc, os.path.join(ROOT, "tests", "drop_in_traverse.cpp"), "-o", exe,
+                    "-L" + lib, "-lsequoia_gpu", "-Wl,-rpath," + lib], check=True)
+    subprocess.run([exe, str(tmp_path / "tris.bin"), str(tmp_path / "rays.bin"), str(tmp_path / "out.bin")],
+                   check=True, timeout=300)
+    out = np.fromfile(str(tmp_path / "out.bin"), np.int32).reshape(-1, 2)
+    one, many, twice = out[:64], out[64:64 + len(rays)], out[64 + len(rays):]
+    nodes, root, _ = oracle.build_sah(tris, 8, 8)
+    _, _, tests = oracle.trace(nodes, root, tris, rays, 0)
+    rids, _, _ = oracle.trace(nodes, root, tris, rays, 0)
+    assert np.array_equal(many[:, 1], tests.astype(np.int32))
+    assert np.array_equal(many[:, 0], np.where(rids != 0xFFFFFFFF, -1, 0))
+    assert np.array_equal(one, many[:64])
+    assert np.array_equal(twice[:, 1], 2 * one[:, 1]) and np.array_equal(twice[:, 0], one[:, 0])

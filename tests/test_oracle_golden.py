@@ -131,3 +131,20 @@ def test_morton64_tree_valid(oracle, golden):
     nodes, root, codes, perm = oracle.build_morton64(golden["tris"])
     assert np.array_equal(codes, golden["sorted_codes64"]) and np.array_equal(perm, golden["sorted_index64"])
     assert (oracle.leaf_reach(nodes, root, n) == 1).all()
+
+
+def test_heatmap_colour_matches_reference(oracle):
+    """The oracle's restatement of get_heatmap_colour (src/tracer.cpp:25-45)
+    equals the reference's own function bit for bit on the golden inputs
+    (every count / 200 up to 1000, the stops and their float neighbours,
+    out-of-range values, seeded uniform values)."""
+    g = load_golden("heat_ramp")
+    got = oracle.heatmap_colour(g["x"])
+    assert np.array_equal(got.view(np.uint32), g["rgb"].view(np.uint32))
+    if oracle.ref_available("b8"):
+        ref = oracle.ref_heatmap_colour(g["x"], "b8")
+        assert np.array_equal(ref.view(np.uint32), g["rgb"].view(np.uint32))
+    # the heatmap bytes: black at 0, red from 200 tests on, grey-free ramp
+    rgb = oracle.heatmap_ramp(np.array([0, 40, 100, 200, 5000], np.float32)).reshape(-1, 3)
+    assert rgb[0].tolist() == [0, 0, 0] and rgb[3].tolist() == [255, 0, 0] and rgb[4].tolist() == [255, 0, 0]
+    assert rgb[1].tolist() == [0, 0, 255]  # 40 / 200 = 0.2: the blue stop
