@@ -70,6 +70,7 @@ CONFIG = {"workload": "soup_2m: 2,000,000-triangle 64-cluster Gaussian soup, 384
                       "from (0,0,-40)",
           "builder": "Morton LBVH + 8-wide 8-bit quantised collapse", "trace": "closest hit + heatmap",
           "tris": 2_000_000, "rays": 3840 * 2160, "l2": "flushed between steps (512 MB write)"}
+BATCH_BUILDERS = ("morton", "sah")
 LBVH_KERNELS = 8  # scene bounds, Morton codes, 4 onesweep passes, climb (local + global phase)
 TRACE_PROFILE = os.path.join(ROOT, "profiles", "k_trace8_tiles_soup2m.md")
 TRACE_SOURCE = os.path.join(ROOT, "sequoia_gb300", "csrc", "sq_bvh8.cu")
@@ -411,8 +412,8 @@ def batch_leg(ctx, flush, torch):
     stream = torch.cuda.current_stream()
     d_hits = torch.empty(n_rays * 3, dtype=torch.int32, device="cuda")
     out = {"meshes": len(meshes), "tris": n_tris, "rays": n_rays}
-    for builder in ("morton", "sah"):
-        b = ctx.batch(descs, mode="closest", wide=True, graph=True, builder=builder)
+    for builder in BATCH_BUILDERS:
+        b = ctx.batch(descs, mode="closest", wide=True, graph=True, **({"builder": builder} if builder != "morton" else {}))
         best, _ = b.autotune()
         for _ in range(3):
             b.run(hits=False)

@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define SQ_ABI_VERSION 1u
+#define SQ_ABI_VERSION 2u
 
 typedef enum sq_status {
     SQ_OK = 0,
@@ -333,11 +333,14 @@ sq_status sq_trace_batches(sq_ctx* ctx, const sq_bvh* bvh, const sq_ray_source* 
 /* ---- batches: many meshes and ray tiles, one launch sequence ------------ */
 
 /* Build-and-trace of many independent meshes at once: the reference's
- * build_hierarchy_morton + trace (src/builder.cpp:2474, src/tracer.cpp:195)
- * run for every mesh, as one sequence of launches over all meshes, captured
- * once in a CUDA graph (SQ_BATCH_GRAPH) and replayed by sq_batch_run.  The
- * reference has no batched form; each mesh's result equals a separate
- * sq_build + sq_trace of that mesh (same trees, same hits).                */
+ * build_hierarchy_morton or build_hierarchy (binned SAH) + trace
+ * (src/builder.cpp:2474, 1576, src/tracer.cpp:195) run for every mesh, as
+ * one sequence of launches over all meshes, captured once in a CUDA graph
+ * (SQ_BATCH_GRAPH) and replayed by sq_batch_run.  The sequence never waits
+ * on the host: the SAH build runs a fixed number of level launches with
+ * device-side task counts.  The reference has no batched form; each mesh's
+ * result equals a separate sq_build + sq_trace of that mesh with the same
+ * builder settings (same trees, same hits).                               */
 typedef struct sq_batch sq_batch;
 
 typedef struct sq_batch_mesh {
@@ -349,12 +352,14 @@ typedef struct sq_batch_mesh {
 #define SQ_BATCH_GRAPH 0x1u    /* capture the run in a CUDA graph           */
 
 typedef struct sq_batch_params {
-    uint32_t builder;          /* SQ_BUILDER_MORTON                         */
-    uint32_t sort_digit_bits;  /* 6, 8 or 10 (0 = 8)                        */
+    uint32_t builder;          /* SQ_BUILDER_MORTON or SQ_BUILDER_SAH       */
+    uint32_t sort_digit_bits;  /* Morton: 6, 8 or 10 (0 = 8)                */
     uint32_t wide;             /* 1: trace the 8-wide quantised BVH         */
     uint32_t block_threads;    /* trace block: 64, 128 or 256 (0 = 128)     */
     uint32_t mode;             /* sq_trace_mode                             */
     uint32_t flags;            /* SQ_BATCH_*                                */
+    uint32_t sah_bins;         /* SAH: 8, 16 or 32 bins (0 = 8)             */
+    uint32_t leaf_size;        /* SAH: leaf when count <= leaf_size (0 = 8) */
 } sq_batch_params;
 
 typedef struct sq_batch_info {
@@ -371,11 +376,14 @@ sq_status sq_batch_create(sq_ctx* ctx, const sq_batch_mesh* meshes, uint32_t mes
 sq_status sq_batch_run(sq_batch* batch, sq_hit* hits, uint8_t* heatmap_rgb);
 sq_status sq_batch_info_get(const sq_batch* batch, sq_batch_info* info);
 sq_status sq_batch_free(sq_batch* batch);
-/* Time every sort digit width (6/8/10), BVH width (binary / 8-wide) and
- * trace block shape (64/128/256) on this batch, keep the fastest (the batch
- * is re-prepared with it) and return it.  cache_path (optional): JSON-lines
- * file; a cached choice for the batch's size class is used without timing,
- * a new choice is appended.                                                 */
+/* Time every sort digit width (6/8/10; Morton batches) or SAH bin count
+ * (8/16/32; SAH batches), BVH width (binary / 8-wide) and trace block shape
+ * (64/128/256) on this batch, keep the fastest (the batch is re-prepared
+ * with it) and return it.  Digit width, width and block shape never change
+ * a result; the SAH bin count changes the trees, so box-test counts and
+ * any-hit ids may change with it (closest-hit ids and t do not).
+ * cache_path (optional): JSON-lines file; a cached choice for the batch's
+ * size class is used without timing, a new choice is appended.             */
 sq_status sq_batch_autotune(sq_batch* batch, const char* cache_path, sq_batch_params* best,
                             float* best_ms);
 

@@ -70,7 +70,8 @@ class _BatchMesh(C.Structure):
 
 class _BatchParams(C.Structure):
     _fields_ = [("builder", C.c_uint32), ("sort_digit_bits", C.c_uint32), ("wide", C.c_uint32),
-                ("block_threads", C.c_uint32), ("mode", C.c_uint32), ("flags", C.c_uint32)]
+                ("block_threads", C.c_uint32), ("mode", C.c_uint32), ("flags", C.c_uint32),
+                ("sah_bins", C.c_uint32), ("leaf_size", C.c_uint32)]
 
 
 class _ObjInfo(C.Structure):
@@ -243,9 +244,9 @@ class Batch:
         i = _BatchInfo()
         self.ctx._check(load_library().sq_batch_info_get(self.handle, C.byref(i)))
         p = i.params
-        return {"meshes": i.meshes, "tris": i.tris, "rays": i.rays, "graph": bool(i.graph),
-                "sort_digit_bits": p.sort_digit_bits, "wide": p.wide, "block_threads": p.block_threads,
-                "mode": p.mode}
+        return {"meshes": i.meshes, "tris": i.tris, "rays": i.rays, "graph": bool(i.graph), "builder": p.builder,
+                "sort_digit_bits": p.sort_digit_bits, "sah_bins": p.sah_bins, "leaf_size": p.leaf_size,
+                "wide": p.wide, "block_threads": p.block_threads, "mode": p.mode}
 
     def run(self, hits=True, heatmap=False):
         n = self.info()["rays"]
@@ -259,7 +260,12 @@ class Batch:
         ms = C.c_float()
         path = cache_path.encode() if cache_path else None
         self.ctx._check(load_library().sq_batch_autotune(self.handle, path, C.byref(best), C.byref(ms)))
-        return {"sort_digit_bits": best.sort_digit_bits, "wide": best.wide, "block_threads": best.block_threads}, ms.value
+        out = {"wide": best.wide, "block_threads": best.block_threads}
+        if best.builder == BUILDERS["sah"]:
+            out["sah_bins"] = best.sah_bins
+        else:
+            out["sort_digit_bits"] = best.sort_digit_bits
+        return out, ms.value
 
     def free(self):
         if self.handle and self.ctx.handle:
@@ -438,9 +444,11 @@ class Context:
         self._check(load_library().sq_last_trace_stats(self.handle, C.byref(arr)))
         return {"box_tests": arr[0], "tri_tests": arr[1], "bytes": arr[2], "nodes": arr[3]}
 
-    def batch(self, meshes, mode="closest", wide=True, digit_bits=8, block=128, graph=True):
+    def batch(self, meshes, mode="closest", wide=True, digit_bits=8, block=128, graph=True, builder="morton",
+              bins=8, leaf=8):
         """meshes: list of dicts with `tris` and either `rays` (explicit) or a
-        camera (`camera`, `width`, `height`, `origin`, `target`, `up`, `vfov`)."""
+        camera (`camera`, `width`, `height`, `origin`, `target`, `up`, `vfov`).
+        builder: "morton" (digit_bits) or "sah" (bins, leaf)."""
         arr = (_BatchMesh * len(meshes))()
         keep = []
         for k, m in enumerate(meshes):
@@ -455,7 +463,8 @@ class Context:
             if m.get("rays") is not None:
                 keep.append(m["rays"])
             arr[k].rays = src
-        p = _BatchParams(0, digit_bits, 1 if wide else 0, block, MODES[mode], 1 if graph else 0)
+        p = _BatchParams(BUILDERS[builder], digit_bits, 1 if wide else 0, block, MODES[mode], 1 if graph else 0,
+                         bins, leaf)
         h = C.c_void_p()
         self._check(load_library().sq_batch_create(self.handle, arr, len(meshes), C.byref(p), C.byref(h)))
         return Batch(self, h, keep)

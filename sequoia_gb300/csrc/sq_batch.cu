@@ -1,7 +1,7 @@
 // sq_batch.cu -- many meshes and ray tiles, built and traced by one launch
 // sequence that is captured once in a CUDA graph and replayed.
 //
-// Build (all meshes together, no host synchronisation):
+// Build (all meshes together, no host synchronisation), Morton builder:
 //   k_seg_bounds     every mesh's box (warp-aggregated atomics per mesh)
 //   k_seg_morton     30-bit Morton codes in each mesh's own box (as if the
 //                    reference's setup_morton, src/builder.cpp:2204-2237, ran
@@ -14,13 +14,18 @@
 //   8-wide collapse  (optional) seeded with all mesh roots, a fixed number
 //                    of level kernels with device-side task counts: 8-wide
 //                    node m is mesh m's root
+// SAH builder: sqk::build_sah_batch (sq_sah.cu) -- per-mesh root boxes and
+// root tasks, then the binned SAH's level kernels over all meshes' tasks at
+// once, a fixed number of levels with device-side task counts, the small
+// phase and the leaves; the same records a single build of each mesh writes.
 // Trace: one persistent kernel over a job table (mesh, camera or rays,
 // output offset); warps take 32-ray batches of any job.
 //
 // Autotuner: sq_batch_autotune times every combination of sort digit width
-// (6/8/10), BVH width (2 or 8-wide quantised) and trace block shape
-// (64/128/256 threads) on the caller's batch and keeps the fastest; results
-// are cached in a JSON-lines file keyed by the batch's size class.
+// (6/8/10; Morton) or SAH bin count (8/16/32; SAH), BVH width (2 or 8-wide
+// quantised) and trace block shape (64/128/256 threads) on the caller's
+// batch and keeps the fastest; results are cached in a JSON-lines file keyed
+// by the batch's size class and builder.
 #include "sq_internal.cuh"
 #include "sq_lbvh_dev.cuh"
 
@@ -51,6 +56,7 @@ struct sq_batch {
     size_t zero_words = 0;
     uint32_t* d_keys = nullptr;       // 4 x N sort buffers + codes by triangle + sorted codes
     float4* d_info = nullptr;         // 4N climb sibling records
+    void* d_sah_ws = nullptr;         // SAH batches: the builder's workspace
     sq_hit* d_hits = nullptr;
     uint8_t* d_heat = nullptr;
     std::vector<sqk::BatchJob> jobs;  // host copy (roots patched per width)
@@ -198,8 +204,14 @@ sq_status enqueue_run(sq_batch* b)
     uint32_t* vb = kb + N;
     uint32_t* code_by_tri = vb + N;
     uint32_t* codes = code_by_tri + N;
-    SQ_CUDA(c, cudaMemsetAsync(z, 0, sizeof(uint32_t) * words, s));
-    if (N > 0) {
+    if (b->params.builder != SQ_BUILDER_SAH) SQ_CUDA(c, cudaMemsetAsync(z, 0, sizeof(uint32_t) * words, s));
+    if (b->params.builder == SQ_BUILDER_SAH) {
+        const uint32_t nb = b->params.sah_bins ? b->params.sah_bins : 8u;
+        const uint32_t leaf = b->params.leaf_size ? b->params.leaf_size : 8u;
+        const int rc = sqk::build_sah_batch(b->d_tris, N, b->d_off, M, nb, leaf, 3u * N + 2u, b->d_nodes, b->d_sah_ws,
+                                            c->ctrl, s);
+        if (rc) return fail(c, SQ_ERR_CUDA, "batch SAH build: %s", cudaGetErrorString((cudaError_t)rc));
+    } else if (N > 0) {
         const uint32_t g = min((N + 255) / 256, (uint32_t)sms() * 8u);
         k_seg_bounds<<<g, 256, 0, s>>>(b->d_tris, N, b->d_off, M, box_ord);
         k_seg_morton<<<g, 256, sizeof(uint32_t) * passes * radix, s>>>(b->d_tris, N, b->d_off, M, box_ord, ka, va,
@@ -296,8 +308,8 @@ std::string size_class(const sq_batch* b)
 {
     char buf[128];
     auto bucket = [](double v) { return v > 0 ? (int)std::floor(std::log2(v) * 2.0) : -1; };
-    snprintf(buf, sizeof buf, "meshes%d_tris%d_rays%d_mode%u", bucket(b->meshes), bucket(b->tris), bucket(b->rays),
-             b->params.mode);
+    snprintf(buf, sizeof buf, "meshes%d_tris%d_rays%d_mode%u_builder%u", bucket(b->meshes), bucket(b->tris),
+             bucket(b->rays), b->params.mode, b->params.builder);
     return buf;
 }
 
@@ -310,6 +322,12 @@ sq_status sq_batch_create(sq_ctx* c, const sq_batch_mesh* meshes, uint32_t mesh_
 {
     if (!c || !meshes || !params || !out || mesh_count == 0) return fail(c, SQ_ERR_INVALID, "sq_batch_create: bad argument");
     if (params->mode > SQ_TRACE_ANYHIT) return fail(c, SQ_ERR_INVALID, "sq_batch_create: unknown mode");
+    if (params->builder != SQ_BUILDER_MORTON && params->builder != SQ_BUILDER_SAH)
+        return fail(c, SQ_ERR_UNSUPPORTED, "sq_batch_create: batches build with the Morton or the SAH builder");
+    if (params->builder == SQ_BUILDER_SAH &&
+        ((params->sah_bins && params->sah_bins != 8 && params->sah_bins != 16 && params->sah_bins != 32) ||
+         params->leaf_size > 65535u))
+        return fail(c, SQ_ERR_INVALID, "sq_batch_create: SAH bins must be 8, 16 or 32 and leaf_size at most 65535");
     *out = nullptr;
     Guard g(c->device);
     sq_batch* b = new (std::nothrow) sq_batch;
@@ -376,6 +394,13 @@ sq_status sq_batch_create(sq_ctx* c, const sq_batch_mesh* meshes, uint32_t mesh_
     b->d_info = static_cast<float4*>(dalloc(c, sizeof(float4) * 6ull * (N ? N : 1)));
     b->d_hits = static_cast<sq_hit*>(dalloc(c, sizeof(sq_hit) * (rays ? rays : 1)));
     b->d_heat = static_cast<uint8_t*>(dalloc(c, 3ull * (rays ? rays : 1)));
+    if (params->builder == SQ_BUILDER_SAH) {
+        b->d_sah_ws = dalloc(c, sqk::sah_batch_workspace_bytes(N, M));
+        if (!b->d_sah_ws) {
+            sq_batch_free(b);
+            return fail(c, SQ_ERR_OOM, "batch allocation failed");
+        }
+    }
     if (!b->d_tris || !b->d_off || !b->d_rays || !b->d_jobs || !b->d_roots || !b->d_nodes || !b->d_nodes8 ||
         !b->d_tris8 || !b->d_ws8 || !b->d_zero || !b->d_keys || !b->d_info || !b->d_hits || !b->d_heat) {
         sq_batch_free(b);
@@ -455,7 +480,7 @@ sq_status sq_batch_free(sq_batch* b)
     cudaStreamSynchronize(c->stream);
     if (b->graph) cudaGraphExecDestroy(b->graph);
     void* bufs[] = {b->d_tris, b->d_off, b->d_rays, b->d_jobs, b->d_roots, b->d_nodes, b->d_nodes8, b->d_tris8,
-                    b->d_ws8, b->d_zero, b->d_keys, b->d_info, b->d_hits, b->d_heat};
+                    b->d_ws8, b->d_zero, b->d_keys, b->d_info, b->d_hits, b->d_heat, b->d_sah_ws};
     for (void* p : bufs) dfree(c, p);
     delete b;
     return SQ_OK;
@@ -468,17 +493,20 @@ sq_status sq_batch_autotune(sq_batch* b, const char* cache_path, sq_batch_params
     Guard g(c->device);
     const std::string key = size_class(b);
     sq_batch_params base = b->params;
+    const bool sah = base.builder == SQ_BUILDER_SAH;
     // cache lookup
     if (cache_path) {
         if (FILE* fh = fopen(cache_path, "r")) {
             char line[512];
             while (fgets(line, sizeof line, fh)) {
                 char k[160];
-                unsigned db = 0, wide = 0, block = 0;
+                unsigned db = 0, bins = 0, wide = 0, block = 0;
                 float ms = 0;
-                if (sscanf(line, "{\"key\": \"%159[^\"]\", \"sort_digit_bits\": %u, \"wide\": %u, \"block_threads\": %u, \"ms\": %f}",
-                           k, &db, &wide, &block, &ms) == 5 && key == k) {
+                if (sscanf(line, "{\"key\": \"%159[^\"]\", \"sort_digit_bits\": %u, \"sah_bins\": %u, \"wide\": %u, "
+                                 "\"block_threads\": %u, \"ms\": %f}",
+                           k, &db, &bins, &wide, &block, &ms) == 6 && key == k) {
                     b->params.sort_digit_bits = db;
+                    b->params.sah_bins = bins;
                     b->params.wide = wide;
                     b->params.block_threads = block;
                     fclose(fh);
@@ -492,18 +520,21 @@ sq_status sq_batch_autotune(sq_batch* b, const char* cache_path, sq_batch_params
             fclose(fh);
         }
     }
-    const uint32_t digits[3] = {6, 8, 10}, widths[2] = {0, 1}, blocks[3] = {64, 128, 256};
+    // the builder's own knob: sort digit width (Morton) or bin count (SAH)
+    const uint32_t digits[3] = {6, 8, 10}, bin_counts[3] = {8, 16, 32}, widths[2] = {0, 1}, blocks[3] = {64, 128, 256};
+    const uint32_t* knob = sah ? bin_counts : digits;
     float best_t = 3.4e38f;
     sq_batch_params best_p = base;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    for (uint32_t d : digits)
+    for (int ki = 0; ki < 3; ++ki)
         for (uint32_t w : widths)
             for (uint32_t bl : blocks) {
                 if (w && b->tris > sqk::kWide8MaxTris) continue;  // beyond the 8-wide form's reach
                 b->params = base;
-                b->params.sort_digit_bits = d;
+                if (sah) b->params.sah_bins = knob[ki];
+                else b->params.sort_digit_bits = knob[ki];
                 b->params.wide = w;
                 b->params.block_threads = bl;
                 sq_status st = prepare(b);
@@ -530,8 +561,9 @@ sq_status sq_batch_autotune(sq_batch* b, const char* cache_path, sq_batch_params
     if (best_ms) *best_ms = best_t;
     if (cache_path) {
         if (FILE* fh = fopen(cache_path, "a")) {
-            fprintf(fh, "{\"key\": \"%s\", \"sort_digit_bits\": %u, \"wide\": %u, \"block_threads\": %u, \"ms\": %.4f}\n",
-                    key.c_str(), best_p.sort_digit_bits, best_p.wide, best_p.block_threads, best_t);
+            fprintf(fh, "{\"key\": \"%s\", \"sort_digit_bits\": %u, \"sah_bins\": %u, \"wide\": %u, \"block_threads\": %u, "
+                        "\"ms\": %.4f}\n",
+                    key.c_str(), best_p.sort_digit_bits, best_p.sah_bins, best_p.wide, best_p.block_threads, best_t);
             fclose(fh);
         }
     }

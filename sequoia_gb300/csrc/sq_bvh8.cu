@@ -1378,8 +1378,10 @@ __global__ void __launch_bounds__(256) k_trace8_batch_tiles(const sqk::BatchTrac
     if (a.stats) ws.flush(lane, a.stats);
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(256) k_trace8_batch_refill(const sqk::BatchTraceArgs a)
+// Launch bounds of 28 warps per SM whatever the block shape: the same
+// register budget (72) as k_trace8_refill, whose occupancy it needs.
+template <int MODE, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, 896 / BLOCK) k_trace8_batch_refill(const sqk::BatchTraceArgs a)
 {
     constexpr bool ANY = MODE == SQ_TRACE_ANYHIT;
     const uint32_t lane = threadIdx.x & 31u;
@@ -1501,16 +1503,18 @@ void launch8_batch(const sqk::BatchTraceArgs& a, int block, cudaStream_t s)
         return std::array<int, 6>{blocks_per_sm(k_trace8_batch_tiles<MODE>, 64),
                                   blocks_per_sm(k_trace8_batch_tiles<MODE>, 128),
                                   blocks_per_sm(k_trace8_batch_tiles<MODE>, 256),
-                                  blocks_per_sm(k_trace8_batch_refill<MODE>, 64),
-                                  blocks_per_sm(k_trace8_batch_refill<MODE>, 128),
-                                  blocks_per_sm(k_trace8_batch_refill<MODE>, 256)};
+                                  blocks_per_sm(k_trace8_batch_refill<MODE, 64>, 64),
+                                  blocks_per_sm(k_trace8_batch_refill<MODE, 128>, 128),
+                                  blocks_per_sm(k_trace8_batch_refill<MODE, 256>, 256)};
     });
     const int bi = block <= 64 ? 0 : (block <= 128 ? 1 : 2);
     const int v = a.refill ? 1 : 0;
     uint32_t grid = (uint32_t)(per_sm[3 * v + bi] * sm_count());
     const uint32_t need = (a.total_batches + (uint32_t)(block / 32) - 1) / (uint32_t)(block / 32);
     if (grid > need) grid = need;
-    if (v) k_trace8_batch_refill<MODE><<<grid, block, 0, s>>>(a);
+    if (v && bi == 0) k_trace8_batch_refill<MODE, 64><<<grid, 64, 0, s>>>(a);
+    else if (v && bi == 1) k_trace8_batch_refill<MODE, 128><<<grid, 128, 0, s>>>(a);
+    else if (v) k_trace8_batch_refill<MODE, 256><<<grid, 256, 0, s>>>(a);
     else k_trace8_batch_tiles<MODE><<<grid, block, 0, s>>>(a);
 }
 

@@ -341,6 +341,12 @@ int sort_passes(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b, uint32_t* 
 
 // binned SAH / grid builders (sq_sah.cu)
 size_t sah_workspace_bytes(uint32_t n);
+size_t sah_batch_workspace_bytes(uint32_t n, uint32_t meshes);
+// SAH trees of M meshes in one launch sequence with no host synchronisation
+// (graph-capturable): mesh m = triangles [off[m], off[m + 1]) (off on the
+// device), root record root0 + m, leaf records at 2n + 2 + position.
+int build_sah_batch(const float* tris, uint32_t n, const uint32_t* off, uint32_t M, uint32_t nb, uint32_t leaf_size,
+                    uint32_t root0, sq::Node* nodes, void* ws, uint32_t* err, cudaStream_t s);
 int build_sah(const float* tris, uint32_t n, uint32_t nb, uint32_t leaf_size, int grid, uint32_t scene_box_cells,
               sq::Node* nodes, float* scene_out, void* ws, uint32_t* sort_keys, uint32_t* sort_vals,
               uint32_t* sort_alt_keys, uint32_t* sort_alt_vals, uint32_t* sort_lookback, uint32_t* sort_counters,

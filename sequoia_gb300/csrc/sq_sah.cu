@@ -40,6 +40,9 @@ constexpr uint32_t kSmall = 128;
 constexpr int kMaxBins = 32;
 constexpr int kBinWords = 13;  // -pmin xyz, pmax xyz, -cmin xyz, cmax xyz (ordered ints), count
 constexpr int kStackDepth = 24;
+// Large-phase levels of the batched build (device-side counts, no host
+// round trip): deeper work is finished by the small phase.
+constexpr uint32_t kBatchLargeLevels = 24;
 
 struct __align__(16) Task {
     uint32_t begin, count, slot, flags;  // flags: bit0 = ids live in buffer B, bit1 = root-like record
@@ -62,10 +65,15 @@ struct Split {
     uint32_t pad[3];
 };
 
+// Task counts.  n_large[l & 1] holds the large tasks of level l: level l
+// reads it and appends its large children to n_large[(l + 1) & 1], which
+// the level's prep kernel clears first; the kernels read the counts on the
+// device, so a level needs no host round trip.
 struct Ctl {
-    uint32_t n_large_next, n_small, n_leaf, small_pop;
-    uint32_t err_bits, pad[3];
+    uint32_t n_large[2], n_small, n_leaf;
+    uint32_t small_pop, err_bits, pad[2];
 };
+static_assert(sizeof(Ctl) == 32, "Ctl is 32 bytes");
 
 __device__ __forceinline__ float box_sa(const float* mn, const float* mx)
 {
@@ -156,9 +164,10 @@ __global__ void __launch_bounds__(256) k_sah_setup(const float* __restrict__ tri
 __device__ __forceinline__ float dec_neg(uint32_t u) { return -ordered_to_float(u); }
 __device__ __forceinline__ float dec_pos(uint32_t u) { return ordered_to_float(u); }
 
-// Place a task: leaf (recorded in the leaf list), large, or small.
-__device__ void classify(const Task& t, uint32_t leaf_size, Task* __restrict__ large_next, Task* __restrict__ small,
-                         LeafRange* __restrict__ leaves, Ctl* ctl)
+// Place a task: leaf (recorded in the leaf list), large (appended to
+// large_next, counted in *large_cnt), or small.
+__device__ void classify(const Task& t, uint32_t leaf_size, Task* __restrict__ large_next, uint32_t* large_cnt,
+                         Task* __restrict__ small, LeafRange* __restrict__ leaves, Ctl* ctl)
 {
     const bool leaf = t.count <= leaf_size || !(box_sa(t.cmn, t.cmx) > 0.0f);
     if (leaf) {
@@ -169,7 +178,7 @@ __device__ void classify(const Task& t, uint32_t leaf_size, Task* __restrict__ l
         lr.pad[0] = lr.pad[1] = 0;
         leaves[k] = lr;
     } else if (t.count > kSmall) {
-        large_next[atomicAdd(&ctl->n_large_next, 1u)] = t;
+        large_next[atomicAdd(large_cnt, 1u)] = t;
     } else {
         small[atomicAdd(&ctl->n_small, 1u)] = t;
     }
@@ -188,7 +197,7 @@ __global__ void k_root_task(const uint32_t* __restrict__ root_ord, uint32_t n, u
         scene_out[k] = t.pmn[k];
         scene_out[3 + k] = t.pmx[k];
     }
-    classify(t, leaf_size, large, small, leaves, ctl);
+    classify(t, leaf_size, large, &ctl->n_large[0], small, leaves, ctl);
 }
 
 // ---------------------------------------------------------------------------
@@ -277,7 +286,7 @@ __global__ void k_grid_tasks(const uint32_t* __restrict__ cell_ord, const uint32
         // the plain grid builder gives every cell node the scene box (src/builder.cpp:2173-2174)
         for (int k = 0; k < 3; ++k) { t.pmn[k] = dec_neg(root_ord[k]); t.pmx[k] = dec_pos(root_ord[3 + k]); }
     }
-    classify(t, leaf_size, large, small, leaves, ctl);
+    classify(t, leaf_size, large, &ctl->n_large[0], small, leaves, ctl);
 }
 
 // heap of 63 inner nodes above the 64 cell nodes (src/builder.cpp:2181-2188)
@@ -439,12 +448,27 @@ __device__ __forceinline__ Task child_task(uint32_t begin, uint32_t count, uint3
 
 // ---------------------------------------------------------------------------
 // large phase
+//
+// Every kernel reads the level's task count *ntp on the device and loops
+// over its work (chunks per block, tasks per warp), so the same kernels run
+// with an exact grid when the host knows the count and with a fixed grid in
+// the graph-captured batch build, where it does not.
 
-__global__ void k_large_prep(const Task* __restrict__ tasks, uint32_t nt, int nb, Split* __restrict__ split,
-                             uint32_t* __restrict__ chunk_start)
+__global__ void k_large_zero(uint32_t* __restrict__ bins, const uint32_t* __restrict__ ntp, int nb)
+{
+    const size_t per = (size_t)nb * kBinWords;
+    const size_t words = (size_t)(*ntp) * per;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < words; i += (size_t)gridDim.x * blockDim.x)
+        bins[(i / per) * (kMaxBins * kBinWords) + i % per] = 0;
+}
+
+__global__ void k_large_prep(const Task* __restrict__ tasks, const uint32_t* __restrict__ ntp, uint32_t* next_cnt,
+                             int nb, Split* __restrict__ split, uint32_t* __restrict__ chunk_start)
 {
     // single block: chunk counts and their exclusive scan
     __shared__ uint32_t s_sum[1024];
+    const uint32_t nt = *ntp;
+    if (threadIdx.x == 0) *next_cnt = 0;  // this level's large children are counted from 0
     uint32_t carry = 0;
     for (uint32_t base = 0; base < nt; base += blockDim.x) {
         const uint32_t t = base + threadIdx.x;
@@ -486,144 +510,154 @@ __device__ __forceinline__ uint32_t task_of_chunk(const uint32_t* __restrict__ c
     return lo;
 }
 
-__global__ void __launch_bounds__(256) k_large_bin(const Task* __restrict__ tasks, uint32_t nt,
+__global__ void __launch_bounds__(256) k_large_bin(const Task* __restrict__ tasks, const uint32_t* __restrict__ ntp,
                                                    const Split* __restrict__ split, const uint32_t* __restrict__ chunk_start,
                                                    const uint32_t* __restrict__ ids_a, const uint32_t* __restrict__ ids_b,
                                                    const float4* __restrict__ tb, int nb, uint32_t* __restrict__ bins_g)
 {
     __shared__ uint32_t s_wb[8][kMaxBins * kBinWords];
-    const uint32_t c = blockIdx.x;
-    if (c >= __ldg(chunk_start + nt)) return;
-    const uint32_t t = task_of_chunk(chunk_start, nt, c);
-    const Task tk = tasks[t];
-    const Split sp = split[t];
-    const uint32_t off = (c - chunk_start[t]) * kChunk;
-    const uint32_t len = min(kChunk, tk.count - off);
-    const uint32_t* ids = (tk.flags & 1u) ? ids_b : ids_a;
+    const uint32_t nt = *ntp;
+    const uint32_t chunks = chunk_start[nt];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t* wb = s_wb[warp];
-    for (int j = lane; j < kMaxBins * kBinWords; j += 32) wb[j] = 0;
-    __syncwarp();
-    for (uint32_t base = warp * 32; base < len; base += 256) {
-        const uint32_t j = base + lane;
-        float mn[3], mx[3], cc[3];
-        int bin = nb;
-        if (j < len) {
-            load_box(tb, ids[tk.begin + off + j], mn, mx);
-            for (int a = 0; a < 3; ++a) cc[a] = (mn[a] + mx[a]) * 0.5f;
-            bin = bin_of(sp.k1, sel(cc, sp.axis), sp.cmin, nb);
-        } else {
-            for (int a = 0; a < 3; ++a) { mn[a] = mx[a] = cc[a] = 0.0f; }
+    for (uint32_t c = blockIdx.x; c < chunks; c += gridDim.x) {
+        const uint32_t t = task_of_chunk(chunk_start, nt, c);
+        const Task tk = tasks[t];
+        const Split sp = split[t];
+        const uint32_t off = (c - chunk_start[t]) * kChunk;
+        const uint32_t len = min(kChunk, tk.count - off);
+        const uint32_t* ids = (tk.flags & 1u) ? ids_b : ids_a;
+        for (int j = lane; j < kMaxBins * kBinWords; j += 32) wb[j] = 0;
+        __syncwarp();
+        for (uint32_t base = warp * 32; base < len; base += 256) {
+            const uint32_t j = base + lane;
+            float mn[3], mx[3], cc[3];
+            int bin = nb;
+            if (j < len) {
+                load_box(tb, ids[tk.begin + off + j], mn, mx);
+                for (int a = 0; a < 3; ++a) cc[a] = (mn[a] + mx[a]) * 0.5f;
+                bin = bin_of(sp.k1, sel(cc, sp.axis), sp.cmin, nb);
+            } else {
+                for (int a = 0; a < 3; ++a) { mn[a] = mx[a] = cc[a] = 0.0f; }
+            }
+            warp_bin_add(wb, bin, nb, mn, mx, cc);
         }
-        warp_bin_add(wb, bin, nb, mn, mx, cc);
-    }
-    __syncthreads();
-    uint32_t* g = bins_g + (size_t)t * kMaxBins * kBinWords;
-    for (int j = threadIdx.x; j < nb * kBinWords; j += blockDim.x) {
-        uint32_t v = s_wb[0][j];
-        const bool is_count = (j % kBinWords) == 12;
-        for (int w = 1; w < 8; ++w) v = is_count ? v + s_wb[w][j] : max(v, s_wb[w][j]);
-        if (v) {
-            if (is_count) atomicAdd(g + j, v); else atomicMax(g + j, v);
+        __syncthreads();
+        uint32_t* g = bins_g + (size_t)t * kMaxBins * kBinWords;
+        for (int j = threadIdx.x; j < nb * kBinWords; j += blockDim.x) {
+            uint32_t v = s_wb[0][j];
+            const bool is_count = (j % kBinWords) == 12;
+            for (int w = 1; w < 8; ++w) v = is_count ? v + s_wb[w][j] : max(v, s_wb[w][j]);
+            if (v) {
+                if (is_count) atomicAdd(g + j, v); else atomicMax(g + j, v);
+            }
         }
+        __syncthreads();  // every warp's bins read before the next chunk clears them
     }
 }
 
-__global__ void k_large_split(const Task* __restrict__ tasks, uint32_t nt, Split* __restrict__ split,
+__global__ void k_large_split(const Task* __restrict__ tasks, const uint32_t* __restrict__ ntp, Split* __restrict__ split,
                               const uint32_t* __restrict__ bins_g, int nb, uint32_t base, uint32_t leaf_size,
-                              Node* __restrict__ nodes, Task* large_next, Task* small, LeafRange* leaves, Ctl* ctl)
+                              Node* __restrict__ nodes, Task* large_next, uint32_t* next_cnt, Task* small,
+                              LeafRange* leaves, Ctl* ctl)
 {
-    const uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nt = *ntp;
     const int lane = threadIdx.x & 31;
-    if (t >= nt) return;
-    const Task tk = tasks[t];
-    const PlaneResult r = warp_choose_plane(bins_g + (size_t)t * kMaxBins * kBinWords, nb);
-    if (lane != 0) return;
-    if (r.plane < 0 || r.nl == 0 || r.nl == tk.count) {
-        // no plane scored below FLT_MAX: the node becomes a leaf
-        Task leaf = tk;
-        leaf.count = tk.count;
-        const uint32_t k = atomicAdd(&ctl->n_leaf, 1u);
-        LeafRange lr;
-        lr.begin = tk.begin; lr.count = tk.count; lr.slot = tk.slot; lr.flags = tk.flags;
-        for (int a = 0; a < 3; ++a) { lr.pmn[a] = tk.pmn[a]; lr.pmx[a] = tk.pmx[a]; }
-        lr.pad[0] = lr.pad[1] = 0;
-        leaves[k] = lr;
-        (void)leaf;
-        return;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nt; t += warps) {
+        const Task tk = tasks[t];
+        const PlaneResult r = warp_choose_plane(bins_g + (size_t)t * kMaxBins * kBinWords, nb);
+        if (lane != 0) continue;
+        if (r.plane < 0 || r.nl == 0 || r.nl == tk.count) {
+            // no plane scored below FLT_MAX: the node becomes a leaf
+            const uint32_t k = atomicAdd(&ctl->n_leaf, 1u);
+            LeafRange lr;
+            lr.begin = tk.begin; lr.count = tk.count; lr.slot = tk.slot; lr.flags = tk.flags;
+            for (int a = 0; a < 3; ++a) { lr.pmn[a] = tk.pmn[a]; lr.pmx[a] = tk.pmx[a]; }
+            lr.pad[0] = lr.pad[1] = 0;
+            leaves[k] = lr;
+            continue;
+        }
+        Split s = split[t];
+        s.plane = r.plane;
+        s.nl = r.nl;
+        split[t] = s;
+        const uint32_t q = tk.begin + r.nl;
+        Box pb;
+        for (int a = 0; a < 3; ++a) { pb.mn[a] = tk.pmn[a]; pb.mx[a] = tk.pmx[a]; }
+        store_node(nodes + tk.slot, pb, base + 2u * q, 2u, 0);
+        const uint32_t buf = (tk.flags & 1u) ^ 1u;
+        classify(child_task(tk.begin, r.nl, base + 2u * q, buf, r.lp, r.lc), leaf_size, large_next, next_cnt, small,
+                 leaves, ctl);
+        classify(child_task(q, tk.count - r.nl, base + 2u * q + 1u, buf, r.rp, r.rc), leaf_size, large_next, next_cnt,
+                 small, leaves, ctl);
     }
-    Split s = split[t];
-    s.plane = r.plane;
-    s.nl = r.nl;
-    split[t] = s;
-    const uint32_t q = tk.begin + r.nl;
-    Box pb;
-    for (int a = 0; a < 3; ++a) { pb.mn[a] = tk.pmn[a]; pb.mx[a] = tk.pmx[a]; }
-    store_node(nodes + tk.slot, pb, base + 2u * q, 2u, 0);
-    const uint32_t buf = (tk.flags & 1u) ^ 1u;
-    classify(child_task(tk.begin, r.nl, base + 2u * q, buf, r.lp, r.lc), leaf_size, large_next, small, leaves, ctl);
-    classify(child_task(q, tk.count - r.nl, base + 2u * q + 1u, buf, r.rp, r.rc), leaf_size, large_next, small, leaves,
-             ctl);
 }
 
-__global__ void __launch_bounds__(256) k_large_count(const Task* __restrict__ tasks, uint32_t nt,
+__global__ void __launch_bounds__(256) k_large_count(const Task* __restrict__ tasks, const uint32_t* __restrict__ ntp,
                                                      const Split* __restrict__ split,
                                                      const uint32_t* __restrict__ chunk_start,
                                                      const uint32_t* __restrict__ ids_a, const uint32_t* __restrict__ ids_b,
                                                      const float4* __restrict__ tb, int nb,
                                                      uint32_t* __restrict__ chunk_left)
 {
-    const uint32_t c = blockIdx.x;
-    if (c >= __ldg(chunk_start + nt)) return;
-    const uint32_t t = task_of_chunk(chunk_start, nt, c);
-    const Split sp = split[t];
-    if (sp.plane < 0) return;
-    const Task tk = tasks[t];
-    const uint32_t off = (c - chunk_start[t]) * kChunk;
-    const uint32_t len = min(kChunk, tk.count - off);
-    const uint32_t* ids = (tk.flags & 1u) ? ids_b : ids_a;
-    uint32_t cnt = 0;
-    for (uint32_t j = threadIdx.x; j < len; j += blockDim.x) {
-        float mn[3], mx[3];
-        load_box(tb, ids[tk.begin + off + j], mn, mx);
-        const float cc = (sel(mn, sp.axis) + sel(mx, sp.axis)) * 0.5f;
-        cnt += bin_of(sp.k1, cc, sp.cmin, nb) <= sp.plane;
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xFFFFFFFFu, cnt, o);
     __shared__ uint32_t s[8];
-    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = cnt;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t total = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) total += s[w];
-        chunk_left[c] = total;
+    const uint32_t nt = *ntp;
+    const uint32_t chunks = chunk_start[nt];
+    for (uint32_t c = blockIdx.x; c < chunks; c += gridDim.x) {
+        const uint32_t t = task_of_chunk(chunk_start, nt, c);
+        const Split sp = split[t];
+        if (sp.plane < 0) continue;  // block-uniform
+        const Task tk = tasks[t];
+        const uint32_t off = (c - chunk_start[t]) * kChunk;
+        const uint32_t len = min(kChunk, tk.count - off);
+        const uint32_t* ids = (tk.flags & 1u) ? ids_b : ids_a;
+        uint32_t cnt = 0;
+        for (uint32_t j = threadIdx.x; j < len; j += blockDim.x) {
+            float mn[3], mx[3];
+            load_box(tb, ids[tk.begin + off + j], mn, mx);
+            const float cc = (sel(mn, sp.axis) + sel(mx, sp.axis)) * 0.5f;
+            cnt += bin_of(sp.k1, cc, sp.cmin, nb) <= sp.plane;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xFFFFFFFFu, cnt, o);
+        if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = cnt;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t total = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) total += s[w];
+            chunk_left[c] = total;
+        }
+        __syncthreads();
     }
 }
 
 // exclusive scan of the left counts over each task's chunks (one warp per task)
-__global__ void k_large_scan(const Split* __restrict__ split, uint32_t nt, const uint32_t* __restrict__ chunk_start,
-                             uint32_t* __restrict__ chunk_left)
+__global__ void k_large_scan(const Split* __restrict__ split, const uint32_t* __restrict__ ntp,
+                             const uint32_t* __restrict__ chunk_start, uint32_t* __restrict__ chunk_left)
 {
-    const uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nt = *ntp;
     const int lane = threadIdx.x & 31;
-    if (t >= nt || split[t].plane < 0) return;
-    uint32_t carry = 0;
-    for (uint32_t c0 = chunk_start[t]; c0 < chunk_start[t + 1]; c0 += 32) {
-        const uint32_t c = c0 + lane;
-        const uint32_t v = c < chunk_start[t + 1] ? chunk_left[c] : 0u;
-        uint32_t x = v;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nt; t += warps) {
+        if (split[t].plane < 0) continue;  // warp-uniform
+        uint32_t carry = 0;
+        for (uint32_t c0 = chunk_start[t]; c0 < chunk_start[t + 1]; c0 += 32) {
+            const uint32_t c = c0 + lane;
+            const uint32_t v = c < chunk_start[t + 1] ? chunk_left[c] : 0u;
+            uint32_t x = v;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-            if (lane >= o) x += y;
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (c < chunk_start[t + 1]) chunk_left[c] = carry + x - v;
+            carry += __shfl_sync(0xFFFFFFFFu, x, 31);
         }
-        if (c < chunk_start[t + 1]) chunk_left[c] = carry + x - v;
-        carry += __shfl_sync(0xFFFFFFFFu, x, 31);
     }
 }
 
-__global__ void __launch_bounds__(256) k_large_scatter(const Task* __restrict__ tasks, uint32_t nt,
+__global__ void __launch_bounds__(256) k_large_scatter(const Task* __restrict__ tasks, const uint32_t* __restrict__ ntp,
                                                        const Split* __restrict__ split,
                                                        const uint32_t* __restrict__ chunk_start,
                                                        uint32_t* __restrict__ ids_a, uint32_t* __restrict__ ids_b,
@@ -631,58 +665,71 @@ __global__ void __launch_bounds__(256) k_large_scatter(const Task* __restrict__ 
                                                        const uint32_t* __restrict__ chunk_left)
 {
     constexpr int kPer = kChunk / 256;  // 8 consecutive elements per thread
-    const uint32_t c = blockIdx.x;
-    if (c >= __ldg(chunk_start + nt)) return;
-    const uint32_t t = task_of_chunk(chunk_start, nt, c);
-    const Split sp = split[t];
-    if (sp.plane < 0) return;
-    const Task tk = tasks[t];
-    const uint32_t off = (c - chunk_start[t]) * kChunk;
-    const uint32_t len = min(kChunk, tk.count - off);
-    const uint32_t* in = (tk.flags & 1u) ? ids_b : ids_a;
-    uint32_t* out = (tk.flags & 1u) ? ids_a : ids_b;
-    uint32_t idv[kPer];
-    bool left[kPer];
-    uint32_t cnt = 0;
-#pragma unroll
-    for (int k = 0; k < kPer; ++k) {
-        const uint32_t j = threadIdx.x * kPer + k;
-        left[k] = false;
-        idv[k] = 0;
-        if (j < len) {
-            idv[k] = in[tk.begin + off + j];
-            float mn[3], mx[3];
-            load_box(tb, idv[k], mn, mx);
-            const float cc = (sel(mn, sp.axis) + sel(mx, sp.axis)) * 0.5f;
-            left[k] = bin_of(sp.k1, cc, sp.cmin, nb) <= sp.plane;
-            cnt += left[k];
-        }
-    }
-    // block exclusive scan of per-thread left counts
     __shared__ uint32_t s_w[8];
+    const uint32_t nt = *ntp;
+    const uint32_t chunks = chunk_start[nt];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t x = cnt;
+    for (uint32_t c = blockIdx.x; c < chunks; c += gridDim.x) {
+        const uint32_t t = task_of_chunk(chunk_start, nt, c);
+        const Split sp = split[t];
+        if (sp.plane < 0) continue;  // block-uniform
+        const Task tk = tasks[t];
+        const uint32_t off = (c - chunk_start[t]) * kChunk;
+        const uint32_t len = min(kChunk, tk.count - off);
+        const uint32_t* in = (tk.flags & 1u) ? ids_b : ids_a;
+        uint32_t* out = (tk.flags & 1u) ? ids_a : ids_b;
+        uint32_t idv[kPer];
+        bool left[kPer];
+        uint32_t cnt = 0;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) s_w[warp] = x;
-    __syncthreads();
-    uint32_t wsum = 0;
-    for (int w = 0; w < warp; ++w) wsum += s_w[w];
-    uint32_t lrank = wsum + x - cnt;                    // left elements before this thread in the chunk
-    const uint32_t left_before = chunk_left[c];          // left elements before this chunk in the task
-    const uint32_t lbase = tk.begin + left_before;
-    const uint32_t rbase = tk.begin + sp.nl + (off - left_before);
-#pragma unroll
-    for (int k = 0; k < kPer; ++k) {
-        const uint32_t j = threadIdx.x * kPer + k;
-        if (j < len) {
-            if (left[k]) { out[lbase + lrank] = idv[k]; lrank++; }
-            else out[rbase + (j - lrank)] = idv[k];
+        for (int k = 0; k < kPer; ++k) {
+            const uint32_t j = threadIdx.x * kPer + k;
+            left[k] = false;
+            idv[k] = 0;
+            if (j < len) {
+                idv[k] = in[tk.begin + off + j];
+                float mn[3], mx[3];
+                load_box(tb, idv[k], mn, mx);
+                const float cc = (sel(mn, sp.axis) + sel(mx, sp.axis)) * 0.5f;
+                left[k] = bin_of(sp.k1, cc, sp.cmin, nb) <= sp.plane;
+                cnt += left[k];
+            }
         }
+        // block exclusive scan of per-thread left counts
+        uint32_t x = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) s_w[warp] = x;
+        __syncthreads();
+        uint32_t wsum = 0;
+        for (int w = 0; w < warp; ++w) wsum += s_w[w];
+        uint32_t lrank = wsum + x - cnt;                    // left elements before this thread in the chunk
+        const uint32_t left_before = chunk_left[c];          // left elements before this chunk in the task
+        const uint32_t lbase = tk.begin + left_before;
+        const uint32_t rbase = tk.begin + sp.nl + (off - left_before);
+#pragma unroll
+        for (int k = 0; k < kPer; ++k) {
+            const uint32_t j = threadIdx.x * kPer + k;
+            if (j < len) {
+                if (left[k]) { out[lbase + lrank] = idv[k]; lrank++; }
+                else out[rbase + (j - lrank)] = idv[k];
+            }
+        }
+        __syncthreads();  // s_w read by every warp before the next chunk writes it
     }
+}
+
+// After the last fixed level of the batch build: large tasks still left go
+// to the small phase, whose warps split subtrees of any size.
+__global__ void k_large_to_small(const Task* __restrict__ large, const uint32_t* __restrict__ ntp,
+                                 Task* __restrict__ small, Ctl* ctl)
+{
+    const uint32_t nt = *ntp;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x)
+        small[atomicAdd(&ctl->n_small, 1u)] = large[t];
 }
 
 // ---------------------------------------------------------------------------
@@ -841,27 +888,171 @@ __global__ void __launch_bounds__(128) k_small(const Task* __restrict__ small, C
 
 int sms() { return sm_count(); }
 
+// Workspace carving shared by the single and the batched build.
+struct SahWs {
+    float4* tb;
+    uint32_t *ids_a, *ids_b;
+    Task *lists[2], *small;
+    LeafRange* leaves;
+    Split* split;
+    uint32_t *chunk_start, *chunk_left, *bins, *cells, *hist, *root_ord;
+    Ctl* ctl;
+};
+
+size_t sah_tasks(uint32_t n) { return n / kSmall + 2; }
+
+size_t sah_ws_bytes(uint32_t n, uint32_t meshes)
+{
+    const size_t tasks = sah_tasks(n);
+    size_t b = 0;
+    auto add = [&](size_t bytes) { b += (bytes + 255) / 256 * 256; };
+    add(sizeof(float4) * 2ull * n);               // triangle boxes
+    add(sizeof(uint32_t) * (size_t)n);            // ids A
+    add(sizeof(uint32_t) * (size_t)n);            // ids B
+    add(sizeof(Task) * tasks);                    // large lists (two levels)
+    add(sizeof(Task) * tasks);
+    add(sizeof(Task) * ((size_t)n / 2 + 2));      // small list
+    add(sizeof(LeafRange) * ((size_t)n + 66 + meshes));  // leaf list (+64 empty grid cells, + empty meshes)
+    add(sizeof(Split) * tasks);
+    add(sizeof(uint32_t) * (tasks + 1));          // chunk starts
+    add(sizeof(uint32_t) * ((size_t)n / kChunk + tasks + 1));  // chunk left counts
+    add(sizeof(uint32_t) * (size_t)kMaxBins * kBinWords * tasks);  // bins
+    add(sizeof(uint32_t) * 64 * kBinWords);       // grid cells
+    add(sizeof(uint32_t) * 64);                   // grid histogram
+    add(sizeof(uint32_t) * 16ull * (meshes ? meshes : 1));  // root boxes (12 words per mesh)
+    add(sizeof(Ctl));
+    return b;
+}
+
+SahWs carve(void* ws, uint32_t n, uint32_t meshes)
+{
+    const size_t tasks = sah_tasks(n);
+    char* p = static_cast<char*>(ws);
+    auto take = [&](size_t bytes) { char* r = p; p += (bytes + 255) / 256 * 256; return r; };
+    SahWs w;
+    w.tb = reinterpret_cast<float4*>(take(sizeof(float4) * 2ull * n));
+    w.ids_a = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * (size_t)n));
+    w.ids_b = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * (size_t)n));
+    w.lists[0] = reinterpret_cast<Task*>(take(sizeof(Task) * tasks));
+    w.lists[1] = reinterpret_cast<Task*>(take(sizeof(Task) * tasks));
+    w.small = reinterpret_cast<Task*>(take(sizeof(Task) * ((size_t)n / 2 + 2)));
+    w.leaves = reinterpret_cast<LeafRange*>(take(sizeof(LeafRange) * ((size_t)n + 66 + meshes)));
+    w.split = reinterpret_cast<Split*>(take(sizeof(Split) * tasks));
+    w.chunk_start = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * (tasks + 1)));
+    w.chunk_left = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * ((size_t)n / kChunk + tasks + 1)));
+    w.bins = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * (size_t)kMaxBins * kBinWords * tasks));
+    w.cells = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * 64 * kBinWords));
+    w.hist = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * 64));
+    w.root_ord = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * 16ull * (meshes ? meshes : 1)));
+    w.ctl = reinterpret_cast<Ctl*>(take(sizeof(Ctl)));
+    return w;
+}
+
+// One level of the large phase on the tasks in w.lists[level & 1], whose
+// count is ctl->n_large[level & 1] on the device.  chunk_grid / task_blocks:
+// exact grids when the host knows the count, fixed ones otherwise (the
+// kernels loop over whatever the count holds).
+void enqueue_large_level(const SahWs& w, uint32_t level, int nb, uint32_t base, uint32_t leaf_size, Node* nodes,
+                         uint32_t chunk_grid, uint32_t task_blocks, cudaStream_t s)
+{
+    const Task* proc = w.lists[level & 1];
+    Task* outl = w.lists[(level + 1) & 1];
+    const uint32_t* ntp = &w.ctl->n_large[level & 1];
+    uint32_t* next = &w.ctl->n_large[(level + 1) & 1];
+    k_large_zero<<<task_blocks, 256, 0, s>>>(w.bins, ntp, nb);
+    k_large_prep<<<1, 1024, 0, s>>>(proc, ntp, next, nb, w.split, w.chunk_start);
+    k_large_bin<<<chunk_grid, 256, 0, s>>>(proc, ntp, w.split, w.chunk_start, w.ids_a, w.ids_b, w.tb, nb, w.bins);
+    k_large_split<<<task_blocks, 128, 0, s>>>(proc, ntp, w.split, w.bins, nb, base, leaf_size, nodes, outl, next,
+                                              w.small, w.leaves, w.ctl);
+    k_large_count<<<chunk_grid, 256, 0, s>>>(proc, ntp, w.split, w.chunk_start, w.ids_a, w.ids_b, w.tb, nb,
+                                             w.chunk_left);
+    k_large_scan<<<task_blocks, 128, 0, s>>>(w.split, ntp, w.chunk_start, w.chunk_left);
+    k_large_scatter<<<chunk_grid, 256, 0, s>>>(proc, ntp, w.split, w.chunk_start, w.ids_a, w.ids_b, w.tb, nb,
+                                               w.chunk_left);
+}
+
+// ---------------------------------------------------------------------------
+// batch: many meshes in one build
+
+// Boxes, ids and every mesh's root boxes (order-preserving words, 12 per
+// mesh at a stride of 16): triangle i belongs to the mesh m with
+// off[m] <= i < off[m + 1]; lanes of one mesh merge through the warp before
+// one atomic per word.
+__global__ void __launch_bounds__(256) k_sah_setup_seg(const float* __restrict__ tris, uint32_t n,
+                                                       const uint32_t* __restrict__ off, uint32_t M,
+                                                       float4* __restrict__ tb, uint32_t* __restrict__ ids,
+                                                       uint32_t* __restrict__ root_ord)
+{
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const bool valid = i < n;
+        uint32_t m = 0xFFFFFFFFu;
+        uint32_t e[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) e[k] = 0u;
+        if (valid) {
+            uint32_t lo = 0, hi = M;  // largest m with off[m] <= i
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (__ldg(off + mid) <= i) lo = mid; else hi = mid;
+            }
+            m = lo;
+            float t[9];
+            load_tri(tris, i, t);
+            const Box b = tri_box(t);
+            tb[2ull * i] = make_float4(b.mn[0], b.mn[1], b.mn[2], 0.0f);
+            tb[2ull * i + 1] = make_float4(b.mx[0], b.mx[1], b.mx[2], 0.0f);
+            ids[i] = i;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float c = (b.mn[k] + b.mx[k]) * 0.5f;
+                e[k] = float_to_ordered(-b.mn[k]);
+                e[3 + k] = float_to_ordered(b.mx[k]);
+                e[6 + k] = float_to_ordered(-c);
+                e[9 + k] = float_to_ordered(c);
+            }
+        }
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, m);
+#pragma unroll
+        for (int k = 0; k < 12; ++k) e[k] = __reduce_max_sync(peers, e[k]);
+        if (valid && (threadIdx.x & 31) == (uint32_t)(__ffs(peers) - 1))
+            for (int k = 0; k < 12; ++k) atomicMax(root_ord + 16ull * m + k, e[k]);
+    }
+}
+
+// One root task per mesh: triangles [off[m], off[m + 1]), record root0 + m.
+__global__ void k_root_tasks_seg(const uint32_t* __restrict__ root_ord, const uint32_t* __restrict__ off, uint32_t M,
+                                 uint32_t leaf_size, uint32_t root0, Task* large, Task* small, LeafRange* leaves,
+                                 Ctl* ctl)
+{
+    for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
+        Task t;
+        t.begin = off[m];
+        t.count = off[m + 1] - off[m];
+        t.slot = root0 + m;
+        t.flags = 2u;
+        const uint32_t* ro = root_ord + 16ull * m;
+        for (int k = 0; k < 3; ++k) {
+            if (t.count) {
+                t.pmn[k] = dec_neg(ro[k]);
+                t.pmx[k] = dec_pos(ro[3 + k]);
+                t.cmn[k] = dec_neg(ro[6 + k]);
+                t.cmx[k] = dec_pos(ro[9 + k]);
+            } else {
+                t.pmn[k] = t.cmn[k] = FLT_MAX;
+                t.pmx[k] = t.cmx[k] = -FLT_MAX;
+            }
+        }
+        classify(t, leaf_size, large, &ctl->n_large[0], small, leaves, ctl);
+    }
+}
+
 }  // namespace
 
 namespace sqk {
 
-size_t sah_workspace_bytes(uint32_t n)
-{
-    const size_t tasks = n / kSmall + 2;
-    size_t b = 0;
-    b += sizeof(float4) * 2ull * n;            // triangle boxes
-    b += sizeof(uint32_t) * 2ull * n;          // ids A/B
-    b += sizeof(Task) * 2 * tasks;             // large lists (cur/next)
-    b += sizeof(Task) * ((size_t)n / 2 + 2);   // small list
-    b += sizeof(LeafRange) * ((size_t)n + 66); // leaf list (+64 empty grid cells)
-    b += sizeof(Split) * tasks;
-    b += sizeof(uint32_t) * (tasks + 1);       // chunk starts
-    b += sizeof(uint32_t) * ((size_t)n / kChunk + tasks + 1);  // chunk left counts
-    b += sizeof(uint32_t) * (size_t)kMaxBins * kBinWords * tasks;  // bins
-    b += sizeof(uint32_t) * 64 * kBinWords + 64 * 4 + 64;         // grid cells, hist, root
-    b += sizeof(Ctl) + 4096;
-    return b;
-}
+size_t sah_workspace_bytes(uint32_t n) { return sah_ws_bytes(n, 0); }
+size_t sah_batch_workspace_bytes(uint32_t n, uint32_t meshes) { return sah_ws_bytes(n, meshes); }
 
 // Builds a SAH (grid = 0) or grid (grid = 1) BVH.  ws: workspace of
 // sah_workspace_bytes(n) bytes; keys/vals/alt: 4n-word sort buffers (grid
@@ -872,72 +1063,79 @@ int build_sah(const float* tris, uint32_t n, uint32_t nb, uint32_t leaf_size, in
               uint32_t* sort_alt_keys, uint32_t* sort_alt_vals, uint32_t* sort_lookback, uint32_t* sort_counters,
               uint32_t* err, uint32_t* host_ctl, cudaStream_t s)
 {
-    const size_t tasks = n / kSmall + 2;
-    char* p = static_cast<char*>(ws);
-    auto take = [&](size_t bytes) { char* r = p; p += (bytes + 255) / 256 * 256; return r; };
-    float4* tb = reinterpret_cast<float4*>(take(sizeof(float4) * 2ull * n));
-    uint32_t* ids_a = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * (size_t)n));
-    uint32_t* ids_b = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * (size_t)n));
-    Task* lcur = reinterpret_cast<Task*>(take(sizeof(Task) * tasks));
-    Task* lnext = reinterpret_cast<Task*>(take(sizeof(Task) * tasks));
-    Task* small = reinterpret_cast<Task*>(take(sizeof(Task) * ((size_t)n / 2 + 2)));
-    LeafRange* leaves = reinterpret_cast<LeafRange*>(take(sizeof(LeafRange) * ((size_t)n + 66)));
-    Split* split = reinterpret_cast<Split*>(take(sizeof(Split) * tasks));
-    uint32_t* chunk_start = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * (tasks + 1)));
-    uint32_t* chunk_left = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * ((size_t)n / kChunk + tasks + 1)));
-    uint32_t* bins = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * (size_t)kMaxBins * kBinWords * tasks));
-    uint32_t* cells = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * 64 * kBinWords));
-    uint32_t* hist = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * 64));
-    uint32_t* root_ord = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * 16));
-    Ctl* ctl = reinterpret_cast<Ctl*>(take(sizeof(Ctl)));
+    const SahWs w = carve(ws, n, 0);
     const uint32_t base = grid ? 128u : 0u;
     const uint32_t leaf0 = base + 2u * n + 2u;
     cudaError_t e;
 #define SQ_TRY(x) do { if ((e = (x)) != cudaSuccess) return (int)e; } while (0)
-    SQ_TRY(cudaMemsetAsync(cells, 0, sizeof(uint32_t) * 64 * kBinWords, s));
-    SQ_TRY(cudaMemsetAsync(hist, 0, sizeof(uint32_t) * 64, s));
-    SQ_TRY(cudaMemsetAsync(root_ord, 0, sizeof(uint32_t) * 16, s));
-    SQ_TRY(cudaMemsetAsync(ctl, 0, sizeof(Ctl), s));
+    SQ_TRY(cudaMemsetAsync(w.cells, 0, sizeof(uint32_t) * 64 * kBinWords, s));
+    SQ_TRY(cudaMemsetAsync(w.hist, 0, sizeof(uint32_t) * 64, s));
+    SQ_TRY(cudaMemsetAsync(w.root_ord, 0, sizeof(uint32_t) * 16, s));
+    SQ_TRY(cudaMemsetAsync(w.ctl, 0, sizeof(Ctl), s));
     const uint32_t g = min((n + 255) / 256, (uint32_t)sms() * 8u);
-    k_sah_setup<<<g, 256, 0, s>>>(tris, n, tb, ids_a, root_ord);
-    Task* proc = lcur;  // large tasks of the current level
-    Task* outl = lnext; // their large children
+    k_sah_setup<<<g, 256, 0, s>>>(tris, n, w.tb, w.ids_a, w.root_ord);
     if (!grid) {
-        k_root_task<<<1, 1, 0, s>>>(root_ord, n, leaf_size, proc, small, leaves, ctl, scene_out);
+        k_root_task<<<1, 1, 0, s>>>(w.root_ord, n, leaf_size, w.lists[0], w.small, w.leaves, w.ctl, scene_out);
     } else {
         // bin into 64 cells keyed by Morton slot, then stable sort by slot
-        k_grid_bin<<<g, 256, 0, s>>>(tb, n, root_ord, sort_keys, cells, hist);
-        SQ_TRY(cudaMemcpyAsync(sort_vals, ids_a, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToDevice, s));
-        const int which = sort_passes(sort_keys, sort_vals, sort_alt_keys, sort_alt_vals, n, hist, sort_lookback,
+        k_grid_bin<<<g, 256, 0, s>>>(w.tb, n, w.root_ord, sort_keys, w.cells, w.hist);
+        SQ_TRY(cudaMemcpyAsync(sort_vals, w.ids_a, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToDevice, s));
+        const int which = sort_passes(sort_keys, sort_vals, sort_alt_keys, sort_alt_vals, n, w.hist, sort_lookback,
                                       sort_counters, 6, 1, err, s);
-        SQ_TRY(cudaMemcpyAsync(ids_a, which ? sort_alt_vals : sort_vals, sizeof(uint32_t) * (size_t)n,
+        SQ_TRY(cudaMemcpyAsync(w.ids_a, which ? sort_alt_vals : sort_vals, sizeof(uint32_t) * (size_t)n,
                                cudaMemcpyDeviceToDevice, s));
-        k_grid_tasks<<<1, 64, 0, s>>>(cells, root_ord, n, leaf_size, scene_box_cells, proc, small, leaves, ctl,
-                                      scene_out);
+        k_grid_tasks<<<1, 64, 0, s>>>(w.cells, w.root_ord, n, leaf_size, scene_box_cells, w.lists[0], w.small,
+                                      w.leaves, w.ctl, scene_out);
     }
-    // large phase, one level per iteration (the host reads the task count)
-    for (;;) {
-        SQ_TRY(cudaMemcpyAsync(host_ctl, ctl, sizeof(uint32_t) * 4, cudaMemcpyDeviceToHost, s));
+    // large phase, one level per iteration; the host reads the level's task
+    // count to size the grids and to stop
+    for (uint32_t level = 0;; ++level) {
+        SQ_TRY(cudaMemcpyAsync(host_ctl, &w.ctl->n_large[level & 1], sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
         SQ_TRY(cudaStreamSynchronize(s));
         const uint32_t nt = host_ctl[0];
         if (nt == 0) break;
-        SQ_TRY(cudaMemsetAsync(&ctl->n_large_next, 0, sizeof(uint32_t), s));
-        SQ_TRY(cudaMemsetAsync(bins, 0, sizeof(uint32_t) * (size_t)kMaxBins * kBinWords * nt, s));
-        k_large_prep<<<1, 1024, 0, s>>>(proc, nt, (int)nb, split, chunk_start);
         const uint32_t max_chunks = (uint32_t)((size_t)n / kChunk + nt + 1);
-        k_large_bin<<<max_chunks, 256, 0, s>>>(proc, nt, split, chunk_start, ids_a, ids_b, tb, (int)nb, bins);
-        k_large_split<<<(nt + 3) / 4, 128, 0, s>>>(proc, nt, split, bins, (int)nb, base, leaf_size, nodes, outl, small,
-                                                   leaves, ctl);
-        k_large_count<<<max_chunks, 256, 0, s>>>(proc, nt, split, chunk_start, ids_a, ids_b, tb, (int)nb, chunk_left);
-        k_large_scan<<<(nt + 3) / 4, 128, 0, s>>>(split, nt, chunk_start, chunk_left);
-        k_large_scatter<<<max_chunks, 256, 0, s>>>(proc, nt, split, chunk_start, ids_a, ids_b, tb, (int)nb, chunk_left);
-        std::swap(proc, outl);
+        enqueue_large_level(w, level, (int)nb, base, leaf_size, nodes, max_chunks, (nt + 3) / 4, s);
     }
     // small phase and leaves
     const uint32_t sg = (uint32_t)sms() * 8u;
-    k_small<<<sg, 128, 0, s>>>(small, ctl, ids_a, ids_b, tb, (int)nb, leaf_size, base, nodes, leaf0, err);
-    k_emit_leaves<<<sg, 256, 0, s>>>(leaves, ctl, ids_a, ids_b, tb, nodes, leaf0, err);
+    k_small<<<sg, 128, 0, s>>>(w.small, w.ctl, w.ids_a, w.ids_b, w.tb, (int)nb, leaf_size, base, nodes, leaf0, err);
+    k_emit_leaves<<<sg, 256, 0, s>>>(w.leaves, w.ctl, w.ids_a, w.ids_b, w.tb, nodes, leaf0, err);
     if (grid) k_grid_heap<<<1, 32, 0, s>>>(nodes);
+    return (int)cudaGetLastError();
+#undef SQ_TRY
+}
+
+// Binned SAH trees of M meshes at once, with no host synchronisation (a
+// fixed number of large-phase levels with device-side task counts, so the
+// sequence can be captured in a CUDA graph).  Mesh m holds triangles
+// [off[m], off[m + 1]) of the concatenated `tris` (off on the device, M + 1
+// words); its root is record root0 + m, inner records at 2q and 2q + 1 for a
+// split at q, leaf records at 2n + 2 + position -- the layout of a single
+// build, shifted by the mesh's offset.  Large tasks left after the last
+// fixed level go to the small phase (same splits, one warp per subtree).
+int build_sah_batch(const float* tris, uint32_t n, const uint32_t* off, uint32_t M, uint32_t nb, uint32_t leaf_size,
+                    uint32_t root0, sq::Node* nodes, void* ws, uint32_t* err, cudaStream_t s)
+{
+    const SahWs w = carve(ws, n, M);
+    const uint32_t leaf0 = 2u * n + 2u;
+    cudaError_t e;
+#define SQ_TRY(x) do { if ((e = (x)) != cudaSuccess) return (int)e; } while (0)
+    SQ_TRY(cudaMemsetAsync(w.root_ord, 0, sizeof(uint32_t) * 16ull * M, s));
+    SQ_TRY(cudaMemsetAsync(w.ctl, 0, sizeof(Ctl), s));
+    const uint32_t sm = (uint32_t)sms();
+    if (n > 0) {
+        const uint32_t g = min((n + 255) / 256, sm * 8u);
+        k_sah_setup_seg<<<g, 256, 0, s>>>(tris, n, off, M, w.tb, w.ids_a, w.root_ord);
+    }
+    k_root_tasks_seg<<<(M + 127) / 128, 128, 0, s>>>(w.root_ord, off, M, leaf_size, root0, w.lists[0], w.small,
+                                                      w.leaves, w.ctl);
+    for (uint32_t level = 0; level < kBatchLargeLevels; ++level)
+        enqueue_large_level(w, level, (int)nb, 0u, leaf_size, nodes, sm * 8u, sm * 8u, s);
+    k_large_to_small<<<sm, 256, 0, s>>>(w.lists[kBatchLargeLevels & 1], &w.ctl->n_large[kBatchLargeLevels & 1],
+                                       w.small, w.ctl);
+    k_small<<<sm * 8u, 128, 0, s>>>(w.small, w.ctl, w.ids_a, w.ids_b, w.tb, (int)nb, leaf_size, 0u, nodes, leaf0, err);
+    k_emit_leaves<<<sm * 8u, 256, 0, s>>>(w.leaves, w.ctl, w.ids_a, w.ids_b, w.tb, nodes, leaf0, err);
     return (int)cudaGetLastError();
 #undef SQ_TRY
 }

@@ -741,20 +741,139 @@ __global__ void __launch_bounds__(256) k_trace_batch(const sqk::BatchTraceArgs a
     if (a.stats) ws.flush(lane, a.stats);
 }
 
+// Batched trace with per-lane ray refill (closest / any-hit): as
+// k_trace_refill over the job table's ray slots (slot g: lane g mod 32 of
+// the job's 32-ray batch g / 32); a lane keeps its current job's batch range
+// and searches the table only when a slot leaves it.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_trace_batch_refill(const sqk::BatchTraceArgs a)
+{
+    constexpr bool ANY = MODE == SQ_TRACE_ANYHIT;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t total = a.total_batches * 32u;
+    uint32_t st_node[kStack];
+    float st_tn[kStack];
+    Lane2 L;
+    L.cur = kNoHit;
+    bool has = false, exhausted = false, explicit_rays = false;
+    uint32_t out = 0, tri_offset = 0;
+    uint32_t cj = 0, jlo = 1, jhi = 0;
+    unsigned long long s_bt = 0, s_tt = 0, s_by = 0;
+    for (;;) {
+        const uint32_t need = __ballot_sync(0xFFFFFFFFu, !has && !exhausted);
+        if (need) {
+            const uint32_t leader = __ffs(need) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(a.work, __popc(need));
+            base = __shfl_sync(0xFFFFFFFFu, base, leader);
+            if (!has && !exhausted) {
+                const uint32_t g = base + __popc(need & ((1u << lane) - 1u));
+                if (g >= total) {
+                    exhausted = true;
+                } else {
+                    const uint32_t b = g >> 5, l = g & 31u;
+                    if (b < jlo || b >= jhi) {
+                        cj = find_job(a.jobs, a.njobs, b);
+                        jlo = __ldg(&a.jobs[cj].batch_begin);
+                        jhi = cj + 1 < a.njobs ? __ldg(&a.jobs[cj + 1].batch_begin) : a.total_batches;
+                    }
+                    const sqk::BatchJob& job = a.jobs[cj];
+                    const uint32_t lb = b - jlo;
+                    Ray r;
+                    bool ok;
+                    uint32_t rid;
+                    explicit_rays = job.ray_kind == SQ_RAYS_EXPLICIT;
+                    if (!explicit_rays) {
+                        const uint32_t tiles_x = (job.width + 7u) >> 3;
+                        const uint32_t x = (lb % tiles_x) * 8u + (l & 7u);
+                        const uint32_t y = (lb / tiles_x) * 4u + (l >> 3);
+                        ok = x < job.width && y < job.height;
+                        rid = y * job.width + x;
+                        if (ok) {
+                            if (job.ray_kind == SQ_RAYS_REFERENCE_CAMERA) gen_reference_camera(x, y, job.width, job.height, job.cam, r);
+                            else gen_pinhole(x, y, job.width, job.height, job.cam, r);
+                        }
+                    } else {
+                        rid = lb * 32u + l;
+                        ok = rid < job.ray_count;
+                        if (ok) {
+                            const float4* p = reinterpret_cast<const float4*>(job.rays ? job.rays : a.rays) +
+                                              2ull * (job.ray_offset + rid);
+                            const float4 x0 = __ldg(p), x1 = __ldg(p + 1);
+                            r.o[0] = x0.x; r.o[1] = x0.y; r.o[2] = x0.z; r.tmin = x0.w;
+                            r.d[0] = x1.x; r.d[1] = x1.y; r.d[2] = x1.z; r.tmax = x1.w;
+                        }
+                    }
+                    if (ok) {
+                        out = job.out_offset + rid;
+                        tri_offset = job.tri_offset;
+                        lane2_start<ANY>(L, a.nodes, a.node_count, a.tri_count, job.root, a.tris, r);
+                        has = true;
+                    }
+                }
+            }
+        }
+        const uint32_t busy = __ballot_sync(0xFFFFFFFFu, has);
+        if (!busy) {
+            if (__all_sync(0xFFFFFFFFu, exhausted)) break;
+            continue;
+        }
+        if (has) {
+            if (L.cur != kNoHit) visit2<ANY>(L, a.nodes, a.node_count, a.tri_count, a.tris, st_node, st_tn);
+            if (L.cur == kNoHit) {
+                has = false;
+                Result res = lane2_result(L);
+                if (res.overflow) raise_error(a.err, SQ_DEVERR_STACK_OVERFLOW);
+                if (res.bad) raise_error(a.err, SQ_DEVERR_TOPOLOGY);
+                if (res.id != kNoHit) res.id -= tri_offset;
+                if (a.stats) {
+                    s_bt += res.tests;
+                    s_tt += res.tri_tests;
+                    s_by += (explicit_rays ? 32u : 0u) + (a.hits ? 12u : 0u) + (a.heat ? 3u : 0u) +
+                            32ull * res.tests + 36ull * res.tri_tests;
+                }
+                if (a.hits) {
+                    uint32_t* h = reinterpret_cast<uint32_t*>(a.hits) + 3ull * out;
+                    h[0] = res.id;
+                    h[1] = __float_as_uint(res.t);
+                    h[2] = res.tests;
+                }
+                if (a.heat) write_heat(a.heat + 3ull * out, (float)res.tests, a.heat_ramp);
+            }
+        }
+    }
+    if (a.stats) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            s_bt += __shfl_xor_sync(0xFFFFFFFFu, s_bt, o);
+            s_tt += __shfl_xor_sync(0xFFFFFFFFu, s_tt, o);
+            s_by += __shfl_xor_sync(0xFFFFFFFFu, s_by, o);
+        }
+        if (lane == 0) {
+            atomicAdd(a.stats, s_bt); atomicAdd(a.stats + 1, s_tt); atomicAdd(a.stats + 2, s_by); atomicAdd(a.stats + 3, s_bt);
+        }
+    }
+}
+
 template <int MODE>
 void launch_batch(const sqk::BatchTraceArgs& a, int block, cudaStream_t s)
 {
     if (a.total_batches == 0) return;
-    static PerDevice<std::array<int, 3>> cache;
-    const std::array<int, 3> per_sm = cache.get([] {
-        return std::array<int, 3>{blocks_per_sm(k_trace_batch<MODE>, 64), blocks_per_sm(k_trace_batch<MODE>, 128),
-                                  blocks_per_sm(k_trace_batch<MODE>, 256)};
+    constexpr int RM = MODE == SQ_TRACE_REF ? SQ_TRACE_CLOSEST : MODE;  // refill: closest / any-hit only
+    static PerDevice<std::array<int, 6>> cache;
+    const std::array<int, 6> per_sm = cache.get([] {
+        return std::array<int, 6>{blocks_per_sm(k_trace_batch<MODE>, 64), blocks_per_sm(k_trace_batch<MODE>, 128),
+                                  blocks_per_sm(k_trace_batch<MODE>, 256), blocks_per_sm(k_trace_batch_refill<RM>, 64),
+                                  blocks_per_sm(k_trace_batch_refill<RM>, 128),
+                                  blocks_per_sm(k_trace_batch_refill<RM>, 256)};
     });
+    const bool refill = a.refill && MODE != SQ_TRACE_REF;
     const int bi = block <= 64 ? 0 : (block <= 128 ? 1 : 2);
-    uint32_t grid = (uint32_t)(per_sm[bi] * sm_count());
+    uint32_t grid = (uint32_t)(per_sm[(refill ? 3 : 0) + bi] * sm_count());
     const uint32_t need = (a.total_batches + (uint32_t)(block / 32) - 1) / (uint32_t)(block / 32);
     if (grid > need) grid = need;
-    k_trace_batch<MODE><<<grid, block, 0, s>>>(a);
+    if (refill) k_trace_batch_refill<RM><<<grid, block, 0, s>>>(a);
+    else k_trace_batch<MODE><<<grid, block, 0, s>>>(a);
 }
 
 }  // namespace

@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol(lib_built):
 def test_abi_version(lib_built):
     lib = ctypes.CDLL(lib_built)
     lib.sq_abi_version.restype = ctypes.c_uint32
-    assert lib.sq_abi_version() == 1
+    assert lib.sq_abi_version() == 2
 
 
 def test_struct_sizes():
