@@ -507,8 +507,74 @@ def coherent_leg(ctx, flush, torch, scenes_by_name):
     return out
 
 
+# Small fixed workloads, one kernel family each, for ncu captures (inputs
+# larger than L2 where the configuration allows, a few GB on the device at
+# most).  Each runs its work twice (a warm-up, then the captured run).
+PROFILE_CASES = ("trace_binary", "trace8_refill", "sah", "grid", "coherent", "batch", "lbvh8m")
+
+
+def run_case(name):
+    import torch
+    import sequoia_gb300 as sq
+    from sequoia_gb300 import scenes
+    ctx = sq.Context(0)
+    w = WORKLOAD
+    cam = dict(camera="pinhole", width=w["width"], height=w["height"], origin=w["eye"], target=w["target"],
+               up=w["up"], vfov=w["vfov"])
+    soup = torch.from_numpy(make_scene()).cuda() if name != "lbvh8m" else None
+    for _ in range(2):
+        if name == "trace_binary":     # k_trace<closest>: FP32 binary BVH, 3840x2160 camera rays
+            bvh = ctx.build(soup, "morton")
+            hits = torch.empty(w["width"] * w["height"] * 3, dtype=torch.int32, device="cuda")
+            ctx.trace(bvh, "closest", hits=hits, **cam)
+        elif name == "trace8_refill":  # k_trace8_refill: 2^22 incoherent rays on the 8-wide BVH
+            bvh = ctx.build(soup, "morton", wide=True)
+            lo, hi = scenes.scene_box(make_scene())
+            rays = torch.from_numpy(scenes.random_rays(1 << 22, lo, hi, seed=5)).cuda()
+            hits = torch.empty((1 << 22) * 3, dtype=torch.int32, device="cuda")
+            ctx.trace(bvh, "closest", rays=rays, hits=hits)
+        elif name == "sah":            # binned SAH, 32 bins, 2M soup
+            bvh = ctx.build(soup, "sah", bins=32, leaf=8)
+        elif name == "grid":           # grid builder, 2M soup
+            bvh = ctx.build(soup, "grid", bins=8, leaf=8)
+        elif name == "coherent":       # trace_packet<8>, trace_bundle<64> on the 8-bin SAH tree, 1920x1080
+            bvh = ctx.build(soup, "sah", bins=8, leaf=8)
+            v = make_scene().reshape(-1, 3)
+            lo, hi = v.min(0), v.max(0)
+            c = (lo + hi) * np.float32(0.5)
+            org = (float(c[0]), float(c[1]), float(np.float32(2) * lo[2] - c[2]))
+            heat = torch.empty(1920 * 1080 * 3, dtype=torch.uint8, device="cuda")
+            for mode, k in (("packet", 8), ("bundle", 64)):
+                ctx.trace(bvh, mode, k=k, camera="reference", width=1920, height=1080, origin=org, heatmap=heat)
+        elif name == "batch":          # 64 meshes, Morton + 8-wide, one graph launch
+            meshes, tiles = scenes.mesh_batch(64, seed=4000)
+            descs = []
+            for m, side in zip(meshes, tiles):
+                lo, hi = scenes.scene_box(m)
+                cc = (lo + hi) * 0.5
+                ext = float(max(hi - lo))
+                descs.append(dict(tris=torch.from_numpy(m).cuda(), camera="pinhole", width=int(side), height=int(side),
+                                  origin=(float(cc[0]), float(cc[1]) + 0.5 * ext, float(cc[2]) - 2.5 * ext),
+                                  target=tuple(float(x) for x in cc), up=(0.0, 1.0, 0.0), vfov=50.0))
+            b = ctx.batch(descs, mode="closest", wide=True, graph=True)
+            b.run(hits=False)
+            b.free()
+            bvh = None
+        elif name == "lbvh8m":         # Morton LBVH of the 8M soup (256 clusters)
+            t8 = torch.from_numpy(scenes.gaussian_soup(8_000_000, 256, seed=5)).cuda()
+            bvh = ctx.build(t8, "morton")
+        else:
+            raise SystemExit("unknown case %s (one of %s)" % (name, ", ".join(PROFILE_CASES)))
+        if bvh is not None:
+            ctx.sync()
+            bvh.free()
+    print("case %s ok: %s" % (name, json.dumps(ctx.timings())), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--case", choices=PROFILE_CASES, help="run one small profiling workload and exit")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
@@ -518,6 +584,9 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the comparison legs (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.case:
+        run_case(args.case)
+        return
     if args.impl == "reference":
         run_reference(args)
         return
