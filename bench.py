@@ -73,7 +73,7 @@ CONFIG = {"workload": "soup_2m: 2,000,000-triangle 64-cluster Gaussian soup, 384
 BATCH_BUILDERS = ("morton", "sah")
 LBVH_KERNELS = 8  # scene bounds, Morton codes, 4 onesweep passes, climb (local + global phase)
 TRACE_PROFILE = os.path.join(ROOT, "profiles", "k_trace8_tiles_soup2m.md")
-TRACE_SOURCE = os.path.join(ROOT, "sequoia_gb300", "csrc", "sq_bvh8.cu")
+TRACE_SOURCE = os.path.join(ROOT, "sequoia_gb300", "csrc", "sq_bvh8_trace.cu")
 
 
 def measured_peaks():

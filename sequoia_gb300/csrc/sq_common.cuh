@@ -379,7 +379,7 @@ void trace(const TraceArgs& a, cudaStream_t s);
 bool coherent_shape_ok(uint32_t bundle, uint32_t k, uint32_t w, uint32_t h);
 void trace_coherent(const TraceArgs& a, uint32_t bundle, uint32_t k, cudaStream_t s);
 
-// 8-wide quantised BVH (sq_bvh8.cu)
+// 8-wide quantised BVH (build: sq_bvh8.cu; traversal: sq_bvh8_trace.cu)
 struct Trace8Args {
     const void* nodes;     // 80-byte wide nodes
     const float4* tris8;   // 48-byte triangles in leaf order, id in v0.w
@@ -418,7 +418,7 @@ int build_bvh8(const sq::Node* rec, uint32_t root, uint32_t leaf0, const float* 
                const BarrierStall* stall = nullptr);
 void trace8(const Trace8Args& a, cudaStream_t s);
 
-// batched trace over many BVHs and ray tiles (sq_trace.cu, sq_bvh8.cu)
+// batched trace over many BVHs and ray tiles (sq_trace.cu, sq_bvh8_trace.cu)
 struct BatchJob {
     uint32_t ray_kind;     // sq_ray_kind
     uint32_t width, height;
@@ -448,7 +448,7 @@ struct BatchTraceArgs {
     uint32_t* work;
     uint32_t* err;
     unsigned long long* stats;
-    uint32_t refill;       // 8-wide kernel: 1 = per-lane ray refill (see sq_bvh8.cu)
+    uint32_t refill;       // 8-wide kernel: 1 = per-lane ray refill (see sq_bvh8_trace.cu)
     uint32_t heat_ramp;    // heatmap pixels: 0 = grey, 1 = colour ramp (write_heat)
 };
 void trace_batch(const BatchTraceArgs& a, int block_threads, cudaStream_t s);
