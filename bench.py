@@ -91,22 +91,27 @@ def source_digest(path):
 
 
 def profiled_traffic():
-    """DRAM bytes per launch of the 8-wide trace kernel from the committed
-    ncu summary, with the source digest of the kernel it measured.  Returns
-    (bytes or None, note): None when the kernel source changed since."""
+    """DRAM and L2 bytes per launch of the 8-wide trace kernel and its
+    issue-slot use, from the committed ncu summary, with the source digest of
+    the kernel it measured.  Returns (dict or None, note): None when the
+    kernel source changed since the capture."""
     try:
         with open(TRACE_PROFILE) as fh:
             text = fh.read()
     except OSError:
         return None, "no ncu summary committed"
     m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", text)
+    l2 = re.search(r"l2_bytes_per_launch:\s*([0-9.eE+]+)", text)
+    iss = re.search(r"issue slots busy[^|]*\|\s*([0-9.]+)%", text)
     d = re.search(r"kernel_source_sha256_16:\s*([0-9a-f]{16})", text)
     if not m or not d:
         return None, "ncu summary has no traffic line"
     if d.group(1) != source_digest(TRACE_SOURCE):
         return None, "stale: the kernel source changed after the ncu capture"
-    return float(m.group(1)), "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch, same kernel source " \
-                              "(%s)" % os.path.relpath(TRACE_PROFILE, ROOT)
+    out = {"dram": float(m.group(1)), "l2": float(l2.group(1)) if l2 else None,
+           "issue_frac": float(iss.group(1)) / 100.0 if iss else None}
+    return out, "ncu dram__bytes_read.sum + dram__bytes_write.sum and lts__t_bytes.sum, one launch, same kernel " \
+                "source (%s)" % os.path.relpath(TRACE_PROFILE, ROOT)
 
 
 class ClockSampler:
@@ -705,7 +710,7 @@ def main():
     lbvh_ms = b_ms - statistics.mean(wide_ms)
     build_gbs = n * (200 + 16 * 4) / (lbvh_ms / 1e3) / 1e9
     hits_np = d_hits.view(-1, 3).cpu().numpy()
-    traffic, traffic_note = profiled_traffic()
+    prof, traffic_note = profiled_traffic()
 
     cpu = None
     if not args.no_cpu_baseline:
@@ -732,8 +737,12 @@ def main():
         "hit_rays": int((hits_np[:, 0] != -1).sum()),
         "roofline": {"bound": "hbm", "kernel": "k_trace8_tiles<closest>", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-                     "traffic": traffic, "traffic_source": traffic_note,
-                     "dram_frac": (traffic / (tr_ms / 1e3) / 1e9 / peak) if traffic else None,
+                     "traffic": prof["dram"] if prof else None, "traffic_source": traffic_note,
+                     "dram_frac": (prof["dram"] / (tr_ms / 1e3) / 1e9 / peak) if prof else None,
+                     "l2": ({"bytes": prof["l2"], "achieved_gbs": prof["l2"] / (tr_ms / 1e3) / 1e9}
+                            if prof and prof["l2"] else None),
+                     "issue": ({"slots_busy_frac": prof["issue_frac"], "source": "ncu sm__inst_executed, % of peak "
+                                "sustained, same capture"} if prof and prof["issue_frac"] else None),
                      "bytes_model": "kernel-counted requested bytes: 80 B per wide node loaded, 48 B per "
                                     "triangle tested, 15 B of outputs per ray",
                      "limiter": "instruction issue (ALU pipe), not HBM: the tree stays in L2 and L1, so DRAM "

@@ -410,7 +410,8 @@ sq_status sq_last_trace_stats(sq_ctx* ctx, uint64_t stats[4]);
  * one use on this context, then clears itself:
  *   SQ_DEBUG_STALL_LOOKBACK  the next sq_radix_sort_pairs, which must be a
  *                            one-pass sort (key_bits <= digit_bits) of more
- *                            than 4096 keys, runs without its first tile: the
+ *                            than one tile (16384 keys; 4096 with 10-bit
+ *                            digits), runs without its first tile: the
  *                            look-back of the tiles after it waits on words
  *                            that nothing publishes, gives up after `limit`
  *                            polls and raises SQ_DEVERR_LOOKBACK_TIMEOUT.

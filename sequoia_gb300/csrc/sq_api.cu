@@ -210,9 +210,11 @@ sq_status build_morton(sq_ctx* c, sq_bvh* b, const sq_build_params& p)
     if (passes % 2 == 0) { ka = b->codes; va = b->perm; kb = alt; vb = alt + n; }
     else { ka = alt; va = alt + n; kb = b->codes; vb = b->perm; }
     sqk::scene_bounds(b->tris, n, p.morton_bounds, zero + z_box, s);
-    sqk::morton_codes(b->tris, n, p.morton_bounds, zero + z_box, ka, va, zero + z_hist, db, passes, s);
+    // the values are the triangle numbers: the sort's first pass generates
+    // them instead of reading them
+    sqk::morton_codes(b->tris, n, p.morton_bounds, zero + z_box, ka, nullptr, zero + z_hist, db, passes, s);
     SQ_CUDA(c, cudaEventRecord(c->ev[1], s));
-    sqk::sort_passes(ka, va, kb, vb, n, zero + z_hist, zero + z_lb, zero + z_ctr, db, passes, err, s);
+    sqk::sort_passes(ka, va, kb, vb, n, zero + z_hist, zero + z_lb, zero + z_ctr, db, passes, err, s, nullptr, true);
     SQ_CUDA(c, cudaEventRecord(c->ev[2], s));
     // the sort's second buffer is free now: it lists the climb's open nodes;
     // box_ord leaves words 6 and 7 of the zeroed region for their count
@@ -642,8 +644,8 @@ sq_status sq_radix_sort_pairs(sq_ctx* c, const uint32_t* keys_in, const uint32_t
     sqk::SortStall stall{c->stall_lookback ? c->stall_lookback - 1u : 0u};
     const bool stalled = c->stall_lookback != 0;
     c->stall_lookback = 0;
-    if (stalled && (passes != 1 || n <= 4096))
-        return fail(c, SQ_ERR_INVALID, "look-back stall injection needs a one-pass sort of more than 4096 keys");
+    if (stalled && (passes != 1 || n <= sqk::sort_tile_keys(n, digit_bits)))
+        return fail(c, SQ_ERR_INVALID, "look-back stall injection needs a one-pass sort of two tiles or more");
     uint32_t* zero = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * z_words));
     uint32_t* buf = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * 4ull * n));
     if (!zero || !buf) { dfree(c, zero); dfree(c, buf); return fail(c, SQ_ERR_OOM, "allocation failed"); }

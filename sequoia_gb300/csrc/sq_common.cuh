@@ -320,6 +320,8 @@ void lbvh_climb64(const uint64_t* codes, const uint32_t* perm, const float* tris
                   cudaStream_t s);
 
 // onesweep radix sort (sq_sort.cu)
+// keys per tile of a pass over n keys (4096, 8192 or 16384)
+uint32_t sort_tile_keys(uint32_t n, uint32_t digit_bits);
 size_t sort_lookback_words(uint32_t n, uint32_t digit_bits, uint32_t passes);
 void sort_histogram(const uint32_t* keys, uint32_t n, uint32_t* hist, uint32_t digit_bits, uint32_t passes,
                     cudaStream_t s);
@@ -333,11 +335,14 @@ struct SortStall {
     uint32_t spin_limit;
 };
 // Runs `passes` onesweep passes; hist/lookback/counters must be zeroed
-// before (lookback and counters) and filled (hist).  Returns which buffer
-// holds the result: 0 = (keys_a, vals_a), 1 = (keys_b, vals_b).
+// before (lookback and counters) and filled (hist).  With iota_values the
+// first pass takes each key's index as its value and vals_a is not read.
+// Returns which buffer holds the result: 0 = (keys_a, vals_a),
+// 1 = (keys_b, vals_b).
 int sort_passes(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b, uint32_t* vals_b, uint32_t n,
                 const uint32_t* hist, uint32_t* lookback, uint32_t* counters, uint32_t digit_bits,
-                uint32_t passes, uint32_t* err, cudaStream_t s, const SortStall* stall = nullptr);
+                uint32_t passes, uint32_t* err, cudaStream_t s, const SortStall* stall = nullptr,
+                bool iota_values = false);
 
 // binned SAH / grid builders (sq_sah.cu)
 size_t sah_workspace_bytes(uint32_t n);

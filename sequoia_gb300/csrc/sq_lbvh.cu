@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(256) k_morton(const float* __restrict__ tris, 
             const uint32_t code = spread10(q[0]) | (spread10(q[1]) << 1) | (spread10(q[2]) << 2);
             const uint32_t i = first + threadIdx.x;
             keys[i] = code;
-            vals[i] = i;
+            if (vals) vals[i] = i;  // null when the sort's first pass generates the indices
 #pragma unroll
             for (int p = 0; p < PASSES; ++p) atomicAdd(&s_hist[p * RADIX + ((code >> (p * DB)) & (RADIX - 1))], 1u);
         }

@@ -25,7 +25,7 @@
 namespace {
 
 constexpr uint32_t kMaxKeys = SQ_NOALLOC_MAX_KEYS;
-constexpr uint32_t kTileKeys = 4096;  // keys per onesweep tile (sq_sort.cu)
+constexpr uint32_t kTileKeys = 4096;  // the smallest onesweep tile (sq_sort.cu): bounds the tile count
 constexpr uint32_t kMaxTiles = (kMaxKeys + kTileKeys - 1) / kTileKeys;
 // largest (passes x radix) over the supported digit widths for 32-bit keys:
 // 6 bits: 6 x 64, 8 bits: 4 x 256, 10 bits: 4 x 1024

@@ -8,6 +8,11 @@
 // Morton kernel for builds); then one kernel per digit:
 //   - a block takes the next tile from an atomic counter, so tiles are
 //     processed in order and a tile's predecessors are always running;
+//   - a tile is 16 keys per thread of a 256-, 512- or 1024-thread block:
+//     the look-back below is a chain over the tiles, so the largest tiles
+//     that still fill the GPU are the fastest (1024 threads while all tiles
+//     fit one block per SM, 512 beyond that; 256 for 10-bit digits, whose
+//     per-warp digit counts fill shared memory);
 //   - warps rank their keys by digit (stable: items are ranked in index
 //     order within the warp, warps in index order within the tile); the lanes
 //     sharing a digit come from one ballot per digit bit, which costs the
@@ -24,21 +29,19 @@ namespace {
 
 using namespace sq;
 
-constexpr int kBlock = 256;
 constexpr int kItems = 16;
-constexpr int kTile = kBlock * kItems;
-constexpr int kWarps = kBlock / 32;
 constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagInc = 2u << 30;
 constexpr uint32_t kCountMask = (1u << 30) - 1u;
 constexpr uint32_t kSpinLimit = 1u << 22;
 constexpr int kWindow = 8;  // look-back words loaded per round
 
-template <int RADIX>
+template <int RADIX, int BLOCK>
 __device__ __forceinline__ void block_exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t* s_tmp)
 {
-    // RADIX values, kBlock threads; each thread owns a contiguous chunk.
-    constexpr int PER = (RADIX + kBlock - 1) / kBlock;
+    // RADIX values, BLOCK threads; each thread owns a contiguous chunk.
+    constexpr int kWarps = BLOCK / 32;
+    constexpr int PER = (RADIX + BLOCK - 1) / BLOCK;
     uint32_t v[PER];
     uint32_t sum = 0;
     const int t = threadIdx.x;
@@ -78,21 +81,25 @@ __device__ __forceinline__ void block_exclusive_scan(const uint32_t* in, uint32_
     __syncthreads();
 }
 
-template <int DB>
+template <int DB, int BLOCK>
 struct Smem {
     static constexpr int RADIX = 1 << DB;
-    static constexpr size_t bytes = sizeof(uint32_t) * (2 * kTile + kWarps * RADIX + 3 * RADIX + 32);
+    static constexpr size_t bytes = sizeof(uint32_t) * (2 * BLOCK * kItems + (BLOCK / 32) * RADIX + 3 * RADIX + 32);
 };
 
-template <int DB>
-__global__ void __launch_bounds__(kBlock, 4) k_onesweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+// 64 registers a thread at every block size (1024 / BLOCK blocks per SM).
+// iota: each key's value is its index (vin is not read), as in the first
+// pass of a build, whose values are the triangle numbers.
+template <int DB, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_onesweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
                                                      uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n,
                                                      uint32_t shift, const uint32_t* __restrict__ hist,
                                                      uint32_t* __restrict__ lookback, uint32_t* __restrict__ counter,
-                                                     uint32_t* err, uint32_t spin_limit, uint32_t tile_base)
+                                                     uint32_t* err, uint32_t spin_limit, uint32_t tile_base, bool iota)
 {
     constexpr int RADIX = 1 << DB;
     constexpr uint32_t MASK = RADIX - 1;
+    constexpr int kBlock = BLOCK, kWarps = BLOCK / 32, kTile = BLOCK * kItems;
     extern __shared__ __align__(16) uint32_t smem[];
     uint32_t* s_keys = smem;
     uint32_t* s_vals = s_keys + kTile;
@@ -158,8 +165,8 @@ __global__ void __launch_bounds__(kBlock, 4) k_onesweep(const uint32_t* __restri
         st_relaxed_u32(lookback + (size_t)tile * RADIX + d, (tile == 0 ? kFlagInc : kFlagAgg) | run);
     }
     __syncthreads();
-    block_exclusive_scan<RADIX>(hist, s_gbase, s_tmp);
-    block_exclusive_scan<RADIX>(s_bcount, s_lexcl, s_tmp);
+    block_exclusive_scan<RADIX, BLOCK>(hist, s_gbase, s_tmp);
+    block_exclusive_scan<RADIX, BLOCK>(s_bcount, s_lexcl, s_tmp);
     // decoupled look-back, one digit per thread (or several).  The words of
     // kWindow predecessors are loaded at once (independent relaxed loads, one
     // memory latency: each word carries its flag and count together, so no
@@ -206,7 +213,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_onesweep(const uint32_t* __restri
             const uint32_t d = (k[it] >> shift) & MASK;
             const uint32_t pos = s_lexcl[d] + wh[d] + rk[it];
             s_keys[pos] = k[it];
-            s_vals[pos] = vin[idx];
+            s_vals[pos] = iota ? idx : vin[idx];
         }
     }
     __syncthreads();
@@ -240,34 +247,48 @@ __global__ void __launch_bounds__(256) k_sort_hist(const uint32_t* __restrict__ 
     }
 }
 
-template <int DB>
+template <int DB, int BLOCK>
 void launch_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, uint32_t n, uint32_t shift,
                  const uint32_t* hist, uint32_t* lookback, uint32_t* counter, uint32_t* err, uint32_t spin_limit,
-                 uint32_t tile_base, cudaStream_t s)
+                 uint32_t tile_base, bool iota, cudaStream_t s)
 {
-    const size_t bytes = Smem<DB>::bytes;
+    constexpr size_t bytes = Smem<DB, BLOCK>::bytes;
+    static_assert(bytes <= 227 * 1024, "onesweep tile does not fit in shared memory");
     // the opt-in above 48 KB of dynamic shared memory is a per-device
     // attribute of the function: set it on each device's first use
     static PerDevice<bool> configured;
     configured.get([] {
-        cudaFuncSetAttribute(k_onesweep<DB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Smem<DB>::bytes);
+        cudaFuncSetAttribute(k_onesweep<DB, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
         return true;
     });
-    const uint32_t tiles = (n + kTile - 1) / kTile;
+    const uint32_t tiles = (n + BLOCK * kItems - 1) / (BLOCK * kItems);
     if (tiles <= tile_base) return;
-    k_onesweep<DB><<<tiles - tile_base, kBlock, bytes, s>>>(kin, vin, kout, vout, n, shift, hist, lookback, counter,
-                                                            err, spin_limit, tile_base);
+    k_onesweep<DB, BLOCK><<<tiles - tile_base, BLOCK, bytes, s>>>(kin, vin, kout, vout, n, shift, hist, lookback,
+                                                                   counter, err, spin_limit, tile_base, iota);
 }
 
 int sms() { return sm_count(); }
+
+// Threads per block of a pass over n keys (see the file comment).
+uint32_t sort_block(uint32_t n, uint32_t digit_bits)
+{
+    if (digit_bits == 10) return 256;
+    return (uint64_t)n <= (uint64_t)sms() * 1024u * kItems ? 1024u : 512u;
+}
 
 }  // namespace
 
 namespace sqk {
 
+uint32_t sort_tile_keys(uint32_t n, uint32_t digit_bits)
+{
+    return sort_block(n, digit_bits) * (uint32_t)kItems;
+}
+
 size_t sort_lookback_words(uint32_t n, uint32_t digit_bits, uint32_t passes)
 {
-    const size_t tiles = (n + kTile - 1) / kTile;
+    const uint32_t tile = sort_tile_keys(n, digit_bits);
+    const size_t tiles = (n + (size_t)tile - 1) / tile;
     return tiles * ((size_t)1 << digit_bits) * passes;
 }
 
@@ -284,11 +305,12 @@ void sort_histogram(const uint32_t* keys, uint32_t n, uint32_t* hist, uint32_t d
 
 int sort_passes(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b, uint32_t* vals_b, uint32_t n, const uint32_t* hist,
                 uint32_t* lookback, uint32_t* counters, uint32_t digit_bits, uint32_t passes, uint32_t* err,
-                cudaStream_t s, const SortStall* stall)
+                cudaStream_t s, const SortStall* stall, bool iota_values)
 {
     if (n == 0) return 0;
     const size_t radix = (size_t)1 << digit_bits;
     const size_t lb_words = sort_lookback_words(n, digit_bits, 1);
+    const uint32_t block = sort_block(n, digit_bits);
     int cur = 0;
     for (uint32_t p = 0; p < passes; ++p) {
         const uint32_t* kin = cur ? keys_b : keys_a;
@@ -300,9 +322,17 @@ int sort_passes(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b, uint32_t* 
         uint32_t* lb = lookback + p * lb_words;
         const uint32_t spin = stall ? stall->spin_limit : kSpinLimit;
         const uint32_t tb = (stall && p == 0) ? 1u : 0u;
-        if (digit_bits == 8) launch_pass<8>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, spin, tb, s);
-        else if (digit_bits == 10) launch_pass<10>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, spin, tb, s);
-        else launch_pass<6>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, spin, tb, s);
+        const bool iota = iota_values && p == 0;
+        if (digit_bits == 10)
+            launch_pass<10, 256>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, spin, tb, iota, s);
+        else if (digit_bits == 8 && block == 1024)
+            launch_pass<8, 1024>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, spin, tb, iota, s);
+        else if (digit_bits == 8)
+            launch_pass<8, 512>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, spin, tb, iota, s);
+        else if (block == 1024)
+            launch_pass<6, 1024>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, spin, tb, iota, s);
+        else
+            launch_pass<6, 512>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, spin, tb, iota, s);
         cur ^= 1;
     }
     return cur;
