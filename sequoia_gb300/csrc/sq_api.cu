@@ -5,6 +5,7 @@
 // pointer detection, and the build / trace dispatch.
 #include "sq_internal.cuh"
 
+#include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -123,6 +124,20 @@ void camera_params(const sq_ray_source& rs, float* cam)
     }
     cam[12] = (float)(th * (double)rs.width / (double)rs.height);
     cam[13] = (float)th;
+}
+
+// Streams and events of banded traces, created on the first banded call.
+bool band_resources(sq_ctx* c)
+{
+    if (c->copy_stream) return true;
+    bool ok = cudaStreamCreateWithFlags(&c->band_stream[0], cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&c->band_stream[1], cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&c->band_fork, cudaEventDisableTiming) == cudaSuccess;
+    for (auto& e : c->band_done) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+    for (auto& e : c->band_join) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+    ok = ok && cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) == cudaSuccess;
+    if (!ok) cudaGetLastError();
+    return ok;
 }
 
 sq_status check_device_error(sq_ctx* c, uint32_t* bits_out)
@@ -411,6 +426,14 @@ sq_status sq_destroy(sq_ctx* c)
     for (auto& kv : c->free_blocks) cudaFree(kv.second);
     for (auto& kv : c->live_blocks) cudaFree(kv.first);
     for (auto& e : c->ev) cudaEventDestroy(e);
+    for (auto& st : c->band_stream)
+        if (st) cudaStreamDestroy(st);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+    if (c->band_fork) cudaEventDestroy(c->band_fork);
+    for (auto& e : c->band_done)
+        if (e) cudaEventDestroy(e);
+    for (auto& e : c->band_join)
+        if (e) cudaEventDestroy(e);
     cudaFree(c->ctrl);
     if (c->host_ctl) cudaFreeHost(c->host_ctl);
     if (c->own_stream) cudaStreamDestroy(c->stream);
@@ -672,6 +695,68 @@ sq_status sq_radix_sort_pairs(sq_ctx* c, const uint32_t* keys_in, const uint32_t
     return st;
 }
 
+// Camera images of at least this many rays with page-locked host outputs
+// are traced in bands (see sq_trace).
+constexpr uint64_t kBandMinRays = 1u << 21;
+
+// An 8-wide camera trace in up to sq_ctx::kMaxBands row bands of 8x4 tiles:
+// band k traces on band_stream[k % 2] into the device buffers (hits_dev,
+// heat_dev, or the caller's device outputs), and copy_stream copies its rows
+// to the host outputs as soon as it is done.  The bands shrink towards the
+// end (tile-row shares 8:7:6:5:4:3:2:1 of 36), so the copy left when the
+// last band finishes is small and each earlier copy has the later bands'
+// trace time to hide in.  The context stream waits for everything at the
+// end.  Returns false on a CUDA error.
+bool trace8_bands(sq_ctx* c, sqk::Trace8Args w, sq_hit* hits, uint8_t* heat, const sq_hit* hits_dev,
+                  const uint8_t* heat_dev)
+{
+    cudaStream_t s = c->stream;
+    const uint32_t tiles_x = (w.width + 7u) / 8u, tiles_y = (w.height + 3u) / 4u;
+    const uint32_t nb = std::min<uint32_t>(sq_ctx::kMaxBands, tiles_y);
+    uint32_t* counters = static_cast<uint32_t*>(dalloc(c, sizeof(uint32_t) * sq_ctx::kMaxBands));
+    if (!counters) return false;
+    bool ok = cudaMemsetAsync(counters, 0, sizeof(uint32_t) * sq_ctx::kMaxBands, s) == cudaSuccess &&
+              cudaEventRecord(c->band_fork, s) == cudaSuccess &&
+              cudaStreamWaitEvent(c->band_stream[0], c->band_fork, 0) == cudaSuccess &&
+              cudaStreamWaitEvent(c->band_stream[1], c->band_fork, 0) == cudaSuccess &&
+              cudaStreamWaitEvent(c->copy_stream, c->band_fork, 0) == cudaSuccess;
+    // cumulative shares of band k's end: sum of (nb - j) for j <= k, over nb (nb + 1) / 2
+    const uint64_t total = (uint64_t)nb * (nb + 1) / 2;
+    uint64_t cum = 0;
+    for (uint32_t k = 0; ok && k < nb; ++k) {
+        const uint32_t ty0 = (uint32_t)((uint64_t)tiles_y * cum / total);
+        cum += nb - k;
+        const uint32_t ty1 = (uint32_t)((uint64_t)tiles_y * cum / total);
+        if (ty1 == ty0) continue;
+        cudaStream_t bs = c->band_stream[k & 1u];
+        w.tile0 = ty0 * tiles_x;
+        w.tile_end = ty1 * tiles_x;
+        w.work = counters + k;
+        sqk::trace8(w, bs);
+        ok = cudaGetLastError() == cudaSuccess && cudaEventRecord(c->band_done[k], bs) == cudaSuccess &&
+             cudaStreamWaitEvent(c->copy_stream, c->band_done[k], 0) == cudaSuccess;
+        // rows [4 ty0, 4 ty1) of the image are one contiguous range of rays
+        const size_t r0 = (size_t)std::min(4u * ty0, w.height) * w.width;
+        const size_t r1 = (size_t)std::min(4u * ty1, w.height) * w.width;
+        if (ok && hits_dev && hits)
+            ok = cudaMemcpyAsync(hits + r0, hits_dev + r0, sizeof(sq_hit) * (r1 - r0), cudaMemcpyDeviceToHost,
+                                 c->copy_stream) == cudaSuccess;
+        if (ok && heat_dev && heat)
+            ok = cudaMemcpyAsync(heat + 3 * r0, heat_dev + 3 * r0, 3 * (r1 - r0), cudaMemcpyDeviceToHost,
+                                 c->copy_stream) == cudaSuccess;
+    }
+    // join all three streams back into the context stream, even after an
+    // error, so nothing is left running against freed buffers
+    cudaStream_t side[3] = {c->band_stream[0], c->band_stream[1], c->copy_stream};
+    for (int q = 0; q < 3; ++q) {
+        const bool j = cudaEventRecord(c->band_join[q], side[q]) == cudaSuccess &&
+                       cudaStreamWaitEvent(s, c->band_join[q], 0) == cudaSuccess;
+        ok = ok && j;
+    }
+    dfree(c, counters);  // reused only by later work on the context stream, which waits for the bands
+    return ok;
+}
+
 sq_status sq_trace(sq_ctx* c, const sq_bvh* b, const sq_ray_source* rays, uint32_t mode, sq_hit* hits,
                    uint8_t* heatmap_rgb)
 {
@@ -740,6 +825,16 @@ sq_status sq_trace(sq_ctx* c, const sq_bvh* b, const sq_ray_source* rays, uint32
     // page-locked host outputs are written by the kernel in place
     sq_hit* hits_map = (hits && !hits_dev) ? static_cast<sq_hit*>(pinned_device_alias(hits)) : nullptr;
     uint8_t* heat_map = (heatmap_rgb && !heat_dev) ? static_cast<uint8_t*>(pinned_device_alias(heatmap_rgb)) : nullptr;
+    // ... except for a large camera image on the 8-wide tree: the image is
+    // traced in row bands into device memory, and the copy engine moves each
+    // finished band to the host while the next bands trace.  A kernel's
+    // stores into host memory slow it down more than that copy costs.
+    const bool wide_path = !coherent && b->nodes8 && mode != SQ_TRACE_REF && !force_binary;
+    const bool pinned_out = (hits_map || heat_map) && (!hits || hits_dev || hits_map) &&
+                            (!heatmap_rgb || heat_dev || heat_map);
+    const bool banded = wide_path && rays->kind != SQ_RAYS_EXPLICIT && !sched_refill && pinned_out &&
+                        count >= kBandMinRays && band_resources(c);
+    if (banded) hits_map = nullptr, heat_map = nullptr;
     sq_hit* hits_tmp = nullptr;
     uint8_t* heat_tmp = nullptr;
     if (hits && !hits_dev && !hits_map) {
@@ -782,7 +877,14 @@ sq_status sq_trace(sq_ctx* c, const sq_bvh* b, const sq_ray_source* rays, uint32
             // default: explicit rays refill lanes; camera rays keep coherent
             // 8x4 tiles per warp
             w.refill = sched_refill ? 1u : (sched_tiles ? 0u : (a.ray_kind == SQ_RAYS_EXPLICIT ? 1u : 0u));
-            sqk::trace8(w, s);
+            if (banded) {
+                if (!trace8_bands(c, w, hits, heatmap_rgb, hits_tmp, heat_tmp)) {
+                    dfree(c, rays_own); dfree(c, hits_tmp); dfree(c, heat_tmp);
+                    return fail(c, SQ_ERR_CUDA, "sq_trace: banded trace: %s", cudaGetErrorString(cudaGetLastError()));
+                }
+            } else {
+                sqk::trace8(w, s);
+            }
         } else {
             sqk::trace(a, s);
         }
@@ -790,8 +892,8 @@ sq_status sq_trace(sq_ctx* c, const sq_bvh* b, const sq_ray_source* rays, uint32
     SQ_CUDA(c, cudaEventRecord(c->ev[5], s));
     SQ_CUDA(c, cudaGetLastError());
     c->trace_timed = true;
-    if (hits_tmp) SQ_CUDA(c, cudaMemcpyAsync(hits, hits_tmp, sizeof(sq_hit) * count, cudaMemcpyDeviceToHost, s));
-    if (heat_tmp) SQ_CUDA(c, cudaMemcpyAsync(heatmap_rgb, heat_tmp, 3ull * count, cudaMemcpyDeviceToHost, s));
+    if (hits_tmp && !banded) SQ_CUDA(c, cudaMemcpyAsync(hits, hits_tmp, sizeof(sq_hit) * count, cudaMemcpyDeviceToHost, s));
+    if (heat_tmp && !banded) SQ_CUDA(c, cudaMemcpyAsync(heatmap_rgb, heat_tmp, 3ull * count, cudaMemcpyDeviceToHost, s));
     sq_status st = SQ_OK;
     if (hits_tmp || heat_tmp || hits_map || heat_map) st = check_device_error(c, nullptr);
     dfree(c, rays_own);

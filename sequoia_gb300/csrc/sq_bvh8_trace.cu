@@ -588,7 +588,7 @@ __global__ void __launch_bounds__(128) k_trace8_tiles(const sqk::Trace8Args a, u
     ws.reset(lane);
     for (;;) {
         uint32_t b = 0;
-        if (lane == 0) b = atomicAdd(a.work, 1u);
+        if (lane == 0) b = a.tile0 + atomicAdd(a.work, 1u);
         b = __shfl_sync(0xFFFFFFFFu, b, 0);
         if (b >= batches) break;
         Ray8 r;
@@ -791,16 +791,25 @@ void launch8(const sqk::Trace8Args& a, cudaStream_t s)
     if (a.ray_kind == SQ_RAYS_EXPLICIT) batches = (a.ray_count + 31u) / 32u;
     else batches = ((a.width + 7u) / 8u) * ((a.height + 3u) / 4u);
     if (batches == 0) return;
+    // The tiles kernel runs one warp per block: a block's SM slot is free as
+    // soon as its warp finds no tile left, so the next kernel on the GPU (the
+    // next band of a banded image) fills it at once instead of waiting for
+    // the slowest of four warps.
+    constexpr int kTilesBlock = 32;
     static PerDevice<std::array<int, 2>> cache;
     const std::array<int, 2> per_sm = cache.get([] {
-        return std::array<int, 2>{blocks_per_sm(k_trace8_tiles<MODE>, 128), blocks_per_sm(k_trace8_refill<MODE>, 128)};
+        return std::array<int, 2>{blocks_per_sm(k_trace8_tiles<MODE>, kTilesBlock),
+                                  blocks_per_sm(k_trace8_refill<MODE>, 128)};
     });
     const int v = a.refill ? 1 : 0;
     uint32_t grid = (uint32_t)(per_sm[v] * sm_count());
-    const uint32_t need = (batches + 3u) / 4u;
+    if (!v && a.tile_end && a.tile_end < batches) batches = a.tile_end;  // a band of the image
+    const uint32_t first = v ? 0u : min(a.tile0, batches);
+    const uint32_t need = v ? (batches + 3u) / 4u : batches - first;
     if (grid > need) grid = need;
+    if (grid == 0) return;
     if (v) k_trace8_refill<MODE><<<grid, 128, 0, s>>>(a, a.ray_kind == SQ_RAYS_EXPLICIT ? a.ray_count : batches * 32u);
-    else k_trace8_tiles<MODE><<<grid, 128, 0, s>>>(a, batches);
+    else k_trace8_tiles<MODE><<<grid, kTilesBlock, 0, s>>>(a, batches);
 }
 
 // Batch, tiles: as k_trace8_tiles over the job table's 32-ray batches.

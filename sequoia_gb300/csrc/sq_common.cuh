@@ -399,6 +399,9 @@ struct Trace8Args {
     unsigned long long* stats;
     uint32_t refill;       // 1: per-lane ray refill; 0: whole 32-ray batches per warp
     uint32_t heat_ramp;    // heatmap pixels: 0 = grey, 1 = colour ramp (write_heat)
+    // camera rays, tiles schedule: only tiles [tile0, tile_end) of the image
+    // (tile_end 0: to the last tile), so an image can be traced in row bands
+    uint32_t tile0, tile_end;
 };
 // Triangles an 8-wide BVH can address: a traversal stack entry holds the
 // first triangle of a leaf range in 27 bits (and its count in 4).

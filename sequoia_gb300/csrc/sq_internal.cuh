@@ -26,6 +26,13 @@ struct sq_ctx {
     // through before one fails (-1 = off)
     uint32_t stall_lookback = 0, stall_barrier = 0;
     int64_t fail_alloc_in = -1;
+    // banded camera traces into page-locked host memory (created on first
+    // use): two streams the bands alternate on, so a band starts while the
+    // one before it drains, and a copy stream that moves each finished band
+    // to the host while later bands trace
+    static constexpr int kMaxBands = 8;
+    cudaStream_t band_stream[2] = {}, copy_stream = nullptr;
+    cudaEvent_t band_fork = nullptr, band_done[kMaxBands] = {}, band_join[3] = {};
 };
 
 struct sq_bvh {

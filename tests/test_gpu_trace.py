@@ -101,6 +101,47 @@ def test_trace_into_pinned_host_buffers(ctx):
             assert np.array_equal(p_heat.numpy(), ref_heat)
 
 
+def test_banded_trace_into_pinned_host_buffers(ctx):
+    """A camera image of 2^21 rays or more with page-locked host outputs on
+    the 8-wide tree is traced in row bands whose results are copied to the
+    host while later bands trace.  Every combination of pinned and device
+    outputs gives the bytes a single trace into device buffers gives, on an
+    image whose width and height are not multiples of the 8x4 tile."""
+    torch = pytest.importorskip("torch")
+    from sequoia_gb300 import scenes
+    tris = scenes.gaussian_soup(300_000, 16, seed=35)
+    bvh = ctx.build(tris, "morton", wide=True)
+    cam = dict(camera="pinhole", width=2050, height=1031, origin=(0.0, 1.0, -40.0), target=(0, 0, 0), vfov=45.0)
+    count = 2050 * 1031
+    assert count >= 1 << 21
+    d_hits = torch.zeros(count * 3, dtype=torch.int32, device="cuda")
+    d_heat = torch.zeros(count * 3, dtype=torch.uint8, device="cuda")
+    ctx.trace(bvh, "closest", hits=d_hits, heatmap=d_heat, **cam)
+    ctx.sync()
+    want_hits, want_heat = d_hits.cpu().numpy(), d_heat.cpu().numpy()
+    assert (want_hits.reshape(-1, 3)[:, 0] != -1).sum() > 0
+    for pin_hits, pin_heat in ((True, True), (True, False), (False, True)):
+        h = torch.full((count * 3,), 7, dtype=torch.int32)
+        m = torch.full((count * 3,), 7, dtype=torch.uint8)
+        h = h.pin_memory() if pin_hits else h.cuda()
+        m = m.pin_memory() if pin_heat else m.cuda()
+        ctx.trace(bvh, "closest", hits=h, heatmap=m, **cam)
+        ctx.sync()
+        assert np.array_equal(h.cpu().numpy(), want_hits), (pin_hits, pin_heat)
+        assert np.array_equal(m.cpu().numpy(), want_heat), (pin_hits, pin_heat)
+    # hits only, and the colour ramp, pinned
+    h = torch.zeros(count * 3, dtype=torch.int32).pin_memory()
+    ctx.trace(bvh, "closest", hits=h, **cam)
+    assert np.array_equal(h.numpy(), want_hits)
+    ramp_d = torch.zeros(count * 3, dtype=torch.uint8, device="cuda")
+    ctx.trace(bvh, "closest", hits=False, heatmap=ramp_d, ramp=True, **cam)
+    ctx.sync()
+    ramp_p = torch.zeros(count * 3, dtype=torch.uint8).pin_memory()
+    ctx.trace(bvh, "closest", hits=False, heatmap=ramp_p, ramp=True, **cam)
+    assert np.array_equal(ramp_p.numpy(), ramp_d.cpu().numpy())
+    assert ctx.sync() == 0
+
+
 def test_closest_t_vs_fp64(ctx, oracle):
     """Closest-hit t is bit-identical to the oracle (so within any relative
     tolerance of it, 1e-6 included); its error against an FP64 re-intersection
