@@ -50,6 +50,7 @@ typedef enum sq_status {
 #define SQ_DEVERR_TOPOLOGY         0x4u  /* LBVH climb found an inconsistent state  */
 #define SQ_DEVERR_SAH_QUEUE        0x8u  /* SAH task queue overflow / wait ran out  */
 #define SQ_DEVERR_NODE_COUNT       0x10u /* a node would hold more than 65535 prims */
+#define SQ_DEVERR_COPY_TIMEOUT     0x20u /* a bulk copy into shared memory did not complete */
 
 typedef struct sq_ctx sq_ctx;
 typedef struct sq_bvh sq_bvh;
@@ -409,9 +410,9 @@ sq_status sq_last_trace_stats(sq_ctx* ctx, uint64_t stats[4]);
  * (the reference asserts or exits on failure).  Each injection is armed for
  * one use on this context, then clears itself:
  *   SQ_DEBUG_STALL_LOOKBACK  the next sq_radix_sort_pairs, which must be a
- *                            one-pass sort (key_bits <= digit_bits) of more
- *                            than one tile (16384 keys; 4096 with 10-bit
- *                            digits), runs without its first tile: the
+ *                            one-pass sort (key_bits <= digit_bits) that
+ *                            spans more than one tile (any sort of more than
+ *                            16384 keys does), runs without its first tile: the
  *                            look-back of the tiles after it waits on words
  *                            that nothing publishes, gives up after `limit`
  *                            polls and raises SQ_DEVERR_LOOKBACK_TIMEOUT.

@@ -224,10 +224,10 @@ sq_status build_morton(sq_ctx* c, sq_bvh* b, const sq_build_params& p)
     uint32_t *ka, *va, *kb, *vb;
     if (passes % 2 == 0) { ka = b->codes; va = b->perm; kb = alt; vb = alt + n; }
     else { ka = alt; va = alt + n; kb = b->codes; vb = b->perm; }
-    sqk::scene_bounds(b->tris, n, p.morton_bounds, zero + z_box, s);
+    sqk::scene_bounds(b->tris, n, p.morton_bounds, zero + z_box, err, s);
     // the values are the triangle numbers: the sort's first pass generates
     // them instead of reading them
-    sqk::morton_codes(b->tris, n, p.morton_bounds, zero + z_box, ka, nullptr, zero + z_hist, db, passes, s);
+    sqk::morton_codes(b->tris, n, p.morton_bounds, zero + z_box, ka, nullptr, zero + z_hist, db, passes, err, s);
     SQ_CUDA(c, cudaEventRecord(c->ev[1], s));
     sqk::sort_passes(ka, va, kb, vb, n, zero + z_hist, zero + z_lb, zero + z_ctr, db, passes, err, s, nullptr, true);
     SQ_CUDA(c, cudaEventRecord(c->ev[2], s));
@@ -276,7 +276,7 @@ sq_status build_morton64(sq_ctx* c, sq_bvh* b, const sq_build_params& p)
     cudaStream_t s = c->stream;
     SQ_CUDA(c, cudaEventRecord(c->ev[0], s));
     SQ_CUDA(c, cudaMemsetAsync(zero, 0, sizeof(uint32_t) * z_words, s));
-    sqk::scene_bounds(b->tris, n, p.morton_bounds, zero + z_box, s);
+    sqk::scene_bounds(b->tris, n, p.morton_bounds, zero + z_box, err, s);
     sqk::morton_codes64(b->tris, n, zero + z_box, lo, hi, vals, zero + z_hist, s);
     SQ_CUDA(c, cudaEventRecord(c->ev[1], s));
     // an even number of passes leaves each stage's result in its input buffers
@@ -625,8 +625,8 @@ sq_status sq_morton_codes(sq_ctx* c, const sq_triangle* tris, uint32_t n, uint32
     if (!zero || !keys) { dfree(c, zero); dfree(c, keys); dfree(c, owned); return fail(c, SQ_ERR_OOM, "allocation failed"); }
     cudaStream_t s = c->stream;
     SQ_CUDA(c, cudaMemsetAsync(zero, 0, sizeof(uint32_t) * z_words, s));
-    sqk::scene_bounds(dt, n, bounds_mode, zero, s);
-    sqk::morton_codes(dt, n, bounds_mode, zero, keys, keys + n, zero + 8, db, passes, s);
+    sqk::scene_bounds(dt, n, bounds_mode, zero, c->ctrl, s);
+    sqk::morton_codes(dt, n, bounds_mode, zero, keys, keys + n, zero + 8, db, passes, c->ctrl, s);
     SQ_CUDA(c, cudaMemcpyAsync(codes, keys, sizeof(uint32_t) * (size_t)n, cudaMemcpyDefault, s));
     uint32_t ord[6];
     SQ_CUDA(c, cudaMemcpyAsync(ord, zero, sizeof ord, cudaMemcpyDeviceToHost, s));

@@ -293,9 +293,10 @@ struct WarpStats {
 namespace sqk {
 
 // LBVH (sq_lbvh.cu)
-void scene_bounds(const float* tris, uint32_t n, uint32_t mode, uint32_t* box_ord, cudaStream_t s);
-void morton_codes(const float* tris, uint32_t n, uint32_t mode, const uint32_t* box_ord, uint32_t* keys,
-                  uint32_t* vals, uint32_t* hist, uint32_t digit_bits, uint32_t passes, cudaStream_t s);
+// err: the context's device error word (SQ_DEVERR_COPY_TIMEOUT)
+void scene_bounds(const float* tris, uint32_t n, uint32_t mode, uint32_t* box_ord, uint32_t* err, cudaStream_t s);
+void morton_codes(const float* tris, uint32_t n, uint32_t mode, const uint32_t* box_ord, uint32_t* keys, uint32_t* vals,
+                  uint32_t* hist, uint32_t digit_bits, uint32_t passes, uint32_t* err, cudaStream_t s);
 // flags: n zeroed words; info: 6n float4 (a 48-byte record per boundary side)
 // surv: n words of scratch for the nodes left to the global phase;
 // surv_count: one zeroed word.
@@ -320,7 +321,7 @@ void lbvh_climb64(const uint64_t* codes, const uint32_t* perm, const float* tris
                   cudaStream_t s);
 
 // onesweep radix sort (sq_sort.cu)
-// keys per tile of a pass over n keys (4096, 8192 or 16384)
+// keys per tile of a pass over n keys (512 per warp of the block: 4096 to 16384)
 uint32_t sort_tile_keys(uint32_t n, uint32_t digit_bits);
 size_t sort_lookback_words(uint32_t n, uint32_t digit_bits, uint32_t passes);
 void sort_histogram(const uint32_t* keys, uint32_t n, uint32_t* hist, uint32_t digit_bits, uint32_t passes,

@@ -26,6 +26,7 @@
 #include "sq_common.cuh"
 #include "sq_lbvh_dev.cuh"
 
+#include <algorithm>
 #include <cstdio>
 
 namespace {
@@ -53,6 +54,117 @@ __device__ __forceinline__ void stage_tris(const float* __restrict__ tris, uint3
     }
 }
 
+// ---------------------------------------------------------------------------
+// Bulk-copy staging of triangle tiles (TMA, cp.async.bulk): two shared
+// buffers per block, each completed through its own mbarrier, so the copy of
+// a block's next tile is in flight while the current one is processed.  A
+// tile of kTileTris triangles is 9216 bytes, a multiple of 16, and starts on
+// a 16-byte boundary when the array does; the last tile, when partial, is
+// read with plain loads.  Waits are bounded: a copy that does not complete
+// raises SQ_DEVERR_COPY_TIMEOUT and the block gives up.
+constexpr uint32_t kTileBytes = kTileTris * 36u;
+constexpr uint32_t kCopySpins = 1u << 22;
+
+struct TileStage {
+    float tri[2][kTileTris * 9];
+    unsigned long long bar[2];
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// thread 0: start the copy of full tile t into buffer b
+__device__ __forceinline__ void stage_issue(TileStage& st, int b, const float* __restrict__ tris, uint32_t t)
+{
+    const uint32_t bar = smem_addr(&st.bar[b]);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(kTileBytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_addr(st.tri[b])), "l"(tris + 9ull * kTileTris * t), "r"(kTileBytes), "r"(bar)
+                 : "memory");
+}
+
+// every thread: wait for phase `parity` of buffer b's barrier (bounded)
+__device__ __forceinline__ bool stage_wait(TileStage& st, int b, uint32_t parity)
+{
+    const uint32_t bar = smem_addr(&st.bar[b]);
+    for (uint32_t spins = 0; spins < kCopySpins; ++spins) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\t"
+                     "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// Calls body(s_tri, first, count) for each of this block's tiles (tile
+// blockIdx.x + k * gridDim.x), tiles staged as described above; every thread
+// of the block must call it.  Falls back to plain staged loads when the
+// array is not 16-byte aligned.
+template <class Body>
+__device__ void for_each_tile(const float* __restrict__ tris, uint32_t n, bool aligned, uint32_t* err, Body body)
+{
+    __shared__ __align__(128) TileStage st;
+    const uint32_t ntiles = (n + kTileTris - 1) / kTileTris, full = n / kTileTris;
+    if (!aligned) {
+        for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+            const uint32_t first = t * kTileTris, count = min((uint32_t)kTileTris, n - first);
+            __syncthreads();
+            stage_tris(tris, first, count, st.tri[0], false);
+            __syncthreads();
+            body(st.tri[0], first, count);
+        }
+        return;
+    }
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&st.bar[0])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&st.bar[1])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    // per buffer: the barrier phase to wait for, and whether a copy into it
+    // has been started and not yet waited for (the same in every thread)
+    uint32_t parity[2] = {0u, 0u};
+    bool pending[2] = {false, false};
+    uint32_t t = blockIdx.x;
+    if (t < full) {
+        if (threadIdx.x == 0) stage_issue(st, 0, tris, t);
+        pending[0] = true;
+    }
+    bool ok = true;
+    for (int b = 0; t < ntiles; t += gridDim.x, b ^= 1) {
+        const uint32_t next = t + gridDim.x;
+        // buffer b ^ 1 was released by the barrier that ended the last tile
+        if (next < full) {
+            if (threadIdx.x == 0) stage_issue(st, b ^ 1, tris, next);
+            pending[b ^ 1] = true;
+        }
+        const uint32_t first = t * kTileTris, count = min((uint32_t)kTileTris, n - first);
+        if (t < full) {
+            ok = stage_wait(st, b, parity[b]);
+            if (ok) {
+                parity[b] ^= 1u;
+                pending[b] = false;
+            }
+        } else {
+            stage_tris(tris, first, count, st.tri[b], true);  // the partial last tile
+        }
+        if (!__syncthreads_and(ok)) break;
+        body(st.tri[b], first, count);
+        __syncthreads();
+    }
+    if (!__syncthreads_and(ok)) {
+        // give up: wait (bounded) for the copies this block started, so none
+        // lands in shared memory after the block has left
+        if (threadIdx.x == 0) {
+            raise_error(err, SQ_DEVERR_COPY_TIMEOUT);
+            for (int b = 0; b < 2; ++b)
+                if (pending[b]) stage_wait(st, b, parity[b]);
+        }
+        __syncthreads();
+    }
+}
+
 __device__ __forceinline__ float warp_min(float v)
 {
 #pragma unroll
@@ -68,16 +180,11 @@ __device__ __forceinline__ float warp_max(float v)
 
 // box_ord[k] = ordered(-min_k), box_ord[3 + k] = ordered(max_k); zero-initialised.
 __global__ void __launch_bounds__(256) k_scene_bounds(const float* __restrict__ tris, uint32_t n, uint32_t mode,
-                                                      uint32_t* __restrict__ box_ord, bool aligned)
+                                                      uint32_t* __restrict__ box_ord, bool aligned, uint32_t* err)
 {
-    __shared__ __align__(16) float s_tri[kTileTris * 9];
     __shared__ float s_red[8][6];
     float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-    for (uint32_t first = blockIdx.x * kTileTris; first < n; first += gridDim.x * kTileTris) {
-        const uint32_t count = min((uint32_t)kTileTris, n - first);
-        __syncthreads();
-        stage_tris(tris, first, count, s_tri, aligned);
-        __syncthreads();
+    for_each_tile(tris, n, aligned, err, [&](const float* s_tri, uint32_t, uint32_t count) {
         if (threadIdx.x < count) {
             Box b = tri_box(s_tri + 9 * threadIdx.x);
             if (mode == SQ_MORTON_BOUNDS_CENTROID) {
@@ -92,7 +199,7 @@ __global__ void __launch_bounds__(256) k_scene_bounds(const float* __restrict__ 
                 for (int k = 0; k < 3; ++k) { mn[k] = fminf(mn[k], b.mn[k]); mx[k] = fmaxf(mx[k], b.mx[k]); }
             }
         }
-    }
+    });
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < 3; ++k) { mn[k] = warp_min(mn[k]); mx[k] = warp_max(mx[k]); }
@@ -125,10 +232,10 @@ __device__ __forceinline__ uint32_t f2u(float x) { return (x >= 0.0f) ? (uint32_
 template <int DB, int PASSES>
 __global__ void __launch_bounds__(256) k_morton(const float* __restrict__ tris, uint32_t n, uint32_t mode,
                                                 const uint32_t* __restrict__ box_ord, uint32_t* __restrict__ keys,
-                                                uint32_t* __restrict__ vals, uint32_t* __restrict__ hist, bool aligned)
+                                                uint32_t* __restrict__ vals, uint32_t* __restrict__ hist, bool aligned,
+                                                uint32_t* err)
 {
     constexpr int RADIX = 1 << DB;
-    __shared__ __align__(16) float s_tri[kTileTris * 9];
     __shared__ uint32_t s_hist[PASSES * RADIX];
     for (int j = threadIdx.x; j < PASSES * RADIX; j += blockDim.x) s_hist[j] = 0;
     float smin[3], ext[3];
@@ -139,11 +246,7 @@ __global__ void __launch_bounds__(256) k_morton(const float* __restrict__ tris, 
         ext[k] = smax - smin[k];
     }
     (void)mode;
-    for (uint32_t first = blockIdx.x * kTileTris; first < n; first += gridDim.x * kTileTris) {
-        const uint32_t count = min((uint32_t)kTileTris, n - first);
-        __syncthreads();
-        stage_tris(tris, first, count, s_tri, aligned);
-        __syncthreads();
+    for_each_tile(tris, n, aligned, err, [&](const float* s_tri, uint32_t first, uint32_t count) {
         if (threadIdx.x < count) {
             const Box b = tri_box(s_tri + 9 * threadIdx.x);
             uint32_t q[3];
@@ -161,7 +264,7 @@ __global__ void __launch_bounds__(256) k_morton(const float* __restrict__ tris, 
 #pragma unroll
             for (int p = 0; p < PASSES; ++p) atomicAdd(&s_hist[p * RADIX + ((code >> (p * DB)) & (RADIX - 1))], 1u);
         }
-    }
+    });
     __syncthreads();
     for (int j = threadIdx.x; j < PASSES * RADIX; j += blockDim.x) {
         const uint32_t c = s_hist[j];
@@ -395,37 +498,41 @@ __global__ void __launch_bounds__(256, 6) k_lbvh_climb(const Code* __restrict__ 
     };
 
     // Warp phase: nodes whose two children both finish inside this warp are
-    // merged through shuffles (the lanes of the two children find each other
-    // by their common parent), in rounds, until a round merges nothing; only
+    // merged through shuffles, in rounds, until a round merges nothing; only
     // the nodes left then go to the global protocol (k_lbvh_global).  Most
-    // small subtrees never touch the sibling records or the flags.
+    // small subtrees never touch the sibling records or the flags.  A node
+    // [l, r) is always held by the lane of its first position, l - W (run
+    // heads start there, and a merge continues in the left child's lane), so
+    // a left child (parent boundary r) finds its sibling in lane r - W: the
+    // node there must be active and name boundary r as its own parent, as the
+    // right child.  The right child learns that it was merged from an OR of
+    // the lanes the left children took.
     for (;;) {
         if (active && l == sb && r == se) { write_root(); active = false; }
-        const uint32_t A = __ballot_sync(FULL, active);
-        if (!A) break;
-        bool merged = false;
-        if (active) {
-            uint32_t p;
-            bool left;
-            parent_of(p, left);
-            const uint32_t grp = __match_any_sync(A, p);
-            if (__popc(grp) == 2) {
-                const int other = __ffs(grp & ~(1u << lane)) - 1;
-                const uint32_t o_r = __shfl_sync(grp, r, other);
-                const Code o_dr = __shfl_sync(grp, dr, other);
-                const uint32_t o_split = __shfl_sync(grp, split, other);
-                Box ob;
+        if (!__any_sync(FULL, active)) break;
+        uint32_t p = 0;
+        bool left = false;
+        if (active) parent_of(p, left);
+        // (parent boundary, side, active) of every lane; parent boundaries
+        // are below 2^30
+        const uint32_t me = active ? (p << 2) | (left ? 2u : 0u) | 1u : 0u;
+        const bool look = active && left && r - W < 32u;
+        const int src = look ? (int)(r - W) : lane;
+        const uint32_t other = __shfl_sync(FULL, me, src);
+        const bool take = look && other == ((r << 2) | 1u);
+        const uint32_t o_r = __shfl_sync(FULL, r, src);
+        const Code o_dr = __shfl_sync(FULL, dr, src);
+        const uint32_t o_split = __shfl_sync(FULL, split, src);
+        Box ob;
 #pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    ob.mn[k] = __shfl_sync(grp, box.mn[k], other);
-                    ob.mx[k] = __shfl_sync(grp, box.mx[k], other);
-                }
-                if (left) merge(p, true, o_r, ob, o_split, o_dr);
-                else active = false;
-                merged = true;
-            }
+        for (int k = 0; k < 3; ++k) {
+            ob.mn[k] = __shfl_sync(FULL, box.mn[k], src);
+            ob.mx[k] = __shfl_sync(FULL, box.mx[k], src);
         }
-        if (!__any_sync(FULL, merged)) break;
+        const uint32_t taken = __reduce_or_sync(FULL, take ? 1u << src : 0u);
+        if (take) merge(p, true, o_r, ob, o_split, o_dr);
+        if ((taken >> lane) & 1u) active = false;
+        if (!taken) break;
     }
 
     uint32_t p = 0;
@@ -531,25 +638,30 @@ int sms() { return sm_count(); }
 
 namespace sqk {
 
-void scene_bounds(const float* tris, uint32_t n, uint32_t mode, uint32_t* box_ord, cudaStream_t s)
+// Both streaming kernels run eight blocks per SM (two 9 KB tile buffers each;
+// the next tile's bulk copy overlaps the current tile's work).
+void scene_bounds(const float* tris, uint32_t n, uint32_t mode, uint32_t* box_ord, uint32_t* err, cudaStream_t s)
 {
     if (n == 0) return;
     const bool aligned = (reinterpret_cast<uintptr_t>(tris) & 15u) == 0;
     const uint32_t tiles = (n + kTileTris - 1) / kTileTris;
     const uint32_t grid = min(tiles, (uint32_t)sms() * 8u);
-    k_scene_bounds<<<grid, 256, 0, s>>>(tris, n, mode, box_ord, aligned);
+    k_scene_bounds<<<grid, 256, 0, s>>>(tris, n, mode, box_ord, aligned, err);
 }
 
 void morton_codes(const float* tris, uint32_t n, uint32_t mode, const uint32_t* box_ord, uint32_t* keys, uint32_t* vals,
-                  uint32_t* hist, uint32_t digit_bits, uint32_t passes, cudaStream_t s)
+                  uint32_t* hist, uint32_t digit_bits, uint32_t passes, uint32_t* err, cudaStream_t s)
 {
     if (n == 0) return;
     const bool aligned = (reinterpret_cast<uintptr_t>(tris) & 15u) == 0;
     const uint32_t tiles = (n + kTileTris - 1) / kTileTris;
     const uint32_t grid = min(tiles, (uint32_t)sms() * 8u);
-    if (digit_bits == 8 && passes == 4) k_morton<8, 4><<<grid, 256, 0, s>>>(tris, n, mode, box_ord, keys, vals, hist, aligned);
-    else if (digit_bits == 10 && passes == 3) k_morton<10, 3><<<grid, 256, 0, s>>>(tris, n, mode, box_ord, keys, vals, hist, aligned);
-    else if (digit_bits == 6 && passes == 5) k_morton<6, 5><<<grid, 256, 0, s>>>(tris, n, mode, box_ord, keys, vals, hist, aligned);
+    if (digit_bits == 8 && passes == 4)
+        k_morton<8, 4><<<grid, 256, 0, s>>>(tris, n, mode, box_ord, keys, vals, hist, aligned, err);
+    else if (digit_bits == 10 && passes == 3)
+        k_morton<10, 3><<<grid, 256, 0, s>>>(tris, n, mode, box_ord, keys, vals, hist, aligned, err);
+    else if (digit_bits == 6 && passes == 5)
+        k_morton<6, 5><<<grid, 256, 0, s>>>(tris, n, mode, box_ord, keys, vals, hist, aligned, err);
 }
 
 void morton_codes64(const float* tris, uint32_t n, const uint32_t* box_ord, uint32_t* lo, uint32_t* hi,
@@ -584,11 +696,14 @@ void climb_launch(const Code* codes, const uint32_t* perm, const float* tris, ui
     if (n == 0) return;
     k_lbvh_climb<Code, SEG><<<(n + 255) / 256, 256, 0, s>>>(codes, perm, tris, n, nodes, info, surv, surv_count, off, M,
                                                             root0, err);
-    // one thread per possible open node (their count is on the device): the
-    // climbs are chains of round trips, so running them all at once beats a
-    // grid-stride loop over fewer threads
-    k_lbvh_global<Code, SEG><<<(n + 255) / 256, 256, 0, s>>>(surv, surv_count, n, nodes, flags, info, off, M, root0,
-                                                             err);
+    // one thread per open node, all at once: the climbs are chains of round
+    // trips, so running them side by side beats a grid-stride loop over fewer
+    // threads.  Their count is on the device; a warp of 32 positions leaves
+    // about four open nodes (its subtree's two spines), so n / 6 threads plus
+    // a block per SM cover them without launching blocks that find nothing
+    // to do (the loop is grid-stride, so any count is processed)
+    const uint32_t grid = std::min((n + 255u) / 256u, (n / 6u + 255u) / 256u + (uint32_t)sms());
+    k_lbvh_global<Code, SEG><<<grid, 256, 0, s>>>(surv, surv_count, n, nodes, flags, info, off, M, root0, err);
 }
 
 void lbvh_climb(const uint32_t* codes, const uint32_t* perm, const float* tris, uint32_t n, sq::Node* nodes,

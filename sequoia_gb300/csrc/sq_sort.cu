@@ -8,11 +8,13 @@
 // Morton kernel for builds); then one kernel per digit:
 //   - a block takes the next tile from an atomic counter, so tiles are
 //     processed in order and a tile's predecessors are always running;
-//   - a tile is 16 keys per thread of a 256-, 512- or 1024-thread block:
-//     the look-back below is a chain over the tiles, so the largest tiles
-//     that still fill the GPU are the fastest (1024 threads while all tiles
-//     fit one block per SM, 512 beyond that; 256 for 10-bit digits, whose
-//     per-warp digit counts fill shared memory);
+//   - a tile is 16 keys per thread of the block, whose size is chosen per
+//     sort: the look-back below is a chain over the tiles, so the fewest
+//     tiles that still fill the GPU are the fastest.  Up to 16384 keys per
+//     SM the sort is one tile per SM (blocks of 256 to 1024 threads, sized
+//     so the tiles cover every SM); beyond that 512-thread blocks, two per
+//     SM; 10-bit digits always use 256 threads (their per-warp digit counts
+//     fill shared memory);
 //   - warps rank their keys by digit (stable: items are ranked in index
 //     order within the warp, warps in index order within the tile); the lanes
 //     sharing a digit come from one ballot per digit bit, which costs the
@@ -25,6 +27,8 @@
 //     written out so that consecutive threads write consecutive addresses.
 #include "sq_common.cuh"
 
+#include <algorithm>
+
 namespace {
 
 using namespace sq;
@@ -36,12 +40,13 @@ constexpr uint32_t kCountMask = (1u << 30) - 1u;
 constexpr uint32_t kSpinLimit = 1u << 22;
 constexpr int kWindow = 8;  // look-back words loaded per round
 
-template <int RADIX, int BLOCK>
+template <int RADIX, int MINBLOCK>
 __device__ __forceinline__ void block_exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t* s_tmp)
 {
-    // RADIX values, BLOCK threads; each thread owns a contiguous chunk.
-    constexpr int kWarps = BLOCK / 32;
-    constexpr int PER = (RADIX + BLOCK - 1) / BLOCK;
+    // RADIX values over the block's threads (at least MINBLOCK); each thread
+    // owns a contiguous chunk of PER values.
+    const int kWarps = (int)(blockDim.x >> 5);
+    constexpr int PER = (RADIX + MINBLOCK - 1) / MINBLOCK;
     uint32_t v[PER];
     uint32_t sum = 0;
     const int t = threadIdx.x;
@@ -81,17 +86,18 @@ __device__ __forceinline__ void block_exclusive_scan(const uint32_t* in, uint32_
     __syncthreads();
 }
 
-template <int DB, int BLOCK>
-struct Smem {
-    static constexpr int RADIX = 1 << DB;
-    static constexpr size_t bytes = sizeof(uint32_t) * (2 * BLOCK * kItems + (BLOCK / 32) * RADIX + 3 * RADIX + 32);
-};
+// dynamic shared memory of a k_onesweep block of `block` threads
+constexpr size_t smem_bytes(int db, int block)
+{
+    return sizeof(uint32_t) * (2 * (size_t)block * kItems + (size_t)(block / 32) * (1u << db) + 3 * (1u << db) + 32);
+}
 
-// 64 registers a thread at every block size (1024 / BLOCK blocks per SM).
+// MAXB: the largest block the kernel is launched with (any multiple of 32
+// from 256 up to MAXB); 64 registers a thread either way.
 // iota: each key's value is its index (vin is not read), as in the first
 // pass of a build, whose values are the triangle numbers.
-template <int DB, int BLOCK>
-__global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_onesweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+template <int DB, int MAXB>
+__global__ void __launch_bounds__(MAXB, 1024 / MAXB) k_onesweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
                                                      uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n,
                                                      uint32_t shift, const uint32_t* __restrict__ hist,
                                                      uint32_t* __restrict__ lookback, uint32_t* __restrict__ counter,
@@ -99,7 +105,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_onesweep(const uint32_t
 {
     constexpr int RADIX = 1 << DB;
     constexpr uint32_t MASK = RADIX - 1;
-    constexpr int kBlock = BLOCK, kWarps = BLOCK / 32, kTile = BLOCK * kItems;
+    const int kBlock = (int)blockDim.x, kWarps = kBlock >> 5, kTile = kBlock * kItems;
     extern __shared__ __align__(16) uint32_t smem[];
     uint32_t* s_keys = smem;
     uint32_t* s_vals = s_keys + kTile;
@@ -155,7 +161,6 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_onesweep(const uint32_t
     // exclusive offsets across warps per digit; block counts
     for (int d = tid; d < RADIX; d += kBlock) {
         uint32_t run = 0;
-#pragma unroll
         for (int w = 0; w < kWarps; ++w) {
             const uint32_t c = s_whist[w * RADIX + d];
             s_whist[w * RADIX + d] = run;
@@ -165,8 +170,8 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_onesweep(const uint32_t
         st_relaxed_u32(lookback + (size_t)tile * RADIX + d, (tile == 0 ? kFlagInc : kFlagAgg) | run);
     }
     __syncthreads();
-    block_exclusive_scan<RADIX, BLOCK>(hist, s_gbase, s_tmp);
-    block_exclusive_scan<RADIX, BLOCK>(s_bcount, s_lexcl, s_tmp);
+    block_exclusive_scan<RADIX, 256>(hist, s_gbase, s_tmp);
+    block_exclusive_scan<RADIX, 256>(s_bcount, s_lexcl, s_tmp);
     // decoupled look-back, one digit per thread (or several).  The words of
     // kWindow predecessors are loaded at once (independent relaxed loads, one
     // memory latency: each word carries its flag and count together, so no
@@ -247,24 +252,25 @@ __global__ void __launch_bounds__(256) k_sort_hist(const uint32_t* __restrict__ 
     }
 }
 
-template <int DB, int BLOCK>
+template <int DB, int MAXB>
 void launch_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, uint32_t n, uint32_t shift,
                  const uint32_t* hist, uint32_t* lookback, uint32_t* counter, uint32_t* err, uint32_t spin_limit,
-                 uint32_t tile_base, bool iota, cudaStream_t s)
+                 uint32_t tile_base, bool iota, uint32_t block, cudaStream_t s)
 {
-    constexpr size_t bytes = Smem<DB, BLOCK>::bytes;
-    static_assert(bytes <= 227 * 1024, "onesweep tile does not fit in shared memory");
+    constexpr size_t max_bytes = smem_bytes(DB, MAXB);
+    static_assert(max_bytes <= 227 * 1024, "onesweep tile does not fit in shared memory");
     // the opt-in above 48 KB of dynamic shared memory is a per-device
     // attribute of the function: set it on each device's first use
     static PerDevice<bool> configured;
     configured.get([] {
-        cudaFuncSetAttribute(k_onesweep<DB, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        cudaFuncSetAttribute(k_onesweep<DB, MAXB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_bytes);
         return true;
     });
-    const uint32_t tiles = (n + BLOCK * kItems - 1) / (BLOCK * kItems);
+    const uint32_t tile = block * kItems;
+    const uint32_t tiles = (n + tile - 1) / tile;
     if (tiles <= tile_base) return;
-    k_onesweep<DB, BLOCK><<<tiles - tile_base, BLOCK, bytes, s>>>(kin, vin, kout, vout, n, shift, hist, lookback,
-                                                                   counter, err, spin_limit, tile_base, iota);
+    k_onesweep<DB, MAXB><<<tiles - tile_base, block, smem_bytes(DB, (int)block), s>>>(
+        kin, vin, kout, vout, n, shift, hist, lookback, counter, err, spin_limit, tile_base, iota);
 }
 
 int sms() { return sm_count(); }
@@ -273,7 +279,11 @@ int sms() { return sm_count(); }
 uint32_t sort_block(uint32_t n, uint32_t digit_bits)
 {
     if (digit_bits == 10) return 256;
-    return (uint64_t)n <= (uint64_t)sms() * 1024u * kItems ? 1024u : 512u;
+    const uint64_t per_sm = (uint64_t)sms() * 1024u * kItems;
+    if ((uint64_t)n > per_sm) return 512;
+    // the fewest warps whose tiles (512 keys per warp) cover n in one tile per SM
+    const uint64_t warps = ((uint64_t)n + (uint64_t)sms() * 32u * kItems - 1) / ((uint64_t)sms() * 32u * kItems);
+    return 32u * (uint32_t)std::min<uint64_t>(32, std::max<uint64_t>(8, warps));
 }
 
 }  // namespace
@@ -324,15 +334,11 @@ int sort_passes(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b, uint32_t* 
         const uint32_t tb = (stall && p == 0) ? 1u : 0u;
         const bool iota = iota_values && p == 0;
         if (digit_bits == 10)
-            launch_pass<10, 256>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, spin, tb, iota, s);
-        else if (digit_bits == 8 && block == 1024)
-            launch_pass<8, 1024>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, spin, tb, iota, s);
+            launch_pass<10, 256>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, spin, tb, iota, block, s);
         else if (digit_bits == 8)
-            launch_pass<8, 512>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, spin, tb, iota, s);
-        else if (block == 1024)
-            launch_pass<6, 1024>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, spin, tb, iota, s);
+            launch_pass<8, 1024>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, spin, tb, iota, block, s);
         else
-            launch_pass<6, 512>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, spin, tb, iota, s);
+            launch_pass<6, 1024>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, spin, tb, iota, block, s);
         cur ^= 1;
     }
     return cur;

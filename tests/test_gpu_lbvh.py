@@ -48,6 +48,34 @@ def test_radix_sort_random(ctx, oracle, n, digit_bits):
     assert np.array_equal(v, ev)
 
 
+@pytest.mark.parametrize("n", [1, 255, 256, 257, 511, 512, 513, 77_777, 300_000])
+def test_codes_and_tree_from_unaligned_device_triangles(ctx, oracle, n):
+    """The bounds and codes kernels stage triangle tiles with bulk copies when
+    the array starts on a 16-byte boundary and with plain loads otherwise
+    (and for a partial last tile): device triangles at a 16-byte and at a
+    4-byte offset give the oracle's codes, scene box and tree."""
+    torch = pytest.importorskip("torch")
+    from sequoia_gb300 import scenes
+    tris = scenes.gaussian_soup(n, 4, seed=n)
+    want_codes, _ = oracle.morton_codes(tris)
+    onodes, oroot, _, _ = oracle.build_morton(tris)
+    want = oracle.canonical_bfs(onodes, oroot)
+    flat = torch.from_numpy(tris.reshape(-1)).cuda()
+    buf = torch.zeros(flat.numel() + 4, dtype=torch.float32, device="cuda")
+    for off in (0, 1, 4):  # 0 and 16 bytes: aligned; 4 bytes: not
+        view = buf[off:off + flat.numel()]
+        view.copy_(flat)
+        codes, _ = ctx.morton_codes(view)
+        assert np.array_equal(codes, want_codes), off
+        bvh = ctx.build(view, "morton")
+        nodes, root = bvh.export_node1()
+        got = oracle.canonical_bfs(nodes, root)
+        assert len(got) == len(want) and np.array_equal(got["child"], want["child"]), off
+        assert np.array_equal(got["min"], want["min"]) and np.array_equal(got["max"], want["max"]), off
+        bvh.free()
+    assert ctx.sync() == 0
+
+
 def test_radix_sort_full_32bit(ctx, oracle):
     rng = np.random.default_rng(5)
     keys = rng.integers(0, 1 << 32, 300_001, dtype=np.uint64).astype(np.uint32)
