@@ -302,9 +302,12 @@ sq_status sq_radix_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* v
  * explicit rays it holds ray_count*3 bytes).  Outputs host or device:
  * device outputs are written on the context's stream and the call returns
  * without waiting; host outputs are complete when the call returns.
- * Page-locked host outputs (cudaHostAlloc / cudaHostRegister) are written by
- * the kernel in place, so their transfer overlaps the trace; pageable host
- * outputs go through a device buffer and one copy.                           */
+ * Page-locked host outputs (cudaHostAlloc / cudaHostRegister) have their
+ * transfer overlap the trace: a camera image of 2^21 rays or more on an
+ * 8-wide tree is traced in row bands into device memory, each band copied
+ * to the host on a side stream while later bands trace; other traces write
+ * them in place from the kernel.  Pageable host outputs go through a device
+ * buffer and one copy.                                                       */
 sq_status sq_trace(sq_ctx* ctx, const sq_bvh* bvh, const sq_ray_source* rays,
                    uint32_t mode, sq_hit* hits, uint8_t* heatmap_rgb);
 
