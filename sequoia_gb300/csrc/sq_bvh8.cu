@@ -583,15 +583,20 @@ int build_bvh8(const Node* rec, uint32_t root, uint32_t leaf0, const float* tris
                const BarrierStall* stall)
 {
     host_ctl[5] = 0;
-    // every block of the cooperative collapse must be resident: the grid is
-    // the occupancy limit (0: no cooperative launch, use the per-level path)
+    // every block of the cooperative collapse must be resident: at most the
+    // occupancy limit per SM (0: no cooperative launch, use the per-level
+    // path).  From 5M triangles up, four blocks per SM instead of the limit
+    // (five): on Gaussian soups the 6M and 8M collapses took 0.61 / 0.76 ms
+    // with four against 0.64 / 0.86 ms with five, while at 1-4M (and the 4M
+    // terrain) five were as fast or faster.
     static PerDevice<int> cache;
-    const int grid = cache.get([] {
-        int coop = 0, per_sm = 0;
+    const int per_sm = cache.get([] {
+        int coop = 0, occ = 0;
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, current_device());
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collapse_coop, 256, 0);
-        return (coop && per_sm > 0) ? per_sm * sm_count() : 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_collapse_coop, 256, 0);
+        return (coop && occ > 0) ? occ : 0;
     });
+    const int grid = (n >= 5000000u && per_sm > 4 ? 4 : per_sm) * sm_count();
     if (grid == 0) return build_bvh8_levels(rec, root, leaf0, tris, n, nodes8, tris8, ws, host_ctl, err, s);
     const uint32_t capacity = bvh8_capacity(n);
     cudaError_t e;

@@ -43,6 +43,9 @@ constexpr int kStackDepth = 24;
 // Large-phase levels of the batched build (device-side counts, no host
 // round trip): deeper work is finished by the small phase.
 constexpr uint32_t kBatchLargeLevels = 24;
+// Large-phase levels a single build queues between two host reads of the
+// task count (even, so the count read is always the next level's).
+constexpr uint32_t kSahLevelsPerCheck = 4;
 
 struct __align__(16) Task {
     uint32_t begin, count, slot, flags;  // flags: bit0 = ids live in buffer B, bit1 = root-like record
@@ -1087,15 +1090,19 @@ int build_sah(const float* tris, uint32_t n, uint32_t nb, uint32_t leaf_size, in
         k_grid_tasks<<<1, 64, 0, s>>>(w.cells, w.root_ord, n, leaf_size, scene_box_cells, w.lists[0], w.small,
                                       w.leaves, w.ctl, scene_out);
     }
-    // large phase, one level per iteration; the host reads the level's task
-    // count to size the grids and to stop
-    for (uint32_t level = 0;; ++level) {
+    // large phase: the level kernels read their task counts on the device
+    // and stride over them with fixed grids, so levels are queued
+    // kSahLevelsPerCheck at a time and the host reads a count (and waits)
+    // only between such groups; levels past the tree's depth find no tasks
+    // and do nothing.  One host round trip per level left the GPU idle for
+    // most of a small mesh's build.
+    const uint32_t grid_fixed = (uint32_t)sms() * 8u;
+    for (uint32_t level = 0;; level += kSahLevelsPerCheck) {
         SQ_TRY(cudaMemcpyAsync(host_ctl, &w.ctl->n_large[level & 1], sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
         SQ_TRY(cudaStreamSynchronize(s));
-        const uint32_t nt = host_ctl[0];
-        if (nt == 0) break;
-        const uint32_t max_chunks = (uint32_t)((size_t)n / kChunk + nt + 1);
-        enqueue_large_level(w, level, (int)nb, base, leaf_size, nodes, max_chunks, (nt + 3) / 4, s);
+        if (host_ctl[0] == 0) break;
+        for (uint32_t j = 0; j < kSahLevelsPerCheck; ++j)
+            enqueue_large_level(w, level + j, (int)nb, base, leaf_size, nodes, grid_fixed, grid_fixed, s);
     }
     // small phase and leaves
     const uint32_t sg = (uint32_t)sms() * 8u;
