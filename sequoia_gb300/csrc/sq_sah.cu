@@ -19,8 +19,8 @@
 // result is record-for-record the oracle's.
 //
 // Schedule:
-//   large nodes (> kSmall triangles): level by level.  Chunks of kChunk
-//     triangles bin into per-warp shared bins (shared-memory atomics on
+//   large nodes (> kSmall triangles): level by level.  Chunks of 256 or
+//     2048 triangles (by mesh size) bin into per-warp shared bins (shared-memory atomics on
 //     order-preserving integer encodings, or full-warp reductions when a
 //     warp's 32 triangles share one bin), then one atomic per bin value and
 //     block; one warp per node sweeps the planes; a count / scan / scatter
@@ -35,7 +35,12 @@ namespace {
 
 using namespace sq;
 
+// Triangles per chunk of a large level: 2048 from 1M triangles up, 256 below
+// (a small mesh then still spreads a level over many blocks; each thread
+// handles one triangle of a chunk instead of eight dependent ones).
 constexpr uint32_t kChunk = 2048;
+constexpr uint32_t kChunkSmall = 256;
+constexpr uint32_t kChunkSmallBelow = 1u << 20;
 constexpr uint32_t kSmall = 128;
 constexpr int kMaxBins = 32;
 constexpr int kBinWords = 13;  // -pmin xyz, pmax xyz, -cmin xyz, cmax xyz (ordered ints), count
@@ -465,6 +470,7 @@ __global__ void k_large_zero(uint32_t* __restrict__ bins, const uint32_t* __rest
         bins[(i / per) * (kMaxBins * kBinWords) + i % per] = 0;
 }
 
+template <uint32_t CHUNK>
 __global__ void k_large_prep(const Task* __restrict__ tasks, const uint32_t* __restrict__ ntp, uint32_t* next_cnt,
                              int nb, Split* __restrict__ split, uint32_t* __restrict__ chunk_start)
 {
@@ -478,7 +484,7 @@ __global__ void k_large_prep(const Task* __restrict__ tasks, const uint32_t* __r
         uint32_t ch = 0;
         if (t < nt) {
             const Task& tk = tasks[t];
-            ch = (tk.count + kChunk - 1) / kChunk;
+            ch = (tk.count + CHUNK - 1) / CHUNK;
             Split s;
             s.axis = choose_axis(tk.cmn, tk.cmx);
             s.cmin = sel(tk.cmn, s.axis);
@@ -513,6 +519,7 @@ __device__ __forceinline__ uint32_t task_of_chunk(const uint32_t* __restrict__ c
     return lo;
 }
 
+template <uint32_t CHUNK>
 __global__ void __launch_bounds__(256) k_large_bin(const Task* __restrict__ tasks, const uint32_t* __restrict__ ntp,
                                                    const Split* __restrict__ split, const uint32_t* __restrict__ chunk_start,
                                                    const uint32_t* __restrict__ ids_a, const uint32_t* __restrict__ ids_b,
@@ -527,8 +534,8 @@ __global__ void __launch_bounds__(256) k_large_bin(const Task* __restrict__ task
         const uint32_t t = task_of_chunk(chunk_start, nt, c);
         const Task tk = tasks[t];
         const Split sp = split[t];
-        const uint32_t off = (c - chunk_start[t]) * kChunk;
-        const uint32_t len = min(kChunk, tk.count - off);
+        const uint32_t off = (c - chunk_start[t]) * CHUNK;
+        const uint32_t len = min(CHUNK, tk.count - off);
         const uint32_t* ids = (tk.flags & 1u) ? ids_b : ids_a;
         for (int j = lane; j < kMaxBins * kBinWords; j += 32) wb[j] = 0;
         __syncwarp();
@@ -597,6 +604,7 @@ __global__ void k_large_split(const Task* __restrict__ tasks, const uint32_t* __
     }
 }
 
+template <uint32_t CHUNK>
 __global__ void __launch_bounds__(256) k_large_count(const Task* __restrict__ tasks, const uint32_t* __restrict__ ntp,
                                                      const Split* __restrict__ split,
                                                      const uint32_t* __restrict__ chunk_start,
@@ -612,8 +620,8 @@ __global__ void __launch_bounds__(256) k_large_count(const Task* __restrict__ ta
         const Split sp = split[t];
         if (sp.plane < 0) continue;  // block-uniform
         const Task tk = tasks[t];
-        const uint32_t off = (c - chunk_start[t]) * kChunk;
-        const uint32_t len = min(kChunk, tk.count - off);
+        const uint32_t off = (c - chunk_start[t]) * CHUNK;
+        const uint32_t len = min(CHUNK, tk.count - off);
         const uint32_t* ids = (tk.flags & 1u) ? ids_b : ids_a;
         uint32_t cnt = 0;
         for (uint32_t j = threadIdx.x; j < len; j += blockDim.x) {
@@ -660,6 +668,7 @@ __global__ void k_large_scan(const Split* __restrict__ split, const uint32_t* __
     }
 }
 
+template <uint32_t CHUNK>
 __global__ void __launch_bounds__(256) k_large_scatter(const Task* __restrict__ tasks, const uint32_t* __restrict__ ntp,
                                                        const Split* __restrict__ split,
                                                        const uint32_t* __restrict__ chunk_start,
@@ -667,7 +676,7 @@ __global__ void __launch_bounds__(256) k_large_scatter(const Task* __restrict__ 
                                                        const float4* __restrict__ tb, int nb,
                                                        const uint32_t* __restrict__ chunk_left)
 {
-    constexpr int kPer = kChunk / 256;  // 8 consecutive elements per thread
+    constexpr int kPer = CHUNK / 256;  // consecutive elements per thread
     __shared__ uint32_t s_w[8];
     const uint32_t nt = *ntp;
     const uint32_t chunks = chunk_start[nt];
@@ -677,8 +686,8 @@ __global__ void __launch_bounds__(256) k_large_scatter(const Task* __restrict__ 
         const Split sp = split[t];
         if (sp.plane < 0) continue;  // block-uniform
         const Task tk = tasks[t];
-        const uint32_t off = (c - chunk_start[t]) * kChunk;
-        const uint32_t len = min(kChunk, tk.count - off);
+        const uint32_t off = (c - chunk_start[t]) * CHUNK;
+        const uint32_t len = min(CHUNK, tk.count - off);
         const uint32_t* in = (tk.flags & 1u) ? ids_b : ids_a;
         uint32_t* out = (tk.flags & 1u) ? ids_a : ids_b;
         uint32_t idv[kPer];
@@ -918,7 +927,7 @@ size_t sah_ws_bytes(uint32_t n, uint32_t meshes)
     add(sizeof(LeafRange) * ((size_t)n + 66 + meshes));  // leaf list (+64 empty grid cells, + empty meshes)
     add(sizeof(Split) * tasks);
     add(sizeof(uint32_t) * (tasks + 1));          // chunk starts
-    add(sizeof(uint32_t) * ((size_t)n / kChunk + tasks + 1));  // chunk left counts
+    add(sizeof(uint32_t) * ((size_t)n / kChunkSmall + tasks + 1));  // chunk left counts
     add(sizeof(uint32_t) * (size_t)kMaxBins * kBinWords * tasks);  // bins
     add(sizeof(uint32_t) * 64 * kBinWords);       // grid cells
     add(sizeof(uint32_t) * 64);                   // grid histogram
@@ -942,7 +951,7 @@ SahWs carve(void* ws, uint32_t n, uint32_t meshes)
     w.leaves = reinterpret_cast<LeafRange*>(take(sizeof(LeafRange) * ((size_t)n + 66 + meshes)));
     w.split = reinterpret_cast<Split*>(take(sizeof(Split) * tasks));
     w.chunk_start = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * (tasks + 1)));
-    w.chunk_left = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * ((size_t)n / kChunk + tasks + 1)));
+    w.chunk_left = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * ((size_t)n / kChunkSmall + tasks + 1)));
     w.bins = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * (size_t)kMaxBins * kBinWords * tasks));
     w.cells = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * 64 * kBinWords));
     w.hist = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * 64));
@@ -955,23 +964,34 @@ SahWs carve(void* ws, uint32_t n, uint32_t meshes)
 // count is ctl->n_large[level & 1] on the device.  chunk_grid / task_blocks:
 // exact grids when the host knows the count, fixed ones otherwise (the
 // kernels loop over whatever the count holds).
-void enqueue_large_level(const SahWs& w, uint32_t level, int nb, uint32_t base, uint32_t leaf_size, Node* nodes,
-                         uint32_t chunk_grid, uint32_t task_blocks, cudaStream_t s)
+template <uint32_t CHUNK>
+void enqueue_level_chunks(const SahWs& w, uint32_t level, int nb, uint32_t base, uint32_t leaf_size, Node* nodes,
+                          uint32_t chunk_grid, uint32_t task_blocks, cudaStream_t s)
 {
     const Task* proc = w.lists[level & 1];
     Task* outl = w.lists[(level + 1) & 1];
     const uint32_t* ntp = &w.ctl->n_large[level & 1];
     uint32_t* next = &w.ctl->n_large[(level + 1) & 1];
     k_large_zero<<<task_blocks, 256, 0, s>>>(w.bins, ntp, nb);
-    k_large_prep<<<1, 1024, 0, s>>>(proc, ntp, next, nb, w.split, w.chunk_start);
-    k_large_bin<<<chunk_grid, 256, 0, s>>>(proc, ntp, w.split, w.chunk_start, w.ids_a, w.ids_b, w.tb, nb, w.bins);
+    k_large_prep<CHUNK><<<1, 1024, 0, s>>>(proc, ntp, next, nb, w.split, w.chunk_start);
+    k_large_bin<CHUNK><<<chunk_grid, 256, 0, s>>>(proc, ntp, w.split, w.chunk_start, w.ids_a, w.ids_b, w.tb, nb, w.bins);
     k_large_split<<<task_blocks, 128, 0, s>>>(proc, ntp, w.split, w.bins, nb, base, leaf_size, nodes, outl, next,
                                               w.small, w.leaves, w.ctl);
-    k_large_count<<<chunk_grid, 256, 0, s>>>(proc, ntp, w.split, w.chunk_start, w.ids_a, w.ids_b, w.tb, nb,
+    k_large_count<CHUNK><<<chunk_grid, 256, 0, s>>>(proc, ntp, w.split, w.chunk_start, w.ids_a, w.ids_b, w.tb, nb,
                                              w.chunk_left);
     k_large_scan<<<task_blocks, 128, 0, s>>>(w.split, ntp, w.chunk_start, w.chunk_left);
-    k_large_scatter<<<chunk_grid, 256, 0, s>>>(proc, ntp, w.split, w.chunk_start, w.ids_a, w.ids_b, w.tb, nb,
+    k_large_scatter<CHUNK><<<chunk_grid, 256, 0, s>>>(proc, ntp, w.split, w.chunk_start, w.ids_a, w.ids_b, w.tb, nb,
                                                w.chunk_left);
+}
+
+// one large level of a build over n triangles (chunk size by n)
+void enqueue_large_level(const SahWs& w, uint32_t level, int nb, uint32_t base, uint32_t leaf_size, Node* nodes,
+                         uint32_t chunk_grid, uint32_t task_blocks, uint32_t n, cudaStream_t s)
+{
+    if (n < kChunkSmallBelow)
+        enqueue_level_chunks<kChunkSmall>(w, level, nb, base, leaf_size, nodes, chunk_grid, task_blocks, s);
+    else
+        enqueue_level_chunks<kChunk>(w, level, nb, base, leaf_size, nodes, chunk_grid, task_blocks, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -1102,7 +1122,7 @@ int build_sah(const float* tris, uint32_t n, uint32_t nb, uint32_t leaf_size, in
         SQ_TRY(cudaStreamSynchronize(s));
         if (host_ctl[0] == 0) break;
         for (uint32_t j = 0; j < kSahLevelsPerCheck; ++j)
-            enqueue_large_level(w, level + j, (int)nb, base, leaf_size, nodes, grid_fixed, grid_fixed, s);
+            enqueue_large_level(w, level + j, (int)nb, base, leaf_size, nodes, grid_fixed, grid_fixed, n, s);
     }
     // small phase and leaves
     const uint32_t sg = (uint32_t)sms() * 8u;
@@ -1138,7 +1158,7 @@ int build_sah_batch(const float* tris, uint32_t n, const uint32_t* off, uint32_t
     k_root_tasks_seg<<<(M + 127) / 128, 128, 0, s>>>(w.root_ord, off, M, leaf_size, root0, w.lists[0], w.small,
                                                       w.leaves, w.ctl);
     for (uint32_t level = 0; level < kBatchLargeLevels; ++level)
-        enqueue_large_level(w, level, (int)nb, 0u, leaf_size, nodes, sm * 8u, sm * 8u, s);
+        enqueue_large_level(w, level, (int)nb, 0u, leaf_size, nodes, sm * 8u, sm * 8u, n, s);
     k_large_to_small<<<sm, 256, 0, s>>>(w.lists[kBatchLargeLevels & 1], &w.ctl->n_large[kBatchLargeLevels & 1],
                                        w.small, w.ctl);
     k_small<<<sm * 8u, 128, 0, s>>>(w.small, w.ctl, w.ids_a, w.ids_b, w.tb, (int)nb, leaf_size, 0u, nodes, leaf0, err);
