@@ -782,6 +782,173 @@ __global__ void k_emit_leaves(const LeafRange* __restrict__ leaves, const Ctl* _
 
 // ---------------------------------------------------------------------------
 // small phase: one warp per subtree
+//
+// A subtree of at most kStage triangles (every small task of a single build:
+// a task turns small at kSmall or fewer) is staged once in the warp's shared
+// memory -- each triangle's box and id -- and its nodes are binned,
+// partitioned and emitted from there: only 16-bit local indices move between
+// the two orders (the buffer parity of the global ids, which the staged
+// subtree no longer writes), and leaves read their boxes from the stage.  A
+// node then costs shared-memory latency instead of two dependent global
+// round trips per 32 triangles.  Larger small tasks (leftovers of the
+// batched build's fixed large levels) read and write the global buffers.
+constexpr uint32_t kStage = 128;
+
+struct SmallStage {
+    float4 box[kStage][2];      // min xyz, max xyz of local triangle k
+    uint32_t gid[kStage];       // its triangle id
+    uint16_t loc[2][kStage];    // local triangles in the order of buffer parity p
+};
+
+template <bool STAGED>
+__device__ void small_subtree(Task cur, SmallStage& sg, Task* st, uint32_t* wb, uint32_t* __restrict__ ids_a,
+                              uint32_t* __restrict__ ids_b, const float4* __restrict__ tb, int nb, uint32_t leaf_size,
+                              uint32_t base, Node* __restrict__ nodes, uint32_t leaf0, uint32_t* err)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t lt = (1u << lane) - 1u;
+    const uint32_t root_begin = cur.begin;
+    // triangle at position `pos` (global) of the order of parity p
+    auto get = [&](uint32_t p, uint32_t pos, uint32_t& id, uint16_t& li, float* mn, float* mx) {
+        if (STAGED) {
+            li = sg.loc[p][pos - root_begin];
+            const float4 a = sg.box[li][0], b = sg.box[li][1];
+            mn[0] = a.x; mn[1] = a.y; mn[2] = a.z;
+            mx[0] = b.x; mx[1] = b.y; mx[2] = b.z;
+            id = sg.gid[li];
+        } else {
+            li = 0;
+            id = (p ? ids_b : ids_a)[pos];
+            load_box(tb, id, mn, mx);
+        }
+    };
+    auto put = [&](uint32_t p, uint32_t pos, uint32_t id, uint16_t li) {
+        if (STAGED) sg.loc[p][pos - root_begin] = li;
+        else (p ? ids_b : ids_a)[pos] = id;
+    };
+    // leaf records of positions [b, b + c) of parity p (warp_emit_leaf's records)
+    auto emit_leaf = [&](uint32_t p, uint32_t b, uint32_t c, uint32_t slot, uint32_t flags, const float* pmn,
+                         const float* pmx) {
+        for (uint32_t j = lane; j < c; j += 32) {
+            uint32_t id;
+            uint16_t li;
+            Box bb;
+            get(p, b + j, id, li, bb.mn, bb.mx);
+            store_node(nodes + leaf0 + b + j, bb, id, 1u, kLeafFlag);
+            if (c == 1 && !(flags & 2u)) store_node(nodes + slot, bb, id, 1u, kLeafFlag);
+        }
+        if (lane == 0 && (c != 1 || (flags & 2u))) {
+            if (c > 65535u) { raise_error(err, SQ_DEVERR_NODE_COUNT); return; }
+            Box pb;
+            for (int a = 0; a < 3; ++a) { pb.mn[a] = pmn[a]; pb.mx[a] = pmx[a]; }
+            store_node(nodes + slot, pb, leaf0 + b, c, 0);
+        }
+    };
+    if (STAGED) {
+        const uint32_t* in0 = (cur.flags & 1u) ? ids_b : ids_a;
+        for (uint32_t j = lane; j < cur.count; j += 32) {
+            const uint32_t id = in0[cur.begin + j];
+            sg.box[j][0] = __ldg(tb + 2ull * id);
+            sg.box[j][1] = __ldg(tb + 2ull * id + 1);
+            sg.gid[j] = id;
+            sg.loc[cur.flags & 1u][j] = (uint16_t)j;
+        }
+        __syncwarp();
+    }
+    int sp = 0;
+    for (;;) {
+        // cur is splittable (count > leaf_size, centroid area > 0)
+        const uint32_t pin = cur.flags & 1u, pout = pin ^ 1u;
+        const int axis = choose_axis(cur.cmn, cur.cmx);
+        const float cmin = sel(cur.cmn, axis);
+        const float k1 = bin_k1(nb, sel(cur.cmx, axis) - cmin);
+        for (int j = lane; j < kMaxBins * kBinWords; j += 32) wb[j] = 0;
+        __syncwarp();
+        for (uint32_t j0 = 0; j0 < cur.count; j0 += 32) {
+            const uint32_t j = j0 + lane;
+            float mn[3], mx[3], cc[3];
+            int bin = nb;
+            if (j < cur.count) {
+                uint32_t id;
+                uint16_t li;
+                get(pin, cur.begin + j, id, li, mn, mx);
+                for (int a = 0; a < 3; ++a) cc[a] = (mn[a] + mx[a]) * 0.5f;
+                bin = bin_of(k1, sel(cc, axis), cmin, nb);
+            } else {
+                for (int a = 0; a < 3; ++a) { mn[a] = mx[a] = cc[a] = 0.0f; }
+            }
+            warp_bin_add(wb, bin, nb, mn, mx, cc);
+        }
+        const PlaneResult r = warp_choose_plane(wb, nb);
+        __syncwarp();
+        bool have_next = false;
+        if (r.plane < 0 || r.nl == 0 || r.nl == cur.count) {
+            // no plane scored below FLT_MAX: leaf
+            emit_leaf(pin, cur.begin, cur.count, cur.slot, cur.flags, cur.pmn, cur.pmx);
+        } else {
+            const uint32_t q = cur.begin + r.nl;
+            if (lane == 0) {
+                Box pb;
+                for (int a = 0; a < 3; ++a) { pb.mn[a] = cur.pmn[a]; pb.mx[a] = cur.pmx[a]; }
+                store_node(nodes + cur.slot, pb, base + 2u * q, 2u, 0);
+            }
+            // stable partition into the other order
+            uint32_t lc = 0, rc = 0;
+            for (uint32_t j0 = 0; j0 < cur.count; j0 += 32) {
+                const uint32_t j = j0 + lane;
+                const bool valid = j < cur.count;
+                uint32_t id = 0;
+                uint16_t li = 0;
+                bool left = false;
+                if (valid) {
+                    float mn[3], mx[3];
+                    get(pin, cur.begin + j, id, li, mn, mx);
+                    const float cc = (sel(mn, axis) + sel(mx, axis)) * 0.5f;
+                    left = bin_of(k1, cc, cmin, nb) <= r.plane;
+                }
+                const uint32_t lb = __ballot_sync(0xFFFFFFFFu, valid && left);
+                const uint32_t rb = __ballot_sync(0xFFFFFFFFu, valid && !left);
+                if (valid) {
+                    if (left) put(pout, cur.begin + lc + __popc(lb & lt), id, li);
+                    else put(pout, q + rc + __popc(rb & lt), id, li);
+                }
+                lc += __popc(lb);
+                rc += __popc(rb);
+            }
+            __syncwarp();
+            Task ch[2] = {child_task(cur.begin, r.nl, base + 2u * q, pout, r.lp, r.lc),
+                          child_task(q, cur.count - r.nl, base + 2u * q + 1u, pout, r.rp, r.rc)};
+            bool split_ch[2];
+            for (int k = 0; k < 2; ++k) {
+                split_ch[k] = !(ch[k].count <= leaf_size || !(box_sa(ch[k].cmn, ch[k].cmx) > 0.0f));
+                if (!split_ch[k]) emit_leaf(pout, ch[k].begin, ch[k].count, ch[k].slot, ch[k].flags, ch[k].pmn, ch[k].pmx);
+            }
+            if (split_ch[0] && split_ch[1]) {
+                const int small_k = ch[0].count <= ch[1].count ? 0 : 1;
+                if (sp >= kStackDepth) {
+                    raise_error(err, SQ_DEVERR_SAH_QUEUE);
+                    return;
+                }
+                if (lane == 0) st[sp] = ch[1 - small_k];
+                sp++;
+                __syncwarp();
+                cur = ch[small_k];
+                have_next = true;
+            } else if (split_ch[0] || split_ch[1]) {
+                cur = split_ch[0] ? ch[0] : ch[1];
+                have_next = true;
+            }
+        }
+        if (!have_next) {
+            if (sp == 0) break;
+            --sp;
+            __syncwarp();
+            cur = st[sp];
+            __syncwarp();
+        }
+    }
+    __syncwarp();  // the stage is reused by the warp's next subtree
+}
 
 __global__ void __launch_bounds__(128) k_small(const Task* __restrict__ small, Ctl* ctl, uint32_t* __restrict__ ids_a,
                                                uint32_t* __restrict__ ids_b, const float4* __restrict__ tb, int nb,
@@ -790,111 +957,21 @@ __global__ void __launch_bounds__(128) k_small(const Task* __restrict__ small, C
 {
     __shared__ uint32_t s_bins[4][kMaxBins * kBinWords];
     __shared__ Task s_stack[4][kStackDepth];
+    __shared__ SmallStage s_stage[4];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t* wb = s_bins[warp];
-    Task* st = s_stack[warp];
     const uint32_t total = ctl->n_small;
-    const uint32_t lt = (1u << lane) - 1u;
     for (;;) {
         uint32_t ti = 0;
         if (lane == 0) ti = atomicAdd(&ctl->small_pop, 1u);
         ti = __shfl_sync(0xFFFFFFFFu, ti, 0);
         if (ti >= total) return;
-        Task cur = small[ti];
-        int sp = 0;
-        for (;;) {
-            // cur is splittable (count > leaf_size, centroid area > 0)
-            const uint32_t* in = (cur.flags & 1u) ? ids_b : ids_a;
-            uint32_t* out = (cur.flags & 1u) ? ids_a : ids_b;
-            const int axis = choose_axis(cur.cmn, cur.cmx);
-            const float cmin = sel(cur.cmn, axis);
-            const float k1 = bin_k1(nb, sel(cur.cmx, axis) - cmin);
-            for (int j = lane; j < kMaxBins * kBinWords; j += 32) wb[j] = 0;
-            __syncwarp();
-            for (uint32_t j0 = 0; j0 < cur.count; j0 += 32) {
-                const uint32_t j = j0 + lane;
-                float mn[3], mx[3], cc[3];
-                int bin = nb;
-                if (j < cur.count) {
-                    load_box(tb, in[cur.begin + j], mn, mx);
-                    for (int a = 0; a < 3; ++a) cc[a] = (mn[a] + mx[a]) * 0.5f;
-                    bin = bin_of(k1, sel(cc, axis), cmin, nb);
-                } else {
-                    for (int a = 0; a < 3; ++a) { mn[a] = mx[a] = cc[a] = 0.0f; }
-                }
-                warp_bin_add(wb, bin, nb, mn, mx, cc);
-            }
-            const PlaneResult r = warp_choose_plane(wb, nb);
-            __syncwarp();
-            bool have_next = false;
-            if (r.plane < 0 || r.nl == 0 || r.nl == cur.count) {
-                // no plane scored below FLT_MAX: leaf
-                warp_emit_leaf(in, cur.begin, cur.count, cur.slot, cur.flags, cur.pmn, cur.pmx, tb, nodes, leaf0, err);
-            } else {
-                const uint32_t q = cur.begin + r.nl;
-                if (lane == 0) {
-                    Box pb;
-                    for (int a = 0; a < 3; ++a) { pb.mn[a] = cur.pmn[a]; pb.mx[a] = cur.pmx[a]; }
-                    store_node(nodes + cur.slot, pb, base + 2u * q, 2u, 0);
-                }
-                // stable partition into the other buffer
-                uint32_t lc = 0, rc = 0;
-                for (uint32_t j0 = 0; j0 < cur.count; j0 += 32) {
-                    const uint32_t j = j0 + lane;
-                    const bool valid = j < cur.count;
-                    uint32_t id = 0;
-                    bool left = false;
-                    if (valid) {
-                        id = in[cur.begin + j];
-                        float mn[3], mx[3];
-                        load_box(tb, id, mn, mx);
-                        const float cc = (sel(mn, axis) + sel(mx, axis)) * 0.5f;
-                        left = bin_of(k1, cc, cmin, nb) <= r.plane;
-                    }
-                    const uint32_t lb = __ballot_sync(0xFFFFFFFFu, valid && left);
-                    const uint32_t rb = __ballot_sync(0xFFFFFFFFu, valid && !left);
-                    if (valid) {
-                        if (left) out[cur.begin + lc + __popc(lb & lt)] = id;
-                        else out[q + rc + __popc(rb & lt)] = id;
-                    }
-                    lc += __popc(lb);
-                    rc += __popc(rb);
-                }
-                __syncwarp();
-                const uint32_t buf = (cur.flags & 1u) ^ 1u;
-                Task ch[2] = {child_task(cur.begin, r.nl, base + 2u * q, buf, r.lp, r.lc),
-                              child_task(q, cur.count - r.nl, base + 2u * q + 1u, buf, r.rp, r.rc)};
-                bool split_ch[2];
-                for (int k = 0; k < 2; ++k) {
-                    split_ch[k] = !(ch[k].count <= leaf_size || !(box_sa(ch[k].cmn, ch[k].cmx) > 0.0f));
-                    if (!split_ch[k])
-                        warp_emit_leaf(out, ch[k].begin, ch[k].count, ch[k].slot, ch[k].flags, ch[k].pmn, ch[k].pmx, tb,
-                                       nodes, leaf0, err);
-                }
-                if (split_ch[0] && split_ch[1]) {
-                    const int small_k = ch[0].count <= ch[1].count ? 0 : 1;
-                    if (sp >= kStackDepth) {
-                        raise_error(err, SQ_DEVERR_SAH_QUEUE);
-                        return;
-                    }
-                    if (lane == 0) st[sp] = ch[1 - small_k];
-                    sp++;
-                    __syncwarp();
-                    cur = ch[small_k];
-                    have_next = true;
-                } else if (split_ch[0] || split_ch[1]) {
-                    cur = split_ch[0] ? ch[0] : ch[1];
-                    have_next = true;
-                }
-            }
-            if (!have_next) {
-                if (sp == 0) break;
-                --sp;
-                __syncwarp();
-                cur = st[sp];
-                __syncwarp();
-            }
-        }
+        const Task cur = small[ti];
+        if (cur.count <= kStage)
+            small_subtree<true>(cur, s_stage[warp], s_stack[warp], s_bins[warp], ids_a, ids_b, tb, nb, leaf_size, base,
+                                nodes, leaf0, err);
+        else
+            small_subtree<false>(cur, s_stage[warp], s_stack[warp], s_bins[warp], ids_a, ids_b, tb, nb, leaf_size, base,
+                                 nodes, leaf0, err);
     }
 }
 
