@@ -6,6 +6,8 @@
 // reference's own comparisons (see ref_min / ref_max / simd_max below).
 #pragma once
 
+#include <utility>
+
 #include <array>
 #include <atomic>
 #include <cfloat>
@@ -251,6 +253,33 @@ inline int blocks_per_sm(Kernel kernel, int threads)
     int n = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, 0);
     return n > 0 ? n : 1;
+}
+
+// Programmatic dependent launch (chains of short kernels on one stream): a
+// kernel launched with launch_chained may start while the kernel before it
+// on the stream is still running; it calls chain_wait() before its first
+// access to anything the earlier kernel writes (the wait returns once that
+// kernel has completed and its writes are visible, as at a kernel boundary)
+// and chain_release() to let the next kernel start launching.  Without a
+// chained launch both are no-ops.
+__device__ __forceinline__ void chain_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void chain_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <class... KArgs, class... Args>
+inline cudaError_t launch_chained(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                                  Args&&... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
 // Trace statistics of one warp (box tests, triangle tests, requested bytes,

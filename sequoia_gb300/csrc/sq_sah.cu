@@ -464,6 +464,8 @@ __device__ __forceinline__ Task child_task(uint32_t begin, uint32_t count, uint3
 
 __global__ void k_large_zero(uint32_t* __restrict__ bins, const uint32_t* __restrict__ ntp, int nb)
 {
+    chain_wait();  // a chained launch (enqueue_level_chunks)
+    chain_release();
     const size_t per = (size_t)nb * kBinWords;
     const size_t words = (size_t)(*ntp) * per;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < words; i += (size_t)gridDim.x * blockDim.x)
@@ -474,6 +476,8 @@ template <uint32_t CHUNK>
 __global__ void k_large_prep(const Task* __restrict__ tasks, const uint32_t* __restrict__ ntp, uint32_t* next_cnt,
                              int nb, Split* __restrict__ split, uint32_t* __restrict__ chunk_start)
 {
+    chain_wait();  // a chained launch (enqueue_level_chunks)
+    chain_release();
     // single block: chunk counts and their exclusive scan
     __shared__ uint32_t s_sum[1024];
     const uint32_t nt = *ntp;
@@ -525,6 +529,8 @@ __global__ void __launch_bounds__(256) k_large_bin(const Task* __restrict__ task
                                                    const uint32_t* __restrict__ ids_a, const uint32_t* __restrict__ ids_b,
                                                    const float4* __restrict__ tb, int nb, uint32_t* __restrict__ bins_g)
 {
+    chain_wait();  // a chained launch (enqueue_level_chunks)
+    chain_release();
     __shared__ uint32_t s_wb[8][kMaxBins * kBinWords];
     const uint32_t nt = *ntp;
     const uint32_t chunks = chunk_start[nt];
@@ -571,6 +577,8 @@ __global__ void k_large_split(const Task* __restrict__ tasks, const uint32_t* __
                               Node* __restrict__ nodes, Task* large_next, uint32_t* next_cnt, Task* small,
                               LeafRange* leaves, Ctl* ctl)
 {
+    chain_wait();  // a chained launch (enqueue_level_chunks)
+    chain_release();
     const uint32_t nt = *ntp;
     const int lane = threadIdx.x & 31;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
@@ -612,6 +620,8 @@ __global__ void __launch_bounds__(256) k_large_count(const Task* __restrict__ ta
                                                      const float4* __restrict__ tb, int nb,
                                                      uint32_t* __restrict__ chunk_left)
 {
+    chain_wait();  // a chained launch (enqueue_level_chunks)
+    chain_release();
     __shared__ uint32_t s[8];
     const uint32_t nt = *ntp;
     const uint32_t chunks = chunk_start[nt];
@@ -647,6 +657,8 @@ __global__ void __launch_bounds__(256) k_large_count(const Task* __restrict__ ta
 __global__ void k_large_scan(const Split* __restrict__ split, const uint32_t* __restrict__ ntp,
                              const uint32_t* __restrict__ chunk_start, uint32_t* __restrict__ chunk_left)
 {
+    chain_wait();  // a chained launch (enqueue_level_chunks)
+    chain_release();
     const uint32_t nt = *ntp;
     const int lane = threadIdx.x & 31;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
@@ -676,6 +688,8 @@ __global__ void __launch_bounds__(256) k_large_scatter(const Task* __restrict__ 
                                                        const float4* __restrict__ tb, int nb,
                                                        const uint32_t* __restrict__ chunk_left)
 {
+    chain_wait();  // a chained launch (enqueue_level_chunks)
+    chain_release();
     constexpr int kPer = CHUNK / 256;  // consecutive elements per thread
     __shared__ uint32_t s_w[8];
     const uint32_t nt = *ntp;
@@ -1049,16 +1063,23 @@ void enqueue_level_chunks(const SahWs& w, uint32_t level, int nb, uint32_t base,
     Task* outl = w.lists[(level + 1) & 1];
     const uint32_t* ntp = &w.ctl->n_large[level & 1];
     uint32_t* next = &w.ctl->n_large[(level + 1) & 1];
-    k_large_zero<<<task_blocks, 256, 0, s>>>(w.bins, ntp, nb);
-    k_large_prep<CHUNK><<<1, 1024, 0, s>>>(proc, ntp, next, nb, w.split, w.chunk_start);
-    k_large_bin<CHUNK><<<chunk_grid, 256, 0, s>>>(proc, ntp, w.split, w.chunk_start, w.ids_a, w.ids_b, w.tb, nb, w.bins);
-    k_large_split<<<task_blocks, 128, 0, s>>>(proc, ntp, w.split, w.bins, nb, base, leaf_size, nodes, outl, next,
-                                              w.small, w.leaves, w.ctl);
-    k_large_count<CHUNK><<<chunk_grid, 256, 0, s>>>(proc, ntp, w.split, w.chunk_start, w.ids_a, w.ids_b, w.tb, nb,
-                                             w.chunk_left);
-    k_large_scan<<<task_blocks, 128, 0, s>>>(w.split, ntp, w.chunk_start, w.chunk_left);
-    k_large_scatter<CHUNK><<<chunk_grid, 256, 0, s>>>(proc, ntp, w.split, w.chunk_start, w.ids_a, w.ids_b, w.tb, nb,
-                                               w.chunk_left);
+    // seven short kernels per level, chained: each may launch while the one
+    // before it runs and waits for it on the device (chain_wait)
+    launch_chained(k_large_zero, dim3(task_blocks), dim3(256), 0, s, w.bins, ntp, nb);
+    launch_chained(k_large_prep<CHUNK>, dim3(1), dim3(1024), 0, s, proc, ntp, next, nb, w.split, w.chunk_start);
+    launch_chained(k_large_bin<CHUNK>, dim3(chunk_grid), dim3(256), 0, s, proc, ntp, (const Split*)w.split,
+                   (const uint32_t*)w.chunk_start, (const uint32_t*)w.ids_a, (const uint32_t*)w.ids_b,
+                   (const float4*)w.tb, nb, w.bins);
+    launch_chained(k_large_split, dim3(task_blocks), dim3(128), 0, s, proc, ntp, w.split, (const uint32_t*)w.bins, nb,
+                   base, leaf_size, nodes, outl, next, w.small, w.leaves, w.ctl);
+    launch_chained(k_large_count<CHUNK>, dim3(chunk_grid), dim3(256), 0, s, proc, ntp, (const Split*)w.split,
+                   (const uint32_t*)w.chunk_start, (const uint32_t*)w.ids_a, (const uint32_t*)w.ids_b,
+                   (const float4*)w.tb, nb, w.chunk_left);
+    launch_chained(k_large_scan, dim3(task_blocks), dim3(128), 0, s, (const Split*)w.split, ntp,
+                   (const uint32_t*)w.chunk_start, w.chunk_left);
+    launch_chained(k_large_scatter<CHUNK>, dim3(chunk_grid), dim3(256), 0, s, proc, ntp, (const Split*)w.split,
+                   (const uint32_t*)w.chunk_start, w.ids_a, w.ids_b, (const float4*)w.tb, nb,
+                   (const uint32_t*)w.chunk_left);
 }
 
 // one large level of a build over n triangles (chunk size by n)
