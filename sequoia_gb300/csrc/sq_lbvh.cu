@@ -182,6 +182,8 @@ __device__ __forceinline__ float warp_max(float v)
 __global__ void __launch_bounds__(256) k_scene_bounds(const float* __restrict__ tris, uint32_t n, uint32_t mode,
                                                       uint32_t* __restrict__ box_ord, bool aligned, uint32_t* err)
 {
+    chain_wait();  // a chained launch (the build's kernels follow one another)
+    chain_release();
     __shared__ float s_red[8][6];
     float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
     for_each_tile(tris, n, aligned, err, [&](const float* s_tri, uint32_t, uint32_t count) {
@@ -235,6 +237,8 @@ __global__ void __launch_bounds__(256) k_morton(const float* __restrict__ tris, 
                                                 uint32_t* __restrict__ vals, uint32_t* __restrict__ hist, bool aligned,
                                                 uint32_t* err)
 {
+    chain_wait();  // a chained launch (the build's kernels follow one another)
+    chain_release();
     constexpr int RADIX = 1 << DB;
     __shared__ uint32_t s_hist[PASSES * RADIX];
     for (int j = threadIdx.x; j < PASSES * RADIX; j += blockDim.x) s_hist[j] = 0;
@@ -394,6 +398,8 @@ __global__ void __launch_bounds__(256, 6) k_lbvh_climb(const Code* __restrict__ 
                                                     uint32_t* __restrict__ surv_count, const uint32_t* __restrict__ off,
                                                     uint32_t M, uint32_t root0, uint32_t* err)
 {
+    chain_wait();  // a chained launch (the build's kernels follow one another)
+    chain_release();
     constexpr uint32_t FULL = 0xFFFFFFFFu;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = (int)(threadIdx.x & 31u);
@@ -565,6 +571,8 @@ __global__ void __launch_bounds__(256) k_lbvh_global(const uint32_t* __restrict_
                                                      float4* __restrict__ info, const uint32_t* __restrict__ off,
                                                      uint32_t M, uint32_t root0, uint32_t* err)
 {
+    chain_wait();  // a chained launch (the build's kernels follow one another)
+    chain_release();
     const uint32_t leaf0 = 2u * n + 2u;
     const uint32_t count = *surv_count;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
@@ -646,7 +654,7 @@ void scene_bounds(const float* tris, uint32_t n, uint32_t mode, uint32_t* box_or
     const bool aligned = (reinterpret_cast<uintptr_t>(tris) & 15u) == 0;
     const uint32_t tiles = (n + kTileTris - 1) / kTileTris;
     const uint32_t grid = min(tiles, (uint32_t)sms() * 8u);
-    k_scene_bounds<<<grid, 256, 0, s>>>(tris, n, mode, box_ord, aligned, err);
+    launch_chained(k_scene_bounds, dim3(grid), dim3(256), 0, s, tris, n, mode, box_ord, aligned, err);
 }
 
 void morton_codes(const float* tris, uint32_t n, uint32_t mode, const uint32_t* box_ord, uint32_t* keys, uint32_t* vals,
@@ -657,11 +665,11 @@ void morton_codes(const float* tris, uint32_t n, uint32_t mode, const uint32_t* 
     const uint32_t tiles = (n + kTileTris - 1) / kTileTris;
     const uint32_t grid = min(tiles, (uint32_t)sms() * 8u);
     if (digit_bits == 8 && passes == 4)
-        k_morton<8, 4><<<grid, 256, 0, s>>>(tris, n, mode, box_ord, keys, vals, hist, aligned, err);
+        launch_chained(k_morton<8, 4>, dim3(grid), dim3(256), 0, s, tris, n, mode, box_ord, keys, vals, hist, aligned, err);
     else if (digit_bits == 10 && passes == 3)
-        k_morton<10, 3><<<grid, 256, 0, s>>>(tris, n, mode, box_ord, keys, vals, hist, aligned, err);
+        launch_chained(k_morton<10, 3>, dim3(grid), dim3(256), 0, s, tris, n, mode, box_ord, keys, vals, hist, aligned, err);
     else if (digit_bits == 6 && passes == 5)
-        k_morton<6, 5><<<grid, 256, 0, s>>>(tris, n, mode, box_ord, keys, vals, hist, aligned, err);
+        launch_chained(k_morton<6, 5>, dim3(grid), dim3(256), 0, s, tris, n, mode, box_ord, keys, vals, hist, aligned, err);
 }
 
 void morton_codes64(const float* tris, uint32_t n, const uint32_t* box_ord, uint32_t* lo, uint32_t* hi,
@@ -694,8 +702,8 @@ void climb_launch(const Code* codes, const uint32_t* perm, const float* tris, ui
                   uint32_t root0, uint32_t* err, cudaStream_t s)
 {
     if (n == 0) return;
-    k_lbvh_climb<Code, SEG><<<(n + 255) / 256, 256, 0, s>>>(codes, perm, tris, n, nodes, info, surv, surv_count, off, M,
-                                                            root0, err);
+    launch_chained(k_lbvh_climb<Code, SEG>, dim3((n + 255) / 256), dim3(256), 0, s, codes, perm, tris, n, nodes, info, surv,
+                   surv_count, off, M, root0, err);
     // one thread per open node, all at once: the climbs are chains of round
     // trips, so running them side by side beats a grid-stride loop over fewer
     // threads.  Their count is on the device; a warp of 32 positions leaves
@@ -703,7 +711,8 @@ void climb_launch(const Code* codes, const uint32_t* perm, const float* tris, ui
     // a block per SM cover them without launching blocks that find nothing
     // to do (the loop is grid-stride, so any count is processed)
     const uint32_t grid = std::min((n + 255u) / 256u, (n / 6u + 255u) / 256u + (uint32_t)sms());
-    k_lbvh_global<Code, SEG><<<grid, 256, 0, s>>>(surv, surv_count, n, nodes, flags, info, off, M, root0, err);
+    launch_chained(k_lbvh_global<Code, SEG>, dim3(grid), dim3(256), 0, s, surv, surv_count, n, nodes, flags, info, off,
+                   M, root0, err);
 }
 
 void lbvh_climb(const uint32_t* codes, const uint32_t* perm, const float* tris, uint32_t n, sq::Node* nodes,

@@ -103,6 +103,8 @@ __global__ void __launch_bounds__(MAXB, 1024 / MAXB) k_onesweep(const uint32_t* 
                                                      uint32_t* __restrict__ lookback, uint32_t* __restrict__ counter,
                                                      uint32_t* err, uint32_t spin_limit, uint32_t tile_base, bool iota)
 {
+    chain_wait();  // a chained launch (passes follow one another)
+    chain_release();
     constexpr int RADIX = 1 << DB;
     constexpr uint32_t MASK = RADIX - 1;
     const int kBlock = (int)blockDim.x, kWarps = kBlock >> 5, kTile = kBlock * kItems;
@@ -269,8 +271,8 @@ void launch_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint3
     const uint32_t tile = block * kItems;
     const uint32_t tiles = (n + tile - 1) / tile;
     if (tiles <= tile_base) return;
-    k_onesweep<DB, MAXB><<<tiles - tile_base, block, smem_bytes(DB, (int)block), s>>>(
-        kin, vin, kout, vout, n, shift, hist, lookback, counter, err, spin_limit, tile_base, iota);
+    launch_chained(k_onesweep<DB, MAXB>, dim3(tiles - tile_base), dim3(block), smem_bytes(DB, (int)block), s, kin, vin,
+                   kout, vout, n, shift, hist, lookback, counter, err, spin_limit, tile_base, iota);
 }
 
 int sms() { return sm_count(); }
