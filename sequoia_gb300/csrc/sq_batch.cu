@@ -86,6 +86,8 @@ __global__ void __launch_bounds__(256) k_seg_bounds(const float* __restrict__ tr
                                                     const uint32_t* __restrict__ off, uint32_t M,
                                                     uint32_t* __restrict__ box_ord)
 {
+    chain_wait();  // a chained launch (the batch build's kernels follow one another)
+    chain_release();
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
         const bool valid = i < n;
@@ -112,6 +114,8 @@ __global__ void __launch_bounds__(256) k_seg_morton(const float* __restrict__ tr
                                                     uint32_t* __restrict__ vals, uint32_t* __restrict__ code_by_tri,
                                                     uint32_t* __restrict__ hist, uint32_t db, uint32_t passes)
 {
+    chain_wait();  // a chained launch (the batch build's kernels follow one another)
+    chain_release();
     extern __shared__ uint32_t s_hist[];
     const uint32_t radix = 1u << db;
     for (uint32_t j = threadIdx.x; j < passes * radix; j += blockDim.x) s_hist[j] = 0;
@@ -148,6 +152,8 @@ __global__ void __launch_bounds__(256) k_seg_morton(const float* __restrict__ tr
 __global__ void k_mesh_keys(const uint32_t* __restrict__ vals, uint32_t n, const uint32_t* __restrict__ off, uint32_t M,
                             uint32_t* __restrict__ mkeys)
 {
+    chain_wait();  // a chained launch (the batch build's kernels follow one another)
+    chain_release();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         mkeys[i] = mesh_of(off, M, vals[i]);
 }
@@ -155,6 +161,8 @@ __global__ void k_mesh_keys(const uint32_t* __restrict__ vals, uint32_t n, const
 __global__ void k_gather_codes(const uint32_t* __restrict__ perm, uint32_t n, const uint32_t* __restrict__ code_by_tri,
                                uint32_t* __restrict__ codes)
 {
+    chain_wait();  // a chained launch (the batch build's kernels follow one another)
+    chain_release();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         codes[i] = code_by_tri[perm[i]];
 }
@@ -163,6 +171,8 @@ __global__ void k_gather_codes(const uint32_t* __restrict__ perm, uint32_t n, co
 __global__ void k_empty_roots(const uint32_t* __restrict__ off, uint32_t M, Node* __restrict__ nodes, uint32_t root0,
                               uint32_t leaf0)
 {
+    chain_wait();  // a chained launch (the batch build's kernels follow one another)
+    chain_release();
     for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
         if (off[m + 1] != off[m]) continue;
         Box b;
@@ -213,25 +223,28 @@ sq_status enqueue_run(sq_batch* b)
         if (rc) return fail(c, SQ_ERR_CUDA, "batch SAH build: %s", cudaGetErrorString((cudaError_t)rc));
     } else if (N > 0) {
         const uint32_t g = min((N + 255) / 256, (uint32_t)sms() * 8u);
-        k_seg_bounds<<<g, 256, 0, s>>>(b->d_tris, N, b->d_off, M, box_ord);
-        k_seg_morton<<<g, 256, sizeof(uint32_t) * passes * radix, s>>>(b->d_tris, N, b->d_off, M, box_ord, ka, va,
-                                                                      code_by_tri, hist, db, passes);
+        launch_chained(k_seg_bounds, dim3(g), dim3(256), 0, s, (const float*)b->d_tris, N, (const uint32_t*)b->d_off, M,
+                       box_ord);
+        launch_chained(k_seg_morton, dim3(g), dim3(256), sizeof(uint32_t) * passes * radix, s, (const float*)b->d_tris, N,
+                       (const uint32_t*)b->d_off, M, (const uint32_t*)box_ord, ka, va, code_by_tri, hist, db, passes);
         int w = sqk::sort_passes(ka, va, kb, vb, N, hist, lb, ctr, db, passes, c->ctrl, s);
         uint32_t* sv = w ? vb : va;   // values sorted by code
         uint32_t* mk = w ? ka : kb;   // free key buffer for the mesh keys
         uint32_t* ok = w ? kb : ka;
         uint32_t* ov = w ? va : vb;
-        k_mesh_keys<<<g, 256, 0, s>>>(sv, N, b->d_off, M, mk);
+        launch_chained(k_mesh_keys, dim3(g), dim3(256), 0, s, (const uint32_t*)sv, N, (const uint32_t*)b->d_off, M, mk);
         sqk::sort_histogram(mk, N, hist_m, 8, mp, s);
         const int w2 = sqk::sort_passes(mk, sv, ok, ov, N, hist_m, lb_m, ctr + 8, 8, mp, c->ctrl, s);
         uint32_t* perm = w2 ? ov : sv;
-        k_gather_codes<<<g, 256, 0, s>>>(perm, N, code_by_tri, codes);
+        launch_chained(k_gather_codes, dim3(g), dim3(256), 0, s, (const uint32_t*)perm, N, (const uint32_t*)code_by_tri,
+                       codes);
         // the climb of a single build, per mesh segment; the open-node list
         // after the codes, its count in mesh 0's two spare box words
         sqk::lbvh_climb_seg(codes, perm, b->d_tris, N, b->d_off, M, 3u * N + 2u, b->d_nodes, flags, b->d_info,
                             codes + N, box_ord + 6, c->ctrl, s);
     }
-    k_empty_roots<<<(M + 255) / 256, 256, 0, s>>>(b->d_off, M, b->d_nodes, 3u * N + 2u, 2u * N + 2u);
+    launch_chained(k_empty_roots, dim3((M + 255) / 256), dim3(256), 0, s, (const uint32_t*)b->d_off, M, b->d_nodes,
+                   3u * N + 2u, 2u * N + 2u);
     const bool wide = b->params.wide != 0;
     if (wide) {
         const int rc = sqk::build_bvh8_queue(b->d_nodes, b->d_roots, M, 2u * N + 2u, b->d_tris, N, b->d_nodes8,

@@ -345,6 +345,8 @@ __global__ void __launch_bounds__(128) k_collapse_fixed(const Node* __restrict__
                                                         uint32_t* __restrict__ counters2, Node8* __restrict__ nodes8,
                                                         float4* __restrict__ tris8, uint32_t capacity, uint32_t* err)
 {
+    chain_wait();  // a chained launch: the levels follow one another
+    chain_release();
     const uint32_t ntasks = counts[level];
     if (ntasks == 0) return;
     if (level + 1 >= kFixedLevels) {
@@ -524,9 +526,9 @@ int build_bvh8_queue(const Node* rec, const uint32_t* roots_dev, uint32_t nroots
         uint32_t* in_n = (level & 1) ? nb : na;
         uint32_t* out_t = (level & 1) ? ta : tb;
         uint32_t* out_n = (level & 1) ? na : nb;
-        k_collapse_fixed<<<grid, 128, 0, s>>>(rec, leaf0, tris, level, counts, in_t, in_n, out_t, out_n, ws,
-                                              static_cast<Node8*>(nodes8), static_cast<float4*>(tris8),
-                                              capacity, err);
+        launch_chained(k_collapse_fixed, dim3(grid), dim3(128), 0, s, rec, leaf0, tris, level, counts,
+                       (const uint32_t*)in_t, (const uint32_t*)in_n, out_t, out_n, ws, static_cast<Node8*>(nodes8),
+                       static_cast<float4*>(tris8), capacity, err);
     }
     return (int)cudaGetLastError();
 }
