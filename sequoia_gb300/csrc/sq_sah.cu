@@ -79,7 +79,7 @@ struct Split {
 // device, so a level needs no host round trip.
 struct Ctl {
     uint32_t n_large[2], n_small, n_leaf;
-    uint32_t small_pop, err_bits, pad[2];
+    uint32_t small_pop, err_bits, big_pop, pad;  // pop counters of the staged and the unstaged small kernels
 };
 static_assert(sizeof(Ctl) == 32, "Ctl is 32 bytes");
 
@@ -964,6 +964,12 @@ __device__ void small_subtree(Task cur, SmallStage& sg, Task* st, uint32_t* wb, 
     __syncwarp();  // the stage is reused by the warp's next subtree
 }
 
+// One warp per small task: STAGED takes the tasks of at most kStage
+// triangles (all of a single build's), the other kernel the rest (leftovers
+// of the batched build's fixed large levels); each kernel pops the shared
+// list with its own counter and skips the other's tasks.  Two kernels, so
+// the staged one keeps its own, smaller register count.
+template <bool STAGED>
 __global__ void __launch_bounds__(128) k_small(const Task* __restrict__ small, Ctl* ctl, uint32_t* __restrict__ ids_a,
                                                uint32_t* __restrict__ ids_b, const float4* __restrict__ tb, int nb,
                                                uint32_t leaf_size, uint32_t base, Node* __restrict__ nodes,
@@ -971,21 +977,19 @@ __global__ void __launch_bounds__(128) k_small(const Task* __restrict__ small, C
 {
     __shared__ uint32_t s_bins[4][kMaxBins * kBinWords];
     __shared__ Task s_stack[4][kStackDepth];
-    __shared__ SmallStage s_stage[4];
+    __shared__ SmallStage s_stage[STAGED ? 4 : 1];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t total = ctl->n_small;
+    uint32_t* pop = STAGED ? &ctl->small_pop : &ctl->big_pop;
     for (;;) {
         uint32_t ti = 0;
-        if (lane == 0) ti = atomicAdd(&ctl->small_pop, 1u);
+        if (lane == 0) ti = atomicAdd(pop, 1u);
         ti = __shfl_sync(0xFFFFFFFFu, ti, 0);
         if (ti >= total) return;
         const Task cur = small[ti];
-        if (cur.count <= kStage)
-            small_subtree<true>(cur, s_stage[warp], s_stack[warp], s_bins[warp], ids_a, ids_b, tb, nb, leaf_size, base,
-                                nodes, leaf0, err);
-        else
-            small_subtree<false>(cur, s_stage[warp], s_stack[warp], s_bins[warp], ids_a, ids_b, tb, nb, leaf_size, base,
-                                 nodes, leaf0, err);
+        if ((cur.count <= kStage) != STAGED) continue;  // warp-uniform
+        small_subtree<STAGED>(cur, s_stage[STAGED ? warp : 0], s_stack[warp], s_bins[warp], ids_a, ids_b, tb, nb,
+                              leaf_size, base, nodes, leaf0, err);
     }
 }
 
@@ -1224,7 +1228,10 @@ int build_sah(const float* tris, uint32_t n, uint32_t nb, uint32_t leaf_size, in
     }
     // small phase and leaves
     const uint32_t sg = (uint32_t)sms() * 8u;
-    k_small<<<sg, 128, 0, s>>>(w.small, w.ctl, w.ids_a, w.ids_b, w.tb, (int)nb, leaf_size, base, nodes, leaf0, err);
+    // a single build's small tasks all have at most kSmall = kStage triangles
+    static_assert(kSmall <= kStage, "every small task of a single build is staged");
+    k_small<true><<<sg, 128, 0, s>>>(w.small, w.ctl, w.ids_a, w.ids_b, w.tb, (int)nb, leaf_size, base, nodes, leaf0,
+                                     err);
     k_emit_leaves<<<sg, 256, 0, s>>>(w.leaves, w.ctl, w.ids_a, w.ids_b, w.tb, nodes, leaf0, err);
     if (grid) k_grid_heap<<<1, 32, 0, s>>>(nodes);
     return (int)cudaGetLastError();
@@ -1259,7 +1266,10 @@ int build_sah_batch(const float* tris, uint32_t n, const uint32_t* off, uint32_t
         enqueue_large_level(w, level, (int)nb, 0u, leaf_size, nodes, sm * 8u, sm * 8u, n, s);
     k_large_to_small<<<sm, 256, 0, s>>>(w.lists[kBatchLargeLevels & 1], &w.ctl->n_large[kBatchLargeLevels & 1],
                                        w.small, w.ctl);
-    k_small<<<sm * 8u, 128, 0, s>>>(w.small, w.ctl, w.ids_a, w.ids_b, w.tb, (int)nb, leaf_size, 0u, nodes, leaf0, err);
+    k_small<true><<<sm * 8u, 128, 0, s>>>(w.small, w.ctl, w.ids_a, w.ids_b, w.tb, (int)nb, leaf_size, 0u, nodes, leaf0,
+                                          err);
+    k_small<false><<<sm * 8u, 128, 0, s>>>(w.small, w.ctl, w.ids_a, w.ids_b, w.tb, (int)nb, leaf_size, 0u, nodes, leaf0,
+                                           err);
     k_emit_leaves<<<sm * 8u, 256, 0, s>>>(w.leaves, w.ctl, w.ids_a, w.ids_b, w.tb, nodes, leaf0, err);
     return (int)cudaGetLastError();
 #undef SQ_TRY
