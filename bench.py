@@ -463,6 +463,31 @@ def batch_leg(ctx, flush, torch):
         out[builder] = {"autotuned": best, "graph_ms": ms, "graph_mrays_s": n_rays / ms / 1e3,
                         "graph_mtris_s": n_tris / ms / 1e3, "separate_launches_ms": sms,
                         "separate_mrays_s": n_rays / sms / 1e3, "speedup": sms / ms, "same_hits": same}
+        # the other BVH width with the autotuned settings, for comparison
+        kw = dict(builder=builder, block=best["block_threads"])
+        if builder == "sah":
+            kw["bins"] = best["sah_bins"]
+        else:
+            kw["digit_bits"] = best["sort_digit_bits"]
+        other = not best["wide"]
+        b2 = ctx.batch(descs, mode="closest", wide=other, graph=True, **kw)
+        for _ in range(3):
+            b2.run(hits=False)
+        t2 = []
+        for _ in range(5):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            b2.run(hits=False)
+            e1.record(stream)
+            e1.synchronize()
+            t2.append(e0.elapsed_time(e1))
+        got2, _ = b2.run()
+        b2.free()
+        out[builder]["other_width"] = {"wide": int(other), "graph_ms": min(t2),
+                                       "same_hits": bool(np.array_equal(got2["id"], got["id"]) and
+                                                         np.array_equal(got2["t"], got["t"]))}
     return out
 
 
