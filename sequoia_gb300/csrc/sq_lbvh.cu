@@ -162,6 +162,13 @@ __device__ void for_each_tile(const float* __restrict__ tris, uint32_t n, bool a
                 if (pending[b]) stage_wait(st, b, parity[b]);
         }
         __syncthreads();
+        return;
+    }
+    // every copy has completed: retire the barriers before the shared memory
+    // is used for anything else
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(&st.bar[0])) : "memory");
+        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(&st.bar[1])) : "memory");
     }
 }
 
