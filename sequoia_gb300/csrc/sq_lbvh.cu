@@ -572,7 +572,7 @@ __global__ void __launch_bounds__(256, 6) k_lbvh_climb(const Code* __restrict__ 
 // the second arrival merges the two and continues with the parent, whose
 // record it publishes first.  Nothing waits: a first arrival stops.
 template <class Code, bool SEG>
-__global__ void __launch_bounds__(256) k_lbvh_global(const uint32_t* __restrict__ surv,
+__global__ void __launch_bounds__(256, 6) k_lbvh_global(const uint32_t* __restrict__ surv,
                                                      const uint32_t* __restrict__ surv_count, uint32_t n,
                                                      Node* __restrict__ nodes, uint32_t* __restrict__ flags,
                                                      float4* __restrict__ info, const uint32_t* __restrict__ off,
