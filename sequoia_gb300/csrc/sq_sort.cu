@@ -13,8 +13,11 @@
 //     tiles that still fill the GPU are the fastest.  Up to 16384 keys per
 //     SM the sort is one tile per SM (blocks of 256 to 1024 threads, sized
 //     so the tiles cover every SM); beyond that 512-thread blocks, two per
-//     SM; 10-bit digits always use 256 threads (their per-warp digit counts
-//     fill shared memory);
+//     SM.  10-bit digits: per-warp counts of 1024 digits leave room for at
+//     most 26 warps beside the tile, so one tile per SM up to 13,312 keys
+//     per SM and 256-thread blocks beyond;
+//   - the pass's digit histogram and the tile's values are copied into
+//     shared memory with cp.async while the keys are ranked;
 //   - warps rank their keys by digit (stable: items are ranked in index
 //     order within the warp, warps in index order within the tile); the lanes
 //     sharing a digit come from one ballot per digit bit, which costs the
@@ -40,56 +43,70 @@ constexpr uint32_t kCountMask = (1u << 30) - 1u;
 constexpr uint32_t kSpinLimit = 1u << 22;
 constexpr int kWindow = 8;  // look-back words loaded per round
 
+// Exclusive scans of two RADIX-value arrays at once (one set of barriers);
+// in place is allowed (every input is read before any output is written).
 template <int RADIX, int MINBLOCK>
-__device__ __forceinline__ void block_exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t* s_tmp)
+__device__ __forceinline__ void block_exclusive_scan2(const uint32_t* in1, uint32_t* out1, const uint32_t* in2,
+                                                      uint32_t* out2, uint32_t* s_tmp)
 {
-    // RADIX values over the block's threads (at least MINBLOCK); each thread
-    // owns a contiguous chunk of PER values.
     const int kWarps = (int)(blockDim.x >> 5);
     constexpr int PER = (RADIX + MINBLOCK - 1) / MINBLOCK;
-    uint32_t v[PER];
-    uint32_t sum = 0;
+    uint32_t v1[PER], v2[PER];
+    uint32_t sum1 = 0, sum2 = 0;
     const int t = threadIdx.x;
 #pragma unroll
     for (int j = 0; j < PER; ++j) {
         const int d = t * PER + j;
-        v[j] = (d < RADIX) ? in[d] : 0u;
-        sum += v[j];
+        v1[j] = (d < RADIX) ? in1[d] : 0u;
+        v2[j] = (d < RADIX) ? in2[d] : 0u;
+        sum1 += v1[j];
+        sum2 += v2[j];
     }
-    // exclusive scan of per-thread sums across the block
     const int lane = t & 31, warp = t >> 5;
-    uint32_t x = sum;
+    uint32_t x1 = sum1, x2 = sum2;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-        if (lane >= o) x += y;
+        const uint32_t y1 = __shfl_up_sync(0xFFFFFFFFu, x1, o);
+        const uint32_t y2 = __shfl_up_sync(0xFFFFFFFFu, x2, o);
+        if (lane >= o) { x1 += y1; x2 += y2; }
     }
-    if (lane == 31) s_tmp[warp] = x;
+    if (lane == 31) { s_tmp[warp] = x1; s_tmp[32 + warp] = x2; }
     __syncthreads();
     if (warp == 0) {
-        uint32_t w = (lane < kWarps) ? s_tmp[lane] : 0u;
+        uint32_t w1 = (lane < kWarps) ? s_tmp[lane] : 0u, w2 = (lane < kWarps) ? s_tmp[32 + lane] : 0u;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
-            if (lane >= o) w += y;
+            const uint32_t y1 = __shfl_up_sync(0xFFFFFFFFu, w1, o);
+            const uint32_t y2 = __shfl_up_sync(0xFFFFFFFFu, w2, o);
+            if (lane >= o) { w1 += y1; w2 += y2; }
         }
-        if (lane < kWarps) s_tmp[lane] = w;
+        if (lane < kWarps) { s_tmp[lane] = w1; s_tmp[32 + lane] = w2; }
     }
     __syncthreads();
-    uint32_t run = x - sum + (warp > 0 ? s_tmp[warp - 1] : 0u);
+    uint32_t run1 = x1 - sum1 + (warp > 0 ? s_tmp[warp - 1] : 0u);
+    uint32_t run2 = x2 - sum2 + (warp > 0 ? s_tmp[32 + warp - 1] : 0u);
 #pragma unroll
     for (int j = 0; j < PER; ++j) {
         const int d = t * PER + j;
-        if (d < RADIX) out[d] = run;
-        run += v[j];
+        if (d < RADIX) { out1[d] = run1; out2[d] = run2; }
+        run1 += v1[j];
+        run2 += v2[j];
     }
     __syncthreads();
+}
+
+// 4-byte asynchronous copy global -> shared (cp.async, completed by
+// cp.async.wait_all in the issuing thread)
+__device__ __forceinline__ void cp_async4(uint32_t* dst, const uint32_t* src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
 }
 
 // dynamic shared memory of a k_onesweep block of `block` threads
 constexpr size_t smem_bytes(int db, int block)
 {
-    return sizeof(uint32_t) * (2 * (size_t)block * kItems + (size_t)(block / 32) * (1u << db) + 3 * (1u << db) + 32);
+    return sizeof(uint32_t) * (2 * (size_t)block * kItems + (size_t)(block / 32) * (1u << db) + 3 * (1u << db) + 64);
 }
 
 // MAXB: the largest block the kernel is launched with (any multiple of 32
@@ -115,7 +132,7 @@ __global__ void __launch_bounds__(MAXB, 1024 / MAXB) k_onesweep(const uint32_t* 
     uint32_t* s_gbase = s_whist + kWarps * RADIX;  // [RADIX]
     uint32_t* s_lexcl = s_gbase + RADIX;           // [RADIX]
     uint32_t* s_bcount = s_lexcl + RADIX;          // [RADIX]
-    uint32_t* s_tmp = s_bcount + RADIX;            // [32]
+    uint32_t* s_tmp = s_bcount + RADIX;            // [64]
     __shared__ uint32_t s_tile;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -125,10 +142,24 @@ __global__ void __launch_bounds__(MAXB, 1024 / MAXB) k_onesweep(const uint32_t* 
     const uint32_t tile = s_tile;
     const uint32_t base = tile * (uint32_t)kTile;
 
-    // keys stay in registers through the ranking; values are read only in
-    // the scatter (fewer registers: four blocks fit on an SM)
+    // The pass's digit histogram and the tile's values are copied into
+    // shared memory asynchronously (cp.async), so that neither load's latency
+    // falls after the look-back: the histogram into s_gbase (scanned in
+    // place), the values in tile order into s_vals (each thread copies, and
+    // later reads back, its own items).  Keys stay in registers through the
+    // ranking.
+    for (int d = tid; d < RADIX; d += kBlock) cp_async4(s_gbase + d, hist + d);
     uint32_t k[kItems], rk[kItems];
     const uint32_t wbase = base + (uint32_t)warp * (kItems * 32);
+    uint32_t* wvals = s_vals + warp * (kItems * 32);
+    if (!iota) {
+#pragma unroll
+        for (int it = 0; it < kItems; ++it) {
+            const uint32_t idx = wbase + it * 32 + lane;
+            if (idx < n) cp_async4(wvals + it * 32 + lane, vin + idx);
+        }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
 #pragma unroll
     for (int it = 0; it < kItems; ++it) {
         const uint32_t idx = wbase + it * 32 + lane;
@@ -163,17 +194,22 @@ __global__ void __launch_bounds__(MAXB, 1024 / MAXB) k_onesweep(const uint32_t* 
     // exclusive offsets across warps per digit; block counts
     for (int d = tid; d < RADIX; d += kBlock) {
         uint32_t run = 0;
-        for (int w = 0; w < kWarps; ++w) {
-            const uint32_t c = s_whist[w * RADIX + d];
-            s_whist[w * RADIX + d] = run;
-            run += c;
+        for (int w0 = 0; w0 < kWarps; w0 += 4) {
+            uint32_t c[4];  // four independent loads, then the running sum
+#pragma unroll
+            for (int q = 0; q < 4; ++q) c[q] = w0 + q < kWarps ? s_whist[(w0 + q) * RADIX + d] : 0u;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (w0 + q < kWarps) s_whist[(w0 + q) * RADIX + d] = run;
+                run += c[q];
+            }
         }
         s_bcount[d] = run;
         st_relaxed_u32(lookback + (size_t)tile * RADIX + d, (tile == 0 ? kFlagInc : kFlagAgg) | run);
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");
     __syncthreads();
-    block_exclusive_scan<RADIX, 256>(hist, s_gbase, s_tmp);
-    block_exclusive_scan<RADIX, 256>(s_bcount, s_lexcl, s_tmp);
+    block_exclusive_scan2<RADIX, 256>(s_gbase, s_gbase, s_bcount, s_lexcl, s_tmp);
     // decoupled look-back, one digit per thread (or several).  The words of
     // kWindow predecessors are loaded at once (independent relaxed loads, one
     // memory latency: each word carries its flag and count together, so no
@@ -212,16 +248,26 @@ __global__ void __launch_bounds__(MAXB, 1024 / MAXB) k_onesweep(const uint32_t* 
         s_gbase[d] += excl;
     }
     __syncthreads();
-    // local scatter in digit order
+    // local scatter in digit order: keys first (rk becomes the position),
+    // then the values, read back from s_vals before any is overwritten
 #pragma unroll
     for (int it = 0; it < kItems; ++it) {
         const uint32_t idx = wbase + it * 32 + lane;
         if (idx < n) {
             const uint32_t d = (k[it] >> shift) & MASK;
-            const uint32_t pos = s_lexcl[d] + wh[d] + rk[it];
-            s_keys[pos] = k[it];
-            s_vals[pos] = iota ? idx : vin[idx];
+            rk[it] += s_lexcl[d] + wh[d];
+            s_keys[rk[it]] = k[it];
         }
+    }
+    if (!iota) {
+#pragma unroll
+        for (int it = 0; it < kItems; ++it) k[it] = wvals[it * 32 + lane];
+        __syncthreads();
+    }
+#pragma unroll
+    for (int it = 0; it < kItems; ++it) {
+        const uint32_t idx = wbase + it * 32 + lane;
+        if (idx < n) s_vals[rk[it]] = iota ? idx : k[it];
     }
     __syncthreads();
     const uint32_t valid_count = min((uint32_t)kTile, n - base);
@@ -280,12 +326,14 @@ int sms() { return sm_count(); }
 // Threads per block of a pass over n keys (see the file comment).
 uint32_t sort_block(uint32_t n, uint32_t digit_bits)
 {
-    if (digit_bits == 10) return 256;
-    const uint64_t per_sm = (uint64_t)sms() * 1024u * kItems;
-    if ((uint64_t)n > per_sm) return 512;
+    // 10-bit digits: the per-warp counts of 1024 digits leave room for at
+    // most 26 warps beside the tile in shared memory
+    const uint64_t max_warps = digit_bits == 10 ? 26u : 32u;
+    const uint64_t per_sm = (uint64_t)sms() * 32u * max_warps * kItems;
+    if ((uint64_t)n > per_sm) return digit_bits == 10 ? 256u : 512u;
     // the fewest warps whose tiles (512 keys per warp) cover n in one tile per SM
     const uint64_t warps = ((uint64_t)n + (uint64_t)sms() * 32u * kItems - 1) / ((uint64_t)sms() * 32u * kItems);
-    return 32u * (uint32_t)std::min<uint64_t>(32, std::max<uint64_t>(8, warps));
+    return 32u * (uint32_t)std::min<uint64_t>(max_warps, std::max<uint64_t>(8, warps));
 }
 
 }  // namespace
@@ -336,7 +384,7 @@ int sort_passes(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b, uint32_t* 
         const uint32_t tb = (stall && p == 0) ? 1u : 0u;
         const bool iota = iota_values && p == 0;
         if (digit_bits == 10)
-            launch_pass<10, 256>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, spin, tb, iota, block, s);
+            launch_pass<10, 832>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, spin, tb, iota, block, s);
         else if (digit_bits == 8)
             launch_pass<8, 1024>(kin, vin, kout, vout, n, shift, h, lb, counters + p, err, spin, tb, iota, block, s);
         else

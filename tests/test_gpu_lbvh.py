@@ -32,10 +32,11 @@ def test_morton_codes_golden(ctx, name):
 
 
 # tile edges of every tile size (4096, 8192 and 16384 keys), and sizes on
-# both sides of the switch from 16384- to 8192-key tiles (at 16384 keys per
-# SM: 2,490,368 on a 152-SM GB300)
+# both sides of the switch from one tile per SM to smaller tiles (on a 152-SM
+# GB300: 2,490,368 keys for 8-bit digits, 16384 per SM; 2,023,424 for 10-bit
+# digits, 13,312 per SM)
 @pytest.mark.parametrize("n", [1, 2, 7, 8, 9, 255, 256, 257, 4095, 4096, 4097, 8191, 8192, 8193, 16383, 16384, 16385,
-                               100_003, 1_000_000, 2_490_368, 2_490_369, 3_000_017])
+                               100_003, 1_000_000, 2_000_000, 2_023_424, 2_023_425, 2_490_368, 2_490_369, 3_000_017])
 @pytest.mark.parametrize("digit_bits", [6, 8, 10])
 def test_radix_sort_random(ctx, oracle, n, digit_bits):
     rng = np.random.default_rng(n + digit_bits)
