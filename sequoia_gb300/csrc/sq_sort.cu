@@ -103,6 +103,15 @@ __device__ __forceinline__ void cp_async4(uint32_t* dst, const uint32_t* src)
                  : "memory");
 }
 
+// 16-byte asynchronous copy global -> shared of which the first `bytes`
+// (<= 16) are read and the rest zero-filled; both addresses 16-byte aligned
+__device__ __forceinline__ void cp_async16(uint32_t* dst, const uint32_t* src, uint32_t bytes)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(src), "r"(bytes)
+                 : "memory");
+}
+
 // dynamic shared memory of a k_onesweep block of `block` threads
 constexpr size_t smem_bytes(int db, int block)
 {
@@ -153,10 +162,21 @@ __global__ void __launch_bounds__(MAXB, 1024 / MAXB) k_onesweep(const uint32_t* 
     const uint32_t wbase = base + (uint32_t)warp * (kItems * 32);
     uint32_t* wvals = s_vals + warp * (kItems * 32);
     if (!iota) {
+        if ((reinterpret_cast<uintptr_t>(vin) & 15u) == 0) {
+            // the warp's kItems * 32 values as 16-byte chunks, four per lane
+            // (a chunk past n is not copied; one that straddles it copies
+            // only the values before n)
 #pragma unroll
-        for (int it = 0; it < kItems; ++it) {
-            const uint32_t idx = wbase + it * 32 + lane;
-            if (idx < n) cp_async4(wvals + it * 32 + lane, vin + idx);
+            for (int c = 0; c < kItems / 4; ++c) {
+                const uint32_t e = (uint32_t)(c * 32 + lane) * 4u;
+                if (wbase + e < n) cp_async16(wvals + e, vin + wbase + e, min(4u, n - wbase - e) * 4u);
+            }
+        } else {
+#pragma unroll
+            for (int it = 0; it < kItems; ++it) {
+                const uint32_t idx = wbase + it * 32 + lane;
+                if (idx < n) cp_async4(wvals + it * 32 + lane, vin + idx);
+            }
         }
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
@@ -270,13 +290,25 @@ __global__ void __launch_bounds__(MAXB, 1024 / MAXB) k_onesweep(const uint32_t* 
         if (idx < n) s_vals[rk[it]] = iota ? idx : k[it];
     }
     __syncthreads();
+    // kItems rounds (a tile holds kItems * kBlock keys).  A block that is
+    // alone on its SM unrolls them by four so that the rounds' shared-memory
+    // loads overlap; with two blocks per SM the plain loop is faster.
     const uint32_t valid_count = min((uint32_t)kTile, n - base);
-    for (uint32_t j = tid; j < valid_count; j += kBlock) {
+    auto write_out = [&](uint32_t j) {
         const uint32_t key = s_keys[j];
         const uint32_t d = (key >> shift) & MASK;
         const uint32_t gp = s_gbase[d] + (j - s_lexcl[d]);
         kout[gp] = key;
         vout[gp] = s_vals[j];
+    };
+    if (kBlock > 512) {
+#pragma unroll 4
+        for (int it = 0; it < kItems; ++it) {
+            const uint32_t j = (uint32_t)(tid + it * kBlock);
+            if (j < valid_count) write_out(j);
+        }
+    } else {
+        for (uint32_t j = tid; j < valid_count; j += kBlock) write_out(j);
     }
 }
 
